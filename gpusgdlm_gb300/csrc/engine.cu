@@ -1,0 +1,1005 @@
+// The SGDLM engine behind the C ABI of include/sgdlm.h.
+//
+// Plays the role of the reference's SGDLM::HostWrapperImpl<double>
+// (rSGDLM/src/SGDLM/HostWrapperImpl.cu): owns the device state, the simulation
+// buffers and the stream, enforces the prior/posterior state machine, and
+// sequences the kernels of each filtering call.  Differences by design:
+//   * one GPU (no per-device loops, no host-side combine of per-GPU moments);
+//   * flat, strided buffers instead of device pointer arrays;
+//   * draw buffers are series-major and no random-number caches exist (Philox
+//     in registers), so simulation memory is lambda + theta + one LU slab per
+//     resident CTA instead of 2*nsim_batch dense m x m matrices;
+//   * nsim_batch is accepted and reported for API compatibility; it does not
+//     change results (neither does it in the reference) nor memory here.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <set>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/sgdlm.h"
+#include "kernels.hpp"
+
+using namespace sgdlm;
+
+namespace {
+
+// Levels and default of the reference's logger (rSGDLM/src/logger.hpp:16-30,
+// logger.cpp:11).
+enum LogLevel { LOG_ERROR = 0, LOG_WARNING = 5, LOG_INFO = 10, LOG_RESULT = 20, LOG_DEBUG = 50, LOG_SYSDEBUG = 100 };
+
+template <typename T> struct DevBuf {
+  T *ptr = nullptr;
+  size_t count = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  cudaError_t alloc(size_t n) {
+    release();
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&ptr, n * sizeof(T));
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return e;
+    }
+    count = n;
+    return cudaMemset(ptr, 0, n * sizeof(T));
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    count = 0;
+  }
+};
+
+constexpr size_t kMaxP = 64;
+
+}  // namespace
+
+struct sgdlm_engine {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  size_t no_gpus = 1;
+  size_t m = 0, P = 0;
+  bool mem_init = false, sim_init = false, is_prior = false;
+  size_t nsim = 0, nsim_batch = 0;
+  int precision = SGDLM_PRECISION_MIXED;
+  unsigned compat = SGDLM_COMPAT_REFERENCE;
+  uint64_t seed = 1234;  // HostWrapperImpl.cu:63-64 seeds device 0 with 1234
+  uint64_t epoch = 0;
+  int log_level = LOG_RESULT;
+  std::string last_error;
+  uint64_t launches = 0;
+  sgdlm_stats stats{};
+
+  // state
+  DevBuf<double> m_t, C_t, n_t, s_t, W_t, beta, delta;
+  DevBuf<unsigned> p, sp;
+  DevBuf<int> g_rowptr;
+  DevBuf<int2> g_ent;
+  DevBuf<double> y_t, F_t, x_t;
+  DevBuf<double> fm_t, fC_t, fn_t, fs_t, fW_t;
+  DevBuf<double> U64;
+  DevBuf<float> U32;
+  std::vector<unsigned> h_p, h_sp;
+  // simulation
+  DevBuf<unsigned char> lambda, theta, lu_scratch;
+  DevBuf<double> logdet, w, y_fc, stats6, part_a, part_b;
+  DevBuf<int> draw_flags, series_flags;
+  DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
+  DevBuf<uint32_t> dev_epoch;
+  LuPlan plan{};
+  int chunks = 0;
+  cudaEvent_t ev[8] = {};
+
+  void log(int level, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (level == LOG_ERROR) last_error = buf;
+    if (level <= log_level)
+      fprintf(stderr, "%s%s\n",
+              level == LOG_ERROR ? "Error: " : (level == LOG_WARNING ? "Warning: " : ""), buf);
+  }
+  int fail(int status, const char *msg) {
+    log(LOG_ERROR, "%s", msg);
+    return status;
+  }
+  int cuda_fail(cudaError_t e, const char *where) {
+    char buf[256];
+    snprintf(buf, sizeof buf, "CUDA error in %s: %s", where, cudaGetErrorString(e));
+    log(LOG_ERROR, "%s", buf);
+    return e == cudaErrorMemoryAllocation ? SGDLM_ERR_OUT_OF_MEMORY : SGDLM_ERR_DEVICE;
+  }
+  // HostWrapperImpl.cu:1240-1246
+  bool check_initialized() {
+    if (!mem_init) {
+      log(LOG_ERROR, "The device memory is not initialized.");
+      return false;
+    }
+    return true;
+  }
+  // HostWrapperImpl.cu:1249-1255
+  bool check_sim_initialized() {
+    if (!sim_init) {
+      log(LOG_ERROR, "The simulation device memory is not initialized.");
+      return false;
+    }
+    return true;
+  }
+  // HostWrapperImpl.cu:1268-1286
+  bool check_prior(bool want_prior) {
+    if (want_prior && !is_prior) {
+      log(LOG_ERROR, "This function can only be executed when the parameters are prior parameters.");
+      return false;
+    }
+    if (!want_prior && is_prior) {
+      log(LOG_ERROR, "This function can only be executed when the parameters are posterior parameters.");
+      return false;
+    }
+    return true;
+  }
+  size_t tsize() const { return precision == SGDLM_PRECISION_FP64 ? sizeof(double) : sizeof(float); }
+  RngKey key(uint32_t ep) const {
+    return RngKey{(uint32_t)(seed & 0xffffffffu), (uint32_t)(seed >> 32), ep, nullptr};
+  }
+};
+
+namespace {
+
+#define CK(expr)                                                     \
+  do {                                                               \
+    cudaError_t _e = (expr);                                         \
+    if (_e != cudaSuccess) return h->cuda_fail(_e, #expr);           \
+  } while (0)
+
+int h2d(sgdlm_engine *h, void *dst, const void *src, size_t bytes) {
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
+  return SGDLM_OK;
+}
+int d2h(sgdlm_engine *h, void *dst, const void *src, size_t bytes) {
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+  return SGDLM_OK;
+}
+int sync(sgdlm_engine *h) {
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaGetLastError());
+  return SGDLM_OK;
+}
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+// Row-wise CSR of the Gamma entries (see GammaRows), from the host copy of sp.
+int upload_gamma_rows(sgdlm_engine *h) {
+  const size_t m = h->m, P = h->P, mm = m * m;
+  std::vector<int> rowptr(m + 1, 0);
+  std::vector<int2> ent;
+  for (size_t e = 0; e < m * P; ++e)
+    if ((size_t)h->h_sp[e] < mm) rowptr[h->h_sp[e] % m + 1]++;
+  for (size_t r = 0; r < m; ++r) rowptr[r + 1] += rowptr[r];
+  ent.resize(rowptr[m] > 0 ? rowptr[m] : 1);
+  std::vector<int> fill(rowptr.begin(), rowptr.end() - 1);
+  for (size_t e = 0; e < m * P; ++e) {
+    const unsigned pos = h->h_sp[e];
+    if ((size_t)pos < mm) ent[fill[pos % m]++] = make_int2((int)e, (int)(pos / m));
+  }
+  CK(h->g_rowptr.alloc(m + 1));
+  CK(h->g_ent.alloc(ent.size()));
+  CK(cudaMemcpy(h->g_rowptr.ptr, rowptr.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->g_ent.ptr, ent.data(), ent.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  return SGDLM_OK;
+}
+
+int alloc_state(sgdlm_engine *h) {
+  const size_t m = h->m, P = h->P;
+  CK(h->m_t.alloc(P * m));
+  CK(h->C_t.alloc(P * P * m));
+  CK(h->n_t.alloc(m));
+  CK(h->s_t.alloc(m));
+  CK(h->W_t.alloc(P * P * m));
+  CK(h->beta.alloc(m));
+  CK(h->delta.alloc(P * P * m));
+  CK(h->p.alloc(m));
+  CK(h->sp.alloc(P * m));
+  CK(h->y_t.alloc(m));
+  CK(h->F_t.alloc(P * m));
+  CK(h->x_t.alloc(P * m));
+  CK(h->fm_t.alloc(P * m));
+  CK(h->fC_t.alloc(P * P * m));
+  CK(h->fn_t.alloc(m));
+  CK(h->fs_t.alloc(m));
+  CK(h->fW_t.alloc(P * P * m));
+  CK(h->U64.alloc(P * P * m));
+  CK(h->U32.alloc(P * P * m));
+  CK(h->mean_m.alloc(P * m));
+  CK(h->mean_C.alloc(P * P * m));
+  CK(h->mean_n.alloc(m));
+  CK(h->mean_s.alloc(m));
+  CK(h->mean_lambda.alloc(m));
+  CK(h->mean_log_lambda.alloc(m));
+  CK(h->mean_Q.alloc(m));
+  CK(h->series_flags.alloc(m));
+  CK(h->stats6.alloc(8));
+  CK(h->dev_epoch.alloc(1));
+  h->h_p.assign(m, 0);
+  h->h_sp.assign(P * m, 0xFFFFFFFFu);
+  // Parental sets default to "no simultaneous parents" (all external).
+  CK(cudaMemcpy(h->sp.ptr, h->h_sp.data(), P * m * sizeof(unsigned), cudaMemcpyHostToDevice));
+  return upload_gamma_rows(h);
+}
+
+void release_sim(sgdlm_engine *h) {
+  h->lambda.release();
+  h->theta.release();
+  h->lu_scratch.release();
+  h->logdet.release();
+  h->w.release();
+  h->y_fc.release();
+  h->part_a.release();
+  h->part_b.release();
+  h->draw_flags.release();
+  h->sim_init = false;
+  h->nsim = 0;
+  h->nsim_batch = 0;
+}
+
+void release_all(sgdlm_engine *h) {
+  release_sim(h);
+  for (auto *b : {&h->m_t, &h->C_t, &h->n_t, &h->s_t, &h->W_t, &h->beta, &h->delta, &h->y_t,
+                  &h->F_t, &h->x_t, &h->fm_t, &h->fC_t, &h->fn_t, &h->fs_t, &h->fW_t,
+                  &h->U64, &h->mean_m, &h->mean_C, &h->mean_n, &h->mean_s, &h->mean_lambda,
+                  &h->mean_log_lambda, &h->mean_Q, &h->stats6})
+    b->release();
+  h->U32.release();
+  h->p.release();
+  h->sp.release();
+  h->g_rowptr.release();
+  h->g_ent.release();
+  h->series_flags.release();
+  h->dev_epoch.release();
+  h->mem_init = false;
+}
+
+int plan_sim(sgdlm_engine *h, long n, LuPlan *out) {
+  LuPlan pl = (h->precision == SGDLM_PRECISION_FP64)
+                  ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms)
+                  : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms);
+  if (pl.smem > 227 * 1024) {
+    char buf[200];
+    snprintf(buf, sizeof buf,
+             "m = %zu needs %zu bytes of shared memory per LU block at this precision "
+             "(limit 232448); use the mixed precision or a smaller m",
+             h->m, pl.smem);
+    return h->fail(SGDLM_ERR_UNSUPPORTED, buf);
+  }
+  *out = pl;
+  return SGDLM_OK;
+}
+
+int alloc_sim(sgdlm_engine *h, size_t nsim) {
+  const size_t m = h->m, P = h->P, ts = h->tsize();
+  LuPlan pl;
+  int st = plan_sim(h, (long)nsim, &pl);
+  if (st) return st;
+  release_sim(h);
+  h->plan = pl;
+  h->chunks = (int)vb_chunks((long)nsim);
+  CK(h->lambda.alloc(m * nsim * ts));
+  CK(h->theta.alloc(m * nsim * P * ts));
+  CK(h->lu_scratch.alloc((size_t)pl.grid * pl.scratch_elems_per_cta * ts));
+  CK(h->logdet.alloc(nsim));
+  CK(h->w.alloc(nsim));
+  CK(h->y_fc.alloc(nsim * m));
+  CK(h->draw_flags.alloc(nsim));
+  CK(h->part_a.alloc((size_t)h->chunks * m * (P + 2) + m * P));
+  CK(h->part_b.alloc((size_t)h->chunks * m * P * P));
+  h->nsim = nsim;
+  return SGDLM_OK;
+}
+
+// Validates a parental set: p_j <= P, and the Gamma positions (sp < m*m) hit
+// off-diagonal cells at most once.  The reference does not check; a diagonal
+// position races with fillGammas' unit diagonal (kernel_functions.cuh:830-840)
+// and a repeated one with itself, so both are rejected here.
+int validate_parents(sgdlm_engine *h, const unsigned *p, const unsigned *sp) {
+  const size_t m = h->m, P = h->P, mm = m * m;
+  if (p)
+    for (size_t j = 0; j < m; ++j)
+      if (p[j] > P) return h->fail(SGDLM_ERR_BAD_ARG, "p[j] exceeds max_p");
+  if (sp) {
+    std::set<unsigned> seen;
+    for (size_t e = 0; e < m * P; ++e) {
+      const unsigned pos = sp[e];
+      if ((size_t)pos >= mm) continue;
+      if (pos % m == pos / m)
+        return h->fail(SGDLM_ERR_BAD_ARG, "sp addresses a diagonal entry of (I - Gamma)");
+      if (!seen.insert(pos).second)
+        return h->fail(SGDLM_ERR_BAD_ARG, "sp addresses the same entry of (I - Gamma) twice");
+    }
+  }
+  return SGDLM_OK;
+}
+
+template <typename T> T *as(DevBuf<unsigned char> &b) { return reinterpret_cast<T *>(b.ptr); }
+
+// sample -> LU -> fallback, from the given normal-gamma parameters (posterior
+// for VB, forecasting prior for forecasts).
+template <typename T>
+void sample_draws(sgdlm_engine *h, const double *m_t, const double *C_t, const double *n_t,
+                  const double *s_t, RngKey key) {
+  const int m = (int)h->m, P = (int)h->P;
+  const long n = (long)h->nsim;
+  launch_cholesky(h->stream, m, P, h->p.ptr, C_t, h->U64.ptr, h->U32.ptr);
+  const T *U = std::is_same<T, float>::value ? reinterpret_cast<const T *>(h->U32.ptr)
+                                              : reinterpret_cast<const T *>(h->U64.ptr);
+  launch_sample<T>(h->stream, m, P, n, m_t, n_t, s_t, U, key, as<T>(h->lambda), as<T>(h->theta),
+                   h->draw_flags.ptr);
+  h->launches += 2;
+}
+
+template <typename T>
+void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
+  const long n = (long)h->nsim;
+  const bool refine = (h->precision != SGDLM_PRECISION_FP64);
+  const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr};
+  launch_lu<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta), as<T>(h->lu_scratch),
+               h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key, refine, y, rows);
+  launch_lu_fallback<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta),
+                        as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
+                        as<T>(h->lambda), key, y, rows);
+  h->launches += 2;
+}
+
+template <typename T> void vb_moments(sgdlm_engine *h, double *w) {
+  const int m = (int)h->m, P = (int)h->P;
+  const long n = (long)h->nsim;
+  VbScratch scr{h->part_a.ptr, h->part_b.ptr, h->chunks, 0};
+  launch_vb<T>(h->stream, m, P, n, h->p.ptr, h->n_t.ptr, h->s_t.ptr, w, as<T>(h->lambda),
+               as<T>(h->theta), scr, h->mean_m.ptr, h->mean_C.ptr, h->mean_n.ptr,
+               h->mean_s.ptr, h->mean_lambda.ptr, h->mean_log_lambda.ptr, h->mean_Q.ptr,
+               h->series_flags.ptr);
+  h->launches += 4;
+}
+
+// Reads back the per-draw and per-series status words into the stats block.
+int collect_flags(sgdlm_engine *h, bool with_series) {
+  std::vector<int> f(h->nsim);
+  CK(cudaMemcpyAsync(f.data(), h->draw_flags.ptr, h->nsim * sizeof(int), cudaMemcpyDeviceToHost,
+                     h->stream));
+  std::vector<int> sf;
+  if (with_series) {
+    sf.resize(h->m);
+    CK(cudaMemcpyAsync(sf.data(), h->series_flags.ptr, h->m * sizeof(int),
+                       cudaMemcpyDeviceToHost, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  uint64_t piv = 0, sing = 0, cap = 0, newton = 0;
+  for (int v : f) {
+    piv += (v & DRAW_FLAG_REDONE) ? 1 : 0;
+    sing += (v & DRAW_FLAG_SINGULAR) ? 1 : 0;
+    cap += (v & DRAW_FLAG_GAMMA_CAP) ? 1 : 0;
+  }
+  for (int v : sf) newton += (v & 2) ? 1 : 0;
+  h->stats.draws_pivoted = piv;
+  h->stats.draws_singular = sing;
+  h->stats.gamma_cap_hits = cap;
+  if (with_series) h->stats.newton_fallbacks = newton;
+  if (sing) h->log(LOG_WARNING, "%llu draws had a singular (I - Gamma)", (unsigned long long)sing);
+  if (cap) h->log(LOG_WARNING, "%llu gamma draws hit the sampler's attempt cap", (unsigned long long)cap);
+  return SGDLM_OK;
+}
+
+template <typename T>
+int vb_posterior(sgdlm_engine *h, double *o_m, double *o_C, double *o_n, double *o_s,
+                 double *o_w, double *o_sum) {
+  const size_t m = h->m, P = h->P, n = h->nsim;
+  cudaStream_t s = h->stream;
+  const RngKey key = h->key((uint32_t)h->epoch);
+  h->epoch += 1;
+  CK(cudaEventRecord(h->ev[0], s));
+  CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
+  sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, key);
+  CK(cudaEventRecord(h->ev[1], s));
+  lu_draws<T>(h, nullptr, key, nullptr);
+  CK(cudaEventRecord(h->ev[2], s));
+  launch_weights(s, (long)n, h->logdet.ptr, h->w.ptr, h->stats6.ptr);
+  h->launches += 1;
+  CK(cudaEventRecord(h->ev[3], s));
+  vb_moments<T>(h, h->w.ptr);
+  CK(cudaEventRecord(h->ev[4], s));
+  int st;
+  if (o_m && (st = d2h(h, o_m, h->mean_m.ptr, P * m * sizeof(double)))) return st;
+  if (o_C && (st = d2h(h, o_C, h->mean_C.ptr, P * P * m * sizeof(double)))) return st;
+  if (o_n && (st = d2h(h, o_n, h->mean_n.ptr, m * sizeof(double)))) return st;
+  if (o_s && (st = d2h(h, o_s, h->mean_s.ptr, m * sizeof(double)))) return st;
+  if (o_w && (st = d2h(h, o_w, h->w.ptr, n * sizeof(double)))) return st;
+  double st6[8];
+  if ((st = d2h(h, st6, h->stats6.ptr, 6 * sizeof(double)))) return st;
+  if ((st = sync(h))) return st;
+  if (o_sum) *o_sum = st6[0];
+  h->stats.sum_det_weights = st6[0];
+  h->stats.ess = st6[1];
+  h->stats.max_log_det = st6[2];
+  h->stats.ms_sample = elapsed(h->ev[0], h->ev[1]);
+  h->stats.ms_lu = elapsed(h->ev[1], h->ev[2]);
+  h->stats.ms_weights = elapsed(h->ev[2], h->ev[3]);
+  h->stats.ms_vb = elapsed(h->ev[3], h->ev[4]);
+  h->stats.ms_total = elapsed(h->ev[0], h->ev[4]);
+  return collect_flags(h, true);
+}
+
+template <typename T>
+int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, double *o_theta,
+             bool use_existing) {
+  const size_t m = h->m, P = h->P, n = h->nsim;
+  cudaStream_t s = h->stream;
+  int st;
+  if ((st = h2d(h, h->x_t.ptr, x, P * m * sizeof(double)))) return st;
+  const RngKey key = h->key((uint32_t)h->epoch);
+  h->epoch += 1;
+  CK(cudaEventRecord(h->ev[0], s));
+  CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
+  if (!use_existing)
+    sample_draws<T>(h, h->fm_t.ptr, h->fC_t.ptr, h->fn_t.ptr, h->fs_t.ptr, key);
+  CK(cudaEventRecord(h->ev[1], s));
+  lu_draws<T>(h, h->x_t.ptr, key, h->y_fc.ptr);
+  CK(cudaEventRecord(h->ev[2], s));
+  if (o_y && (st = d2h(h, o_y, h->y_fc.ptr, n * m * sizeof(double)))) return st;
+  std::vector<T> lam, th;
+  if (o_lambda) {
+    lam.resize(m * n);
+    if ((st = d2h(h, lam.data(), h->lambda.ptr, m * n * sizeof(T)))) return st;
+  }
+  if (o_theta) {
+    th.resize(m * n * P);
+    if ((st = d2h(h, th.data(), h->theta.ptr, m * n * P * sizeof(T)))) return st;
+  }
+  if ((st = sync(h))) return st;
+  // debug exports use the reference's draw-major layouts:
+  // lambdas (m, nsim), thetas (max_p, m, nsim)   (RcppWrapper.cpp:557-569)
+  if (o_lambda)
+    for (size_t j = 0; j < m; ++j)
+      for (size_t i = 0; i < n; ++i) o_lambda[i * m + j] = (double)lam[j * n + i];
+  if (o_theta)
+    for (size_t j = 0; j < m; ++j)
+      for (size_t i = 0; i < n; ++i)
+        for (size_t k = 0; k < P; ++k) o_theta[(i * m + j) * P + k] = (double)th[(j * n + i) * P + k];
+  h->stats.ms_sample = elapsed(h->ev[0], h->ev[1]);
+  h->stats.ms_lu_forecast = elapsed(h->ev[1], h->ev[2]);
+  h->stats.ms_total = elapsed(h->ev[0], h->ev[2]);
+  return collect_flags(h, false);
+}
+
+template <typename T> int evolve(sgdlm_engine *h) {
+  const int m = (int)h->m, P = (int)h->P;
+  const long n = (long)h->nsim;
+  const RngKey key = h->key((uint32_t)h->epoch);
+  h->epoch += 1;
+  // chol(W) of the forecasting copy (SGDLM.cu:742-747); the forecasting r, c and
+  // W are not re-discounted between steps (HostWrapperImpl.cu:891-900)
+  launch_cholesky(h->stream, m, P, h->p.ptr, h->fW_t.ptr, h->U64.ptr, h->U32.ptr);
+  const T *UW = std::is_same<T, float>::value ? reinterpret_cast<const T *>(h->U32.ptr)
+                                               : reinterpret_cast<const T *>(h->U64.ptr);
+  launch_evolve<T>(h->stream, m, P, n, h->p.ptr, h->fn_t.ptr, h->fs_t.ptr, h->beta.ptr, UW,
+                   key, (h->compat & SGDLM_COMPAT_UNSCALED_EVOLUTION) != 0,
+                   (h->compat & SGDLM_COMPAT_BETA_NO_BOOST) != 0, as<T>(h->lambda),
+                   as<T>(h->theta), h->draw_flags.ptr);
+  h->launches += 2;
+  return sync(h);
+}
+
+int copy_forecast_priors(sgdlm_engine *h) {
+  const size_t m = h->m, P = h->P;
+  cudaStream_t s = h->stream;
+  CK(cudaMemcpyAsync(h->fn_t.ptr, h->n_t.ptr, m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->fs_t.ptr, h->s_t.ptr, m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->fm_t.ptr, h->m_t.ptr, P * m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->fC_t.ptr, h->C_t.ptr, P * P * m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->fW_t.ptr, h->W_t.ptr, P * P * m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return SGDLM_OK;
+}
+
+// Fused step body; every launch on the stream, no host synchronisation.
+template <typename T>
+int filter_step(sgdlm_engine *h, const double *d_y, const double *d_F, const double *d_x,
+                double ess_threshold, double *d_forecast, double *d_w, double *d_stats) {
+  const int m = (int)h->m, P = (int)h->P;
+  const long n = (long)h->nsim;
+  cudaStream_t s = h->stream;
+  RngKey key_vb = h->key(0);
+  key_vb.dev_epoch = h->dev_epoch.ptr;
+  RngKey key_fc = h->key(1);
+  key_fc.dev_epoch = h->dev_epoch.ptr;
+  double *w = d_w ? d_w : h->w.ptr;
+  double *yout = d_forecast ? d_forecast : h->y_fc.ptr;
+  launch_posterior(s, m, P, h->p.ptr, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, d_y, d_F);
+  h->launches += 1;
+  CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
+  sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, key_vb);
+  lu_draws<T>(h, nullptr, key_vb, nullptr);
+  launch_weights(s, n, h->logdet.ptr, w, h->stats6.ptr);
+  vb_moments<T>(h, w);
+  launch_gate(s, m, P, h->stats6.ptr, ess_threshold, h->mean_m.ptr, h->mean_C.ptr,
+              h->mean_n.ptr, h->mean_s.ptr, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr,
+              h->stats6.ptr + 6);
+  launch_prior(s, m, P, h->p.ptr, h->C_t.ptr, h->n_t.ptr, h->W_t.ptr, h->beta.ptr, h->delta.ptr);
+  h->launches += 3;
+  if (d_x) {
+    int st = copy_forecast_priors(h);
+    if (st) return st;
+    CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
+    sample_draws<T>(h, h->fm_t.ptr, h->fC_t.ptr, h->fn_t.ptr, h->fs_t.ptr, key_fc);
+    lu_draws<T>(h, d_x, key_fc, yout);
+  }
+  if (d_stats) {
+    // {ESS, sum_det, accepted, max_log_det, n_finite, sum_w2}
+    CK(cudaMemcpyAsync(d_stats + 0, h->stats6.ptr + 1, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_stats + 1, h->stats6.ptr + 0, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_stats + 2, h->stats6.ptr + 6, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(d_stats + 3, h->stats6.ptr + 2, 3 * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  launch_advance_epoch(s, h->dev_epoch.ptr, 2);
+  h->launches += 1;
+  h->epoch += 2;  // host copy follows the device counter (one call = one advance)
+  CK(cudaGetLastError());
+  return SGDLM_OK;
+}
+
+template <typename T>
+int export_draws(sgdlm_engine *h, double *o_lambda, double *o_theta, double *o_logdet) {
+  const size_t m = h->m, P = h->P, n = h->nsim;
+  std::vector<T> lam, th;
+  int st;
+  if (o_lambda) {
+    lam.resize(m * n);
+    if ((st = d2h(h, lam.data(), h->lambda.ptr, m * n * sizeof(T)))) return st;
+  }
+  if (o_theta) {
+    th.resize(m * n * P);
+    if ((st = d2h(h, th.data(), h->theta.ptr, m * n * P * sizeof(T)))) return st;
+  }
+  if (o_logdet && (st = d2h(h, o_logdet, h->logdet.ptr, n * sizeof(double)))) return st;
+  if ((st = sync(h))) return st;
+  if (o_lambda)
+    for (size_t j = 0; j < m; ++j)
+      for (size_t i = 0; i < n; ++i) o_lambda[i * m + j] = (double)lam[j * n + i];
+  if (o_theta)
+    for (size_t j = 0; j < m; ++j)
+      for (size_t i = 0; i < n; ++i)
+        for (size_t k = 0; k < P; ++k) o_theta[(i * m + j) * P + k] = (double)th[(j * n + i) * P + k];
+  return SGDLM_OK;
+}
+
+}  // namespace
+
+#define HCHECK(h)                                  \
+  do {                                             \
+    if (!(h)) return SGDLM_ERR_BAD_ARG;            \
+    cudaSetDevice((h)->device);                    \
+  } while (0)
+
+extern "C" {
+
+int sgdlm_create(size_t no_gpus, sgdlm_handle *out) {
+  if (!out) return SGDLM_ERR_BAD_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    fprintf(stderr, "[sgdlm] No cuda-enabled devices available.\n");
+    return SGDLM_ERR_NO_DEVICE;
+  }
+  auto h = std::make_unique<sgdlm_engine>();
+  h->device = 0;
+  if (no_gpus != 1)
+    h->log(LOG_INFO, "no_gpus = %zu requested; this engine runs on one GPU", no_gpus);
+  h->no_gpus = 1;
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&h->ev[k]);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "[sgdlm] CUDA initialisation failed: %s\n", cudaGetErrorString(e));
+    return SGDLM_ERR_DEVICE;
+  }
+  *out = h.release();
+  return SGDLM_OK;
+}
+
+int sgdlm_destroy(sgdlm_handle h) {
+  if (!h) return SGDLM_OK;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  release_all(h);
+  for (auto &e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return SGDLM_OK;
+}
+
+int sgdlm_init_memory(sgdlm_handle h, size_t m, size_t max_p) {
+  HCHECK(h);
+  if (m < 1 || max_p < 1) return h->fail(SGDLM_ERR_BAD_DIM, "m and max_p must be positive");
+  if (max_p > kMaxP) return h->fail(SGDLM_ERR_UNSUPPORTED, "max_p above 64 is not supported");
+  if (m > 65535) return h->fail(SGDLM_ERR_UNSUPPORTED, "m above 65535 does not fit the sp encoding");
+  cudaStreamSynchronize(h->stream);
+  release_all(h);
+  h->m = m;
+  h->P = max_p;
+  int st = alloc_state(h);
+  if (st) {
+    release_all(h);
+    return st;
+  }
+  h->mem_init = true;
+  return SGDLM_OK;
+}
+
+int sgdlm_clear_memory(sgdlm_handle h) {
+  HCHECK(h);
+  cudaStreamSynchronize(h->stream);
+  release_all(h);
+  return SGDLM_OK;
+}
+
+int sgdlm_get_no_series(sgdlm_handle h, size_t *m) {
+  HCHECK(h);
+  if (!m) return SGDLM_ERR_BAD_ARG;
+  *m = h->m;
+  return SGDLM_OK;
+}
+int sgdlm_get_max_p(sgdlm_handle h, size_t *max_p) {
+  HCHECK(h);
+  if (!max_p) return SGDLM_ERR_BAD_ARG;
+  *max_p = h->P;
+  return SGDLM_OK;
+}
+int sgdlm_get_no_gpus(sgdlm_handle h, size_t *no_gpus) {
+  HCHECK(h);
+  if (!no_gpus) return SGDLM_ERR_BAD_ARG;
+  *no_gpus = h->no_gpus;
+  return SGDLM_OK;
+}
+
+// initSimMemory (HostWrapperImpl.cu:321-332): nsim_batch is clamped to nsim.
+int sgdlm_init_sim_memory(sgdlm_handle h, size_t nsim, size_t nsim_batch) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (nsim < 1) return h->fail(SGDLM_ERR_BAD_ARG, "nsim must be positive");
+  if (nsim > 0x7FFFFFFFu) return h->fail(SGDLM_ERR_UNSUPPORTED, "nsim above 2^31 - 1 is not supported");
+  cudaStreamSynchronize(h->stream);
+  int st = alloc_sim(h, nsim);
+  if (st) {
+    release_sim(h);
+    return st;
+  }
+  h->nsim_batch = nsim_batch > nsim ? nsim : nsim_batch;
+  h->sim_init = true;
+  return SGDLM_OK;
+}
+
+int sgdlm_clear_sim_memory(sgdlm_handle h) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  cudaStreamSynchronize(h->stream);
+  release_sim(h);
+  return SGDLM_OK;
+}
+
+int sgdlm_get_nsim(sgdlm_handle h, size_t *nsim) {
+  HCHECK(h);
+  if (!nsim) return SGDLM_ERR_BAD_ARG;
+  *nsim = h->nsim;
+  return SGDLM_OK;
+}
+int sgdlm_get_nsim_batch(sgdlm_handle h, size_t *nsim_batch) {
+  HCHECK(h);
+  if (!nsim_batch) return SGDLM_ERR_BAD_ARG;
+  *nsim_batch = h->nsim_batch;
+  return SGDLM_OK;
+}
+int sgdlm_is_prior(sgdlm_handle h, int *is_prior) {
+  HCHECK(h);
+  if (!is_prior) return SGDLM_ERR_BAD_ARG;
+  *is_prior = h->is_prior ? 1 : 0;
+  return SGDLM_OK;
+}
+int sgdlm_set_is_prior(sgdlm_handle h, int is_prior) {
+  HCHECK(h);
+  h->is_prior = is_prior != 0;
+  return SGDLM_OK;
+}
+
+int sgdlm_get_parameters(sgdlm_handle h, double *m_t, double *C_t, double *n_t, double *s_t) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  const size_t m = h->m, P = h->P;
+  int st;
+  if (m_t && (st = d2h(h, m_t, h->m_t.ptr, P * m * sizeof(double)))) return st;
+  if (C_t && (st = d2h(h, C_t, h->C_t.ptr, P * P * m * sizeof(double)))) return st;
+  if (n_t && (st = d2h(h, n_t, h->n_t.ptr, m * sizeof(double)))) return st;
+  if (s_t && (st = d2h(h, s_t, h->s_t.ptr, m * sizeof(double)))) return st;
+  return sync(h);
+}
+
+int sgdlm_set_parameters(sgdlm_handle h, const double *m_t, const double *C_t,
+                         const double *n_t, const double *s_t) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  const size_t m = h->m, P = h->P;
+  int st;
+  if (m_t && (st = h2d(h, h->m_t.ptr, m_t, P * m * sizeof(double)))) return st;
+  if (C_t && (st = h2d(h, h->C_t.ptr, C_t, P * P * m * sizeof(double)))) return st;
+  if (n_t && (st = h2d(h, h->n_t.ptr, n_t, m * sizeof(double)))) return st;
+  if (s_t && (st = h2d(h, h->s_t.ptr, s_t, m * sizeof(double)))) return st;
+  return sync(h);
+}
+
+int sgdlm_get_discount_factors(sgdlm_handle h, double *beta, double *delta) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  const size_t m = h->m, P = h->P;
+  int st;
+  if (beta && (st = d2h(h, beta, h->beta.ptr, m * sizeof(double)))) return st;
+  if (delta && (st = d2h(h, delta, h->delta.ptr, P * P * m * sizeof(double)))) return st;
+  return sync(h);
+}
+
+int sgdlm_set_discount_factors(sgdlm_handle h, const double *beta, const double *delta) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  const size_t m = h->m, P = h->P;
+  int st;
+  if (beta && (st = h2d(h, h->beta.ptr, beta, m * sizeof(double)))) return st;
+  if (delta && (st = h2d(h, h->delta.ptr, delta, P * P * m * sizeof(double)))) return st;
+  return sync(h);
+}
+
+int sgdlm_get_parental_sets(sgdlm_handle h, unsigned *p, unsigned *sp) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (p) std::memcpy(p, h->h_p.data(), h->m * sizeof(unsigned));
+  if (sp) std::memcpy(sp, h->h_sp.data(), h->m * h->P * sizeof(unsigned));
+  return SGDLM_OK;
+}
+
+int sgdlm_set_parental_sets(sgdlm_handle h, const unsigned *p, const unsigned *sp) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  int st = validate_parents(h, p, sp);
+  if (st) return st;
+  const size_t m = h->m, P = h->P;
+  if (p) {
+    std::memcpy(h->h_p.data(), p, m * sizeof(unsigned));
+    if ((st = h2d(h, h->p.ptr, p, m * sizeof(unsigned)))) return st;
+  }
+  if (sp) {
+    std::memcpy(h->h_sp.data(), sp, m * P * sizeof(unsigned));
+    if ((st = h2d(h, h->sp.ptr, sp, m * P * sizeof(unsigned)))) return st;
+    if ((st = sync(h))) return st;
+    if ((st = upload_gamma_rows(h))) return st;
+  }
+  return sync(h);
+}
+
+int sgdlm_compute_posterior(sgdlm_handle h, const double *y_t, const double *F_t) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_prior(true)) return SGDLM_ERR_WRONG_STATE;
+  if (!y_t || !F_t) return h->fail(SGDLM_ERR_BAD_ARG, "null input");
+  const size_t m = h->m, P = h->P;
+  int st;
+  if ((st = h2d(h, h->y_t.ptr, y_t, m * sizeof(double)))) return st;
+  if ((st = h2d(h, h->F_t.ptr, F_t, P * m * sizeof(double)))) return st;
+  launch_posterior(h->stream, (int)m, (int)P, h->p.ptr, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr,
+                   h->s_t.ptr, h->y_t.ptr, h->F_t.ptr);
+  h->launches += 1;
+  if ((st = sync(h))) return st;
+  h->is_prior = false;
+  return SGDLM_OK;
+}
+
+int sgdlm_compute_vb_posterior(sgdlm_handle h, double *mean_m_t, double *mean_C_t,
+                               double *mean_n_t, double *mean_s_t, double *is_weights,
+                               double *sum_det_weights) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+  if (!h->check_prior(false)) return SGDLM_ERR_WRONG_STATE;
+  if (h->precision == SGDLM_PRECISION_FP64)
+    return vb_posterior<double>(h, mean_m_t, mean_C_t, mean_n_t, mean_s_t, is_weights,
+                                sum_det_weights);
+  return vb_posterior<float>(h, mean_m_t, mean_C_t, mean_n_t, mean_s_t, is_weights,
+                             sum_det_weights);
+}
+
+int sgdlm_compute_prior(sgdlm_handle h, int evolve_forecast_variables) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  const int m = (int)h->m, P = (int)h->P;
+  if (evolve_forecast_variables) {
+    launch_prior(h->stream, m, P, h->p.ptr, h->fC_t.ptr, h->fn_t.ptr, h->fW_t.ptr, h->beta.ptr,
+                 h->delta.ptr);
+    h->launches += 1;
+    return sync(h);
+  }
+  if (!h->check_prior(false)) return SGDLM_ERR_WRONG_STATE;
+  launch_prior(h->stream, m, P, h->p.ptr, h->C_t.ptr, h->n_t.ptr, h->W_t.ptr, h->beta.ptr,
+               h->delta.ptr);
+  h->launches += 1;
+  int st = sync(h);
+  if (st) return st;
+  h->is_prior = true;
+  return SGDLM_OK;
+}
+
+int sgdlm_init_forecast_priors(sgdlm_handle h) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  int st = copy_forecast_priors(h);
+  if (st) return st;
+  return sync(h);
+}
+
+int sgdlm_evolve_forecast_samples(sgdlm_handle h) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+  return h->precision == SGDLM_PRECISION_FP64 ? evolve<double>(h) : evolve<float>(h);
+}
+
+int sgdlm_compute_forecast(sgdlm_handle h, double *y_tp1, const double *x_tp1, double *lambdas,
+                           double *thetas, int use_existing_lambdas_and_thetas) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+  if (!h->check_prior(true)) return SGDLM_ERR_WRONG_STATE;
+  if (!x_tp1) return h->fail(SGDLM_ERR_BAD_ARG, "null predictors");
+  const bool ue = use_existing_lambdas_and_thetas != 0;
+  return h->precision == SGDLM_PRECISION_FP64
+             ? forecast<double>(h, y_tp1, x_tp1, lambdas, thetas, ue)
+             : forecast<float>(h, y_tp1, x_tp1, lambdas, thetas, ue);
+}
+
+int sgdlm_get_draws(sgdlm_handle h, double *lambdas, double *thetas, double *log_dets) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+  return h->precision == SGDLM_PRECISION_FP64 ? export_draws<double>(h, lambdas, thetas, log_dets)
+                                              : export_draws<float>(h, lambdas, thetas, log_dets);
+}
+
+int sgdlm_set_precision(sgdlm_handle h, int precision) {
+  HCHECK(h);
+  if (precision != SGDLM_PRECISION_FP64 && precision != SGDLM_PRECISION_MIXED)
+    return h->fail(SGDLM_ERR_BAD_ARG, "unknown precision");
+  if (precision == h->precision) return SGDLM_OK;
+  const int old = h->precision;
+  h->precision = precision;
+  if (h->sim_init) {
+    const size_t nsim = h->nsim, batch = h->nsim_batch;
+    cudaStreamSynchronize(h->stream);
+    int st = alloc_sim(h, nsim);
+    if (st) {
+      h->precision = old;
+      alloc_sim(h, nsim);
+      h->nsim_batch = batch;
+      h->sim_init = true;
+      return st;
+    }
+    h->nsim_batch = batch;
+    h->sim_init = true;
+  }
+  return SGDLM_OK;
+}
+int sgdlm_get_precision(sgdlm_handle h, int *precision) {
+  HCHECK(h);
+  if (!precision) return SGDLM_ERR_BAD_ARG;
+  *precision = h->precision;
+  return SGDLM_OK;
+}
+int sgdlm_set_compat(sgdlm_handle h, unsigned flags) {
+  HCHECK(h);
+  h->compat = flags & SGDLM_COMPAT_REFERENCE;
+  return SGDLM_OK;
+}
+int sgdlm_get_compat(sgdlm_handle h, unsigned *flags) {
+  HCHECK(h);
+  if (!flags) return SGDLM_ERR_BAD_ARG;
+  *flags = h->compat;
+  return SGDLM_OK;
+}
+int sgdlm_set_rng_state(sgdlm_handle h, uint64_t seed, uint64_t epoch) {
+  HCHECK(h);
+  h->seed = seed;
+  h->epoch = epoch;
+  if (h->dev_epoch.ptr) {
+    const uint32_t e32 = (uint32_t)epoch;
+    cudaMemcpyAsync(h->dev_epoch.ptr, &e32, sizeof e32, cudaMemcpyHostToDevice, h->stream);
+    return sync(h);
+  }
+  return SGDLM_OK;
+}
+int sgdlm_get_rng_state(sgdlm_handle h, uint64_t *seed, uint64_t *epoch) {
+  HCHECK(h);
+  if (!seed || !epoch) return SGDLM_ERR_BAD_ARG;
+  *seed = h->seed;
+  *epoch = h->epoch;
+  return SGDLM_OK;
+}
+int sgdlm_get_stats(sgdlm_handle h, sgdlm_stats *out) {
+  HCHECK(h);
+  if (!out) return SGDLM_ERR_BAD_ARG;
+  *out = h->stats;
+  return SGDLM_OK;
+}
+// configureLogLevel (rSGDLM/src/logger.hpp:118-140): snap to the largest level <= level.
+int sgdlm_set_log_level(sgdlm_handle h, int level) {
+  HCHECK(h);
+  const int levels[] = {LOG_SYSDEBUG, LOG_DEBUG, LOG_RESULT, LOG_INFO, LOG_WARNING};
+  int chosen = LOG_ERROR;
+  for (int l : levels)
+    if (level >= l) {
+      chosen = l;
+      break;
+    }
+  h->log_level = chosen;
+  return SGDLM_OK;
+}
+int sgdlm_get_log_level(sgdlm_handle h, int *level) {
+  HCHECK(h);
+  if (!level) return SGDLM_ERR_BAD_ARG;
+  *level = h->log_level;
+  return SGDLM_OK;
+}
+const char *sgdlm_last_error(sgdlm_handle h) { return h ? h->last_error.c_str() : ""; }
+
+int sgdlm_filter_step_device(sgdlm_handle h, const double *d_y, const double *d_F,
+                             const double *d_x, double ess_threshold, double *d_forecast,
+                             double *d_is_weights, double *d_step_stats) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+  if (!h->check_prior(true)) return SGDLM_ERR_WRONG_STATE;
+  if (!d_y || !d_F) return h->fail(SGDLM_ERR_BAD_ARG, "null input");
+  int st = h->precision == SGDLM_PRECISION_FP64
+               ? filter_step<double>(h, d_y, d_F, d_x, ess_threshold, d_forecast, d_is_weights,
+                                     d_step_stats)
+               : filter_step<float>(h, d_y, d_F, d_x, ess_threshold, d_forecast, d_is_weights,
+                                    d_step_stats);
+  if (st) return st;
+  h->is_prior = true;
+  return SGDLM_OK;
+}
+
+int sgdlm_get_stream(sgdlm_handle h, void **stream) {
+  HCHECK(h);
+  if (!stream) return SGDLM_ERR_BAD_ARG;
+  *stream = (void *)h->stream;
+  return SGDLM_OK;
+}
+int sgdlm_synchronize(sgdlm_handle h) {
+  HCHECK(h);
+  return sync(h);
+}
+int sgdlm_get_launch_count(sgdlm_handle h, uint64_t *count) {
+  HCHECK(h);
+  if (!count) return SGDLM_ERR_BAD_ARG;
+  *count = h->launches;
+  return SGDLM_OK;
+}
+
+}  // extern "C"

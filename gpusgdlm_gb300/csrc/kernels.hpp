@@ -1,0 +1,125 @@
+// Launch wrappers for the SGDLM device kernels.  Every wrapper enqueues work on
+// the given stream and returns without synchronising; all device buffers are
+// owned by the engine (engine.cpp).
+//
+// Device layouts (R column-major, as handed over by the reference's Rcpp layer,
+// rSGDLM/src/SGDLM/RcppWrapper.cpp):
+//   m_t   : P x m         (series j at j*P)
+//   C_t   : P x P x m     (series j at j*P*P, column-major within)
+//   n_t,s_t,beta : m
+//   delta : P x P x m
+//   p     : m (unsigned)
+//   sp    : P x m (unsigned; < m*m marks a Gamma position row + m*col)
+// Draw buffers are series-major (GB300 layout, coalesced over draws):
+//   lambda: m x n         (series j, draw i at j*n + i)
+//   theta : m x n x P     (series j, draw i, coefficient k at (j*n + i)*P + k)
+//   y     : n x m         (draw i, series j at i*m + j) == reference (m, nsim)
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sgdlm {
+
+// Per-draw status bits written by the sampler and LU kernels.
+enum : int {
+  DRAW_FLAG_GAMMA_CAP = 1,      // gamma sampler hit its attempt cap
+  DRAW_FLAG_PIVOT = 2,          // no-pivot LU multiplier above threshold -> pivoted redo
+  DRAW_FLAG_SINGULAR = 4,       // zero / non-finite pivot: weight 0, forecast NaN
+  DRAW_FLAG_REDONE = 8,         // draw was refactored by the pivoting fallback
+};
+
+// Philox key and epoch of one sampling call.  When dev_epoch is set (fused,
+// graph-replayable step) the epoch is *dev_epoch + epoch, read on the device.
+struct RngKey {
+  uint32_t k0, k1, epoch;
+  const uint32_t *dev_epoch;
+};
+
+// Advances the device-side epoch counter by `delta` (fused step).
+void launch_advance_epoch(cudaStream_t s, uint32_t *dev_epoch, uint32_t delta);
+
+// (a1) conjugate update, warp per series.  rSGDLM/src/SGDLM/SGDLM.cu:10-113
+void launch_posterior(cudaStream_t s, int m, int P, const unsigned *p, double *m_t,
+                      double *C_t, double *n_t, double *s_t, const double *y,
+                      const double *F);
+
+// (a2) discount step.  rSGDLM/src/SGDLM/SGDLM.cu:115-149
+void launch_prior(cudaStream_t s, int m, int P, const unsigned *p, double *C_t,
+                  double *n_t, double *W_t, const double *beta, const double *delta);
+
+// Upper Cholesky factor U (U'U = C) of the leading p x p block, zero elsewhere,
+// in double and in the sampling precision.  rSGDLM/src/kernel_functions.cuh:845-902
+void launch_cholesky(cudaStream_t s, int m, int P, const unsigned *p, const double *C,
+                     double *U64, float *U32);
+
+// (a3) lambda_ij ~ Gamma(n_j/2, rate n_j s_j/2); theta_ij = m_j + U_j' z/sqrt(s_j lambda_ij).
+// rSGDLM/src/SGDLM/SGDLM.cu:623-677
+template <typename T>
+void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
+                   const double *n_t, const double *s_t, const T *U, RngKey key,
+                   T *lambda, T *theta, int *draw_flags);
+
+// (a9) multi-step evolution of forecast draws.  rSGDLM/src/SGDLM/SGDLM.cu:679-762
+template <typename T>
+void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
+                   const double *r_t, const double *c_t, const double *beta,
+                   const T *UW, RngKey key, bool compat_unscaled_omega,
+                   bool compat_beta_no_boost, T *lambda, T *theta, int *draw_flags);
+
+// (a4)/(a8) batched LU of (I - Gamma_i): log|det| per draw, and optionally the
+// forecast solve y_i = (I - Gamma_i)^-1 nu_i with one refinement step.
+struct LuPlan {
+  int m, P, mp;      // mp = m rounded up to the 32-wide block size
+  int grid, block;   // persistent grid
+  size_t smem;       // dynamic shared memory per CTA
+  size_t scratch_elems_per_cta;
+};
+template <typename T> LuPlan plan_lu(int m, int P, long n, int num_sms);
+// Row-wise list of the Gamma entries of (I - Gamma): for row r, entries
+// rowptr[r] .. rowptr[r+1]-1 are (e = j*P + k, column).  Built on the host from
+// the parental sets; gives the forecast residual a fixed summation order.
+struct GammaRows {
+  const int *rowptr;  // m + 1
+  const int2 *ent;    // nnz
+};
+template <typename T>
+void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const unsigned *sp,
+               const T *theta, T *scratch, double *logdet, int *draw_flags,
+               // forecast solve (x == nullptr: log|det| only)
+               const double *x, const T *lambda, RngKey key, bool refine, double *y,
+               GammaRows rows);
+template <typename T>
+void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n,
+                        const unsigned *sp, const T *theta, T *scratch,
+                        double *logdet, int *draw_flags, const double *x,
+                        const T *lambda, RngKey key, double *y, GammaRows rows);
+
+// (a5) importance weights from log|det| by FP64 log-sum-exp.
+// out6 = {sum_det, ess, max_logdet, n_finite, sum_w2, 0}.  rSGDLM/src/SGDLM/SGDLM.cu:325-335
+void launch_weights(cudaStream_t s, long n, const double *logdet, double *w,
+                    double *out6);
+
+// (a6)/(a7) VB moments and refit.  rSGDLM/src/SGDLM/SGDLM.cu:341-500
+struct VbScratch {
+  double *part_a;   // chunks x m x (P + 2)
+  double *part_b;   // chunks x m x P*P
+  int chunks;
+  int chunk_draws;
+};
+size_t vb_chunks(long n);
+template <typename T>
+void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p,
+               const double *n_t, const double *s_t, const double *w, const T *lambda,
+               const T *theta, VbScratch scr, double *mean_m, double *mean_C,
+               double *mean_n, double *mean_s, double *mean_lambda,
+               double *mean_log_lambda, double *mean_Q, int *series_flags);
+
+// Device-side ESS gate of the fused filter step: copy (mean_m, mean_C, mean_n,
+// mean_s) into the state when stats[1] (ESS) > threshold.
+void launch_gate(cudaStream_t s, int m, int P, const double *stats, double threshold,
+                 const double *mean_m, const double *mean_C, const double *mean_n,
+                 const double *mean_s, double *m_t, double *C_t, double *n_t,
+                 double *s_t, double *accepted);
+
+}  // namespace sgdlm

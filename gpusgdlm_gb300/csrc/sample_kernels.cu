@@ -1,0 +1,230 @@
+// Draw generation: (lambda, theta) from the per-series normal-gamma posterior or
+// prior, and the multi-step evolution of forecast draws.
+//
+// The reference samples with four cuRAND calls into HBM caches, a Marsaglia-Tsang
+// kernel with atomic slot compaction, a one-thread-per-series Cholesky and a
+// pointer-array gemmBatched of batch m*n for theta = U' z
+// (rSGDLM/src/SGDLM/SGDLM.cu:623-677).  Here one thread owns one (draw, series)
+// pair: its normals come out of Philox in registers, U_j sits in shared memory
+// (every thread of the block shares series j, so reads are broadcasts), and the
+// block's theta rows are staged in shared memory so the series-major store is one
+// contiguous coalesced run.
+#include "kernels.hpp"
+#include "rng.cuh"
+
+namespace sgdlm {
+namespace {
+
+constexpr int kSampleThreads = 128;
+
+template <typename T, int PMAX>
+__global__ void __launch_bounds__(kSampleThreads)
+    k_sample(int m, int P, long n, const double *__restrict__ m_t,
+             const double *__restrict__ n_t, const double *__restrict__ s_t,
+             const T *__restrict__ U, RngKey key, T *__restrict__ lambda,
+             T *__restrict__ theta, int *__restrict__ draw_flags) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *Us = reinterpret_cast<T *>(smem_raw);  // P*P, U[row + P*col]
+  T *ms = Us + P * P;                       // P
+  T *stage = ms + P;                        // blockDim.x * P
+  const int j = blockIdx.y;
+  for (int e = threadIdx.x; e < P * P; e += blockDim.x) Us[e] = U[(size_t)j * P * P + e];
+  for (int e = threadIdx.x; e < P; e += blockDim.x) ms[e] = (T)m_t[(size_t)j * P + e];
+  __syncthreads();
+  const long i0 = (long)blockIdx.x * blockDim.x;
+  const long i = i0 + threadIdx.x;
+  if (i < n) {
+    const uint32_t ep = key_epoch(key);
+    const double nj = n_t[j], sj = s_t[j];
+    const T alpha = (T)(0.5 * nj);
+    const T rate = (T)(0.5 * nj * sj);
+    bool fail = false;
+    const T lam = gamma_mt<T>(alpha, (uint32_t)i, (uint32_t)j, TAG_GAMMA, ep, key.k0,
+                              key.k1, false, &fail) / rate;
+    T z[PMAX];
+#pragma unroll
+    for (int q = 0; q < PMAX / 4; ++q) {
+      if (4 * q < P) {
+        const U4 r = philox((uint32_t)i, (uint32_t)j, tag_sub(TAG_THETA, q), ep, key.k0, key.k1);
+        box_muller<T>(r.x, r.y, z[4 * q], z[4 * q + 1]);
+        box_muller<T>(r.z, r.w, z[4 * q + 2], z[4 * q + 3]);
+      } else {
+        z[4 * q] = z[4 * q + 1] = z[4 * q + 2] = z[4 * q + 3] = T(0);
+      }
+    }
+    // theta = m + (U' z) / sqrt(s lambda)   (makeVB_MVN, kernel_functions.cuh:72-83)
+    const T den = dev_sqrt((T)sj * lam);
+    T *row = stage + (size_t)threadIdx.x * P;
+#pragma unroll
+    for (int k = 0; k < PMAX; ++k) {
+      if (k < P) {
+        T acc = T(0);
+#pragma unroll
+        for (int l = 0; l <= k; ++l) acc += Us[l + P * k] * z[l];
+        row[k] = ms[k] + acc / den;
+      }
+    }
+    lambda[(size_t)j * n + i] = lam;
+    if (fail) atomicOr(&draw_flags[i], DRAW_FLAG_GAMMA_CAP);
+  }
+  __syncthreads();
+  const long cnt = (long)min((long)blockDim.x, n - i0) * P;
+  T *dst = theta + ((size_t)j * n + i0) * P;
+  for (long e = threadIdx.x; e < cnt; e += blockDim.x) dst[e] = stage[e];
+}
+
+// eta ~ Beta(beta r/2, (1-beta) r/2) / beta via two gammas (make_gamma_1 and
+// make_beta, kernel_functions.cuh:644-798); lambda *= eta (batchedMultiply
+// :458-466); omega ~ N(0, I) scaled by 1/sqrt(c lambda) and cut at p
+// (scale_omegas :986-1001); theta += U_W' omega (SGDLM.cu:755-758).
+template <typename T, int PMAX>
+__global__ void __launch_bounds__(kSampleThreads)
+    k_evolve(int m, int P, long n, const unsigned *__restrict__ p,
+             const double *__restrict__ r_t, const double *__restrict__ c_t,
+             const double *__restrict__ beta, const T *__restrict__ UW, RngKey key,
+             bool compat_unscaled, bool compat_no_boost, T *__restrict__ lambda,
+             T *__restrict__ theta, int *__restrict__ draw_flags) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *Us = reinterpret_cast<T *>(smem_raw);
+  T *stage = Us + P * P;
+  const int j = blockIdx.y;
+  const long i0 = (long)blockIdx.x * blockDim.x;
+  const long cnt = (long)min((long)blockDim.x, n - i0) * P;
+  T *src = theta + ((size_t)j * n + i0) * P;
+  for (int e = threadIdx.x; e < P * P; e += blockDim.x) Us[e] = UW[(size_t)j * P * P + e];
+  for (long e = threadIdx.x; e < cnt; e += blockDim.x) stage[e] = src[e];
+  __syncthreads();
+  const long i = i0 + threadIdx.x;
+  if (i < n) {
+    const uint32_t ep = key_epoch(key);
+    const double bj = beta[j], rj = r_t[j];
+    bool fail = false;
+    T eta = T(1);
+    if (bj != 1.0) {
+      const T ga = gamma_mt<T>((T)(0.5 * bj * rj), (uint32_t)i, (uint32_t)j, TAG_BETA_A,
+                               ep, key.k0, key.k1, compat_no_boost, &fail);
+      const T gb = gamma_mt<T>((T)(0.5 * (1.0 - bj) * rj), (uint32_t)i, (uint32_t)j,
+                               TAG_BETA_B, ep, key.k0, key.k1, compat_no_boost,
+                               &fail);
+      eta = (ga / (ga + gb)) / (T)bj;
+    }
+    const T lam = lambda[(size_t)j * n + i] * eta;
+    lambda[(size_t)j * n + i] = lam;
+    T w[PMAX];
+#pragma unroll
+    for (int q = 0; q < PMAX / 4; ++q) {
+      if (4 * q < P) {
+        const U4 r = philox((uint32_t)i, (uint32_t)j, tag_sub(TAG_OMEGA, q), ep, key.k0, key.k1);
+        box_muller<T>(r.x, r.y, w[4 * q], w[4 * q + 1]);
+        box_muller<T>(r.z, r.w, w[4 * q + 2], w[4 * q + 3]);
+      } else {
+        w[4 * q] = w[4 * q + 1] = w[4 * q + 2] = w[4 * q + 3] = T(0);
+      }
+    }
+    // The reference's scale_omegas launch only ever reaches draw 0 of series 0
+    // (its z index is always 0), leaving every other omega unscaled; compat mode
+    // reproduces that, the default applies the scaling to every draw.
+    const bool do_scale = !compat_unscaled || (i == 0 && j == 0);
+    if (do_scale) {
+      const T den = dev_sqrt((T)c_t[j] * lam);
+      const unsigned pj = p[j];
+#pragma unroll
+      for (int k = 0; k < PMAX; ++k) w[k] = ((unsigned)k < pj) ? w[k] / den : T(0);
+    }
+    T *row = stage + (size_t)threadIdx.x * P;
+#pragma unroll
+    for (int k = 0; k < PMAX; ++k) {
+      if (k < P) {
+        T acc = T(0);
+#pragma unroll
+        for (int l = 0; l <= k; ++l) acc += Us[l + P * k] * w[l];
+        row[k] = acc + row[k];
+      }
+    }
+    if (fail) atomicOr(&draw_flags[i], DRAW_FLAG_GAMMA_CAP);
+  }
+  __syncthreads();
+  for (long e = threadIdx.x; e < cnt; e += blockDim.x) src[e] = stage[e];
+}
+
+template <typename T> size_t sample_smem(int P) {
+  return ((size_t)P * P + P + (size_t)kSampleThreads * P) * sizeof(T);
+}
+
+}  // namespace
+
+template <typename T>
+void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
+                   const double *n_t, const double *s_t, const T *U, RngKey key,
+                   T *lambda, T *theta, int *draw_flags) {
+  dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
+  const size_t smem = sample_smem<T>(P);
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_sample<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    cudaFuncSetAttribute(k_sample<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    cudaFuncSetAttribute(k_sample<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    cudaFuncSetAttribute(k_sample<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    configured = true;
+  }
+  if (P <= 8)
+    k_sample<T, 8><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
+                                                      lambda, theta, draw_flags);
+  else if (P <= 16)
+    k_sample<T, 16><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
+                                                       lambda, theta, draw_flags);
+  else if (P <= 32)
+    k_sample<T, 32><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
+                                                       lambda, theta, draw_flags);
+  else
+    k_sample<T, 64><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
+                                                       lambda, theta, draw_flags);
+}
+
+template <typename T>
+void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
+                   const double *r_t, const double *c_t, const double *beta,
+                   const T *UW, RngKey key, bool compat_unscaled_omega,
+                   bool compat_beta_no_boost, T *lambda, T *theta, int *draw_flags) {
+  dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
+  const size_t smem = ((size_t)P * P + (size_t)kSampleThreads * P) * sizeof(T);
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_evolve<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    cudaFuncSetAttribute(k_evolve<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    cudaFuncSetAttribute(k_evolve<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    cudaFuncSetAttribute(k_evolve<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
+    configured = true;
+  }
+#define SGDLM_EVOLVE(PM)                                                              \
+  k_evolve<T, PM><<<grid, kSampleThreads, smem, s>>>(m, P, n, p, r_t, c_t, beta, UW, \
+                                                     key, compat_unscaled_omega,      \
+                                                     compat_beta_no_boost, lambda,    \
+                                                     theta, draw_flags)
+  if (P <= 8)
+    SGDLM_EVOLVE(8);
+  else if (P <= 16)
+    SGDLM_EVOLVE(16);
+  else if (P <= 32)
+    SGDLM_EVOLVE(32);
+  else
+    SGDLM_EVOLVE(64);
+#undef SGDLM_EVOLVE
+}
+
+template void launch_sample<float>(cudaStream_t, int, int, long, const double *,
+                                   const double *, const double *, const float *, RngKey,
+                                   float *, float *, int *);
+template void launch_sample<double>(cudaStream_t, int, int, long, const double *,
+                                    const double *, const double *, const double *,
+                                    RngKey, double *, double *, int *);
+template void launch_evolve<float>(cudaStream_t, int, int, long, const unsigned *,
+                                   const double *, const double *, const double *,
+                                   const float *, RngKey, bool, bool, float *, float *,
+                                   int *);
+template void launch_evolve<double>(cudaStream_t, int, int, long, const unsigned *,
+                                    const double *, const double *, const double *,
+                                    const double *, RngKey, bool, bool, double *,
+                                    double *, int *);
+
+}  // namespace sgdlm

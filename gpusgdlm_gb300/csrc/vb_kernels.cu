@@ -1,0 +1,427 @@
+// Importance weights and the Variational-Bayes refit.
+//
+// Reference (rSGDLM/src/SGDLM/SGDLM.cu:325-500): the weight sum is one serial
+// thread (sumVector, kernel_functions.cuh:26-39); every moment is a
+// one-thread-per-output loop over all n draws (meanScalarAndLog :929-946,
+// compute_mean_m_t :949-967, meanBatchedVecVecT :1103-1133 with a global
+// read-modify-write per draw); V^-1 comes from getrf/getri; and Q_ij =
+// lambda (theta - m)' V^-1 (theta - m) is two gemmBatched calls of batch m*n
+// whose only consumer is the weighted mean Q_bar_j (compute_mean_Q_t :1088-1100).
+//
+// Here:
+//  * weights are exp(logdet - max) / sum in FP64 (log-sum-exp), one block;
+//  * pass A and pass B reduce over draws with one block per (series, chunk of
+//    2048 draws), coalesced over the series-major draw buffers, warp-shuffle
+//    block reductions, FP64 chunk partials;
+//  * Q_bar_j is evaluated as trace(V^-1 V): since V = sum_i w_i theta~_i theta~_i'
+//    with the same weights, sum_i w_i theta~_i' V^-1 theta~_i = tr(V^-1 V)
+//    exactly, so the m*n quadratic forms of the reference collapse to a p x p
+//    trace per series (equal to p_j up to the rounding of V^-1);
+//  * the Newton solve for the gamma shape uses the reference's own asymptotic
+//    digamma/trigamma series and stopping rule, in FP64.
+#include "kernels.hpp"
+
+namespace sgdlm {
+namespace {
+
+constexpr int kChunk = 2048;
+constexpr int kVbThreads = 256;
+constexpr int kSub = 128;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum; every thread gets the result.  `red` needs 32 doubles.
+__device__ double block_sum(double v, double *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  const int nw = blockDim.x >> 5;
+  for (int w = 0; w < nw; ++w) t += red[w];
+  return t;
+}
+__device__ double block_max(double v, double *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = -INFINITY;
+  const int nw = blockDim.x >> 5;
+  for (int w = 0; w < nw; ++w) t = fmax(t, red[w]);
+  return t;
+}
+
+__device__ __forceinline__ bool finite_ld(double v) { return v == v && fabs(v) < INFINITY; }
+
+// out6 = {sum |det|, ESS, max logdet, #finite, sum w^2, 0}.
+// A draw whose log|det| is not finite gets weight 0, as detFromLU gives a NaN/Inf
+// determinant weight 0 (kernel_functions.cuh:905-926).
+__global__ void k_weights(long n, const double *__restrict__ logdet, double *__restrict__ w,
+                          double *__restrict__ out6) {
+  __shared__ double red[32];
+  double mx = -INFINITY, cnt = 0.0;
+  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = logdet[i];
+    if (finite_ld(v)) {
+      mx = fmax(mx, v);
+      cnt += 1.0;
+    }
+  }
+  mx = block_max(mx, red);
+  cnt = block_sum(cnt, red);
+  double s = 0.0;
+  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = logdet[i];
+    if (finite_ld(v)) s += exp(v - mx);
+  }
+  s = block_sum(s, red);
+  double s2 = 0.0;
+  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = logdet[i];
+    double wi;
+    if (s > 0.0)
+      wi = finite_ld(v) ? exp(v - mx) / s : 0.0;
+    else
+      wi = NAN;  // every determinant was zero: the reference divides 0 by 0
+    w[i] = wi;
+    s2 += wi * wi;
+  }
+  s2 = block_sum(s2, red);
+  if (threadIdx.x == 0) {
+    out6[0] = (s > 0.0) ? exp(mx) * s : 0.0;
+    out6[1] = 1.0 / s2;
+    out6[2] = mx;
+    out6[3] = cnt;
+    out6[4] = s2;
+    out6[5] = 0.0;
+  }
+}
+
+template <typename T> __device__ __forceinline__ T tlog(T v);
+template <> __device__ __forceinline__ float tlog<float>(float v) { return logf(v); }
+template <> __device__ __forceinline__ double tlog<double>(double v) { return log(v); }
+template <typename T> __device__ __forceinline__ T tsqrt(T v);
+template <> __device__ __forceinline__ float tsqrt<float>(float v) { return sqrtf(v); }
+template <> __device__ __forceinline__ double tsqrt<double>(double v) { return sqrt(v); }
+
+// Pass A: per (chunk, series): sum w lambda, sum w log lambda, sum w lambda theta_k.
+template <typename T, int PMAX>
+__global__ void __launch_bounds__(kVbThreads)
+    k_vb_a(int m, int P, long n, const double *__restrict__ w, const T *__restrict__ lambda,
+           const T *__restrict__ theta, double *__restrict__ part_a) {
+  __shared__ double red[32];
+  const int j = blockIdx.y, c = blockIdx.x;
+  const long i0 = (long)c * kChunk;
+  const long i1 = min(n, i0 + kChunk);
+  T sl = T(0), sll = T(0);
+  T st[PMAX];
+#pragma unroll
+  for (int k = 0; k < PMAX; ++k) st[k] = T(0);
+  for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const T wi = (T)w[i];
+    const T lam = lambda[(size_t)j * n + i];
+    const T wl = wi * lam;
+    sl += wl;
+    sll += wi * tlog(lam);
+    const T *th = theta + ((size_t)j * n + i) * P;
+#pragma unroll
+    for (int k = 0; k < PMAX; ++k)
+      if (k < P) st[k] += wl * th[k];
+  }
+  double *out = part_a + ((size_t)c * m + j) * (P + 2);
+  double v = block_sum((double)sl, red);
+  if (threadIdx.x == 0) out[0] = v;
+  v = block_sum((double)sll, red);
+  if (threadIdx.x == 0) out[1] = v;
+#pragma unroll
+  for (int k = 0; k < PMAX; ++k) {
+    if (k < P) {
+      v = block_sum((double)st[k], red);
+      if (threadIdx.x == 0) out[2 + k] = v;
+    }
+  }
+}
+
+// Combines the chunk partials of pass A: E_w lambda, E_w log lambda, and the
+// uncut weighted mean m_bar = sum w lambda theta / sum w lambda over all P
+// (compute_mean_m_t, kernel_functions.cuh:949-967).
+__global__ void k_vb_a_fin(int m, int P, int chunks, const double *__restrict__ part_a,
+                           double *__restrict__ mean_lambda,
+                           double *__restrict__ mean_log_lambda,
+                           double *__restrict__ mbar_full) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  double sl = 0.0, sll = 0.0;
+  for (int c = 0; c < chunks; ++c) {
+    const double *pa = part_a + ((size_t)c * m + j) * (P + 2);
+    sl += pa[0];
+    sll += pa[1];
+  }
+  mean_lambda[j] = sl;
+  mean_log_lambda[j] = sll;
+  for (int k = 0; k < P; ++k) {
+    double st = 0.0;
+    for (int c = 0; c < chunks; ++c) st += part_a[((size_t)c * m + j) * (P + 2) + 2 + k];
+    mbar_full[(size_t)j * P + k] = st / sl;
+  }
+}
+
+// Pass B: per (chunk, series): V = sum w lambda (theta - m_bar)(theta - m_bar)' over
+// the leading p x p block (meanBatchedVecVecT, kernel_functions.cuh:1103-1133).
+// Draws are staged kSub at a time as X_i = sqrt(w_i lambda_i) (theta_i - m_bar);
+// each thread owns upper-triangle pairs (x <= y), accumulates a sub-chunk in the
+// working precision and flushes it to an FP64 shared accumulator.
+template <typename T>
+__global__ void __launch_bounds__(kVbThreads)
+    k_vb_b(int m, int P, long n, const unsigned *__restrict__ p,
+           const double *__restrict__ w, const T *__restrict__ lambda,
+           const T *__restrict__ theta, const double *__restrict__ mbar_full,
+           double *__restrict__ part_b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int j = blockIdx.y, c = blockIdx.x;
+  const int pj = (int)min((unsigned)P, p[j]);
+  const int npairs = pj * (pj + 1) / 2;
+  double *acc64 = reinterpret_cast<double *>(smem_raw);             // npairs
+  T *mb = reinterpret_cast<T *>(acc64 + (npairs > 0 ? npairs : 1));  // P
+  T *X = mb + P;                                                     // kSub * P
+  for (int q = threadIdx.x; q < npairs; q += blockDim.x) acc64[q] = 0.0;
+  for (int k = threadIdx.x; k < P; k += blockDim.x) mb[k] = (T)mbar_full[(size_t)j * P + k];
+  __syncthreads();
+  const long i0 = (long)c * kChunk;
+  const long i1 = min(n, i0 + kChunk);
+  for (long s0 = i0; s0 < i1; s0 += kSub) {
+    const int cnt = (int)min((long)kSub, i1 - s0);
+    for (int e = threadIdx.x; e < cnt * P; e += blockDim.x) {
+      const int s = e / P, k = e % P;
+      const long i = s0 + s;
+      const T sc = tsqrt<T>((T)w[i] * lambda[(size_t)j * n + i]);
+      X[e] = sc * (theta[((size_t)j * n + i) * P + k] - mb[k]);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
+      // pair index q -> (x, y) with x <= y: column-major over the upper triangle
+      int y = (int)((sqrt(8.0 * q + 1.0) - 1.0) * 0.5);
+      while ((y + 1) * (y + 2) / 2 <= q) ++y;
+      while (y * (y + 1) / 2 > q) --y;
+      const int x = q - y * (y + 1) / 2;
+      T a = T(0);
+      for (int s = 0; s < cnt; ++s) a += X[s * P + x] * X[s * P + y];
+      acc64[q] += (double)a;
+    }
+    __syncthreads();
+  }
+  double *out = part_b + ((size_t)c * m + j) * P * P;
+  for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
+    int y = (int)((sqrt(8.0 * q + 1.0) - 1.0) * 0.5);
+    while ((y + 1) * (y + 2) / 2 <= q) ++y;
+    while (y * (y + 1) / 2 > q) --y;
+    const int x = q - y * (y + 1) / 2;
+    out[x + P * y] = acc64[q];
+  }
+}
+
+// The reference's digamma and trigamma (kernel_functions.cuh:1006-1022): the
+// asymptotic (Stirling) series truncated after the x^-14 and x^-9 terms, applied
+// at any x.  Reproduced as is, including its error at small x.
+__device__ __forceinline__ double psi_series(double x) {
+  const double x2 = x * x, x4 = x2 * x2, x6 = x4 * x2, x8 = x4 * x4;
+  const double x10 = x8 * x2, x12 = x8 * x4, x14 = x12 * x2;
+  return log(x) - 1.0 / (2.0 * x) - 1.0 / (12.0 * x2) + 1.0 / (120.0 * x4) -
+         1.0 / (252.0 * x6) + 1.0 / (240.0 * x8) - 5.0 / (660.0 * x10) +
+         691.0 / (32760.0 * x12) - 1.0 / (12.0 * x14);
+}
+__device__ __forceinline__ double psi1_series(double x) {
+  const double x2 = x * x, x3 = x2 * x, x5 = x3 * x2, x7 = x5 * x2, x9 = x7 * x2;
+  return 1.0 / x + 1.0 / (2.0 * x2) + 1.0 / (6.0 * x3) - 1.0 / (30.0 * x5) +
+         1.0 / (42.0 * x7) - 1.0 / (30.0 * x9);
+}
+
+// Per-series refit, one warp per series (FP64):
+//   V (p x p) from the chunk partials; V^-1 by Gauss-Jordan with partial
+//   pivoting; Q_bar = tr(V^-1 V); Newton for n_bar (compute_mean_n_t,
+//   kernel_functions.cuh:1025-1068); s_bar (compute_mean_s_t :1071-1085);
+//   C_bar = V s_bar inside p x p, zero outside; m_bar cut at p.
+__global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ p,
+                         const double *__restrict__ n_t, const double *__restrict__ s_t,
+                         const double *__restrict__ part_b,
+                         const double *__restrict__ mean_lambda,
+                         const double *__restrict__ mean_log_lambda,
+                         const double *__restrict__ mbar_full, double *__restrict__ mean_m,
+                         double *__restrict__ mean_C, double *__restrict__ mean_n,
+                         double *__restrict__ mean_s, double *__restrict__ mean_Q,
+                         int *__restrict__ series_flags) {
+  extern __shared__ double sh[];
+  const int j = blockIdx.x;
+  const int lane = threadIdx.x;
+  const int pj = (int)min((unsigned)P, p[j]);
+  double *V = sh;                      // P x P, V[x + P*y]
+  double *G = V + (size_t)P * P;       // p x 2p augmented [V | I], G[r + pj*c]
+  double *f = G + (size_t)2 * P * P;   // multipliers of the current column
+  __shared__ int s_piv;
+  __shared__ int s_bad;
+  __shared__ double s_sb;
+  if (lane == 0) s_bad = 0;
+  for (int e = lane; e < P * P; e += 32) {
+    const int x = e % P, y = e / P;
+    double v = 0.0;
+    if (x < pj && y < pj) {
+      const int a = min(x, y), b = max(x, y);
+      for (int c = 0; c < chunks; ++c) v += part_b[((size_t)c * m + j) * P * P + a + P * b];
+    }
+    V[e] = v;
+  }
+  __syncwarp();
+  for (int e = lane; e < pj * 2 * pj; e += 32) {
+    const int r = e % pj, cidx = e / pj;
+    G[e] = (cidx < pj) ? V[r + P * cidx] : ((cidx - pj) == r ? 1.0 : 0.0);
+  }
+  __syncwarp();
+  // Gauss-Jordan with partial pivoting on [V | I] -> [I | V^-1]
+  for (int k = 0; k < pj; ++k) {
+    if (lane == 0) {
+      int best = k;
+      double bv = fabs(G[k + pj * k]);
+      for (int r = k + 1; r < pj; ++r) {
+        const double v = fabs(G[r + pj * k]);
+        if (v > bv) {
+          bv = v;
+          best = r;
+        }
+      }
+      s_piv = best;
+      if (!(bv > 0.0)) s_bad = 1;
+    }
+    __syncwarp();
+    const int pr = s_piv;
+    if (pr != k)
+      for (int cidx = lane; cidx < 2 * pj; cidx += 32) {
+        const double t = G[k + pj * cidx];
+        G[k + pj * cidx] = G[pr + pj * cidx];
+        G[pr + pj * cidx] = t;
+      }
+    __syncwarp();
+    const double piv = G[k + pj * k];
+    for (int r = lane; r < pj; r += 32) f[r] = G[r + pj * k];
+    __syncwarp();
+    for (int cidx = lane; cidx < 2 * pj; cidx += 32) {
+      const double gk = G[k + pj * cidx] / piv;
+      G[k + pj * cidx] = gk;
+      for (int r = 0; r < pj; ++r)
+        if (r != k) G[r + pj * cidx] -= f[r] * gk;
+    }
+    __syncwarp();
+  }
+  // Q_bar = sum_{x,y} Vinv[x][y] V[y][x]
+  double q = 0.0;
+  for (int e = lane; e < pj * pj; e += 32) {
+    const int x = e % pj, y = e / pj;
+    q += G[x + pj * (pj + y)] * V[y + P * x];
+  }
+  q = warp_sum(q);
+  if (lane == 0) {
+    const double El = mean_lambda[j], Ell = mean_log_lambda[j];
+    const double pd = (double)p[j];
+    double mn = n_t[j];
+    double fun, dfun, step = 0.0;
+    size_t iter = 0;
+    do {
+      mn -= step;
+      fun = log(mn + pd - q) - psi_series(mn / 2) - (pd - q) / mn - log(2 * El) + Ell;
+      dfun = 1 / (mn + pd - q) - .5 * psi1_series(mn / 2) + (pd - q) / (mn * mn);
+      step = fun / dfun;
+      if (step > mn) step = .5 * mn;
+    } while (fabs(fun) > 1e-6 && iter++ < 50);
+    int fl = s_bad ? 1 : 0;
+    if (iter >= 50) {
+      mn = n_t[j];
+      fl |= 2;
+    }
+    double sb = (mn + pd - q) / (mn * El);
+    if (sb < 0) {
+      sb = s_t[j];
+      fl |= 4;
+    }
+    mean_n[j] = mn;
+    mean_s[j] = sb;
+    mean_Q[j] = q;
+    if (series_flags) series_flags[j] = fl;
+    s_sb = sb;
+  }
+  __syncwarp();
+  const double sb = s_sb;
+  for (int e = lane; e < P * P; e += 32) {
+    const int x = e % P, y = e / P;
+    mean_C[(size_t)j * P * P + e] = (x < pj && y < pj) ? V[e] * sb : 0.0;
+  }
+  for (int k = lane; k < P; k += 32)
+    mean_m[(size_t)j * P + k] = (k < pj) ? mbar_full[(size_t)j * P + k] : 0.0;
+}
+
+}  // namespace
+
+size_t vb_chunks(long n) { return (size_t)((n + kChunk - 1) / kChunk); }
+
+void launch_weights(cudaStream_t s, long n, const double *logdet, double *w, double *out6) {
+  k_weights<<<1, 1024, 0, s>>>(n, logdet, w, out6);
+}
+
+template <typename T>
+void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const double *n_t,
+               const double *s_t, const double *w, const T *lambda, const T *theta,
+               VbScratch scr, double *mean_m, double *mean_C, double *mean_n,
+               double *mean_s, double *mean_lambda, double *mean_log_lambda,
+               double *mean_Q, int *series_flags) {
+  const int chunks = scr.chunks;
+  dim3 grid((unsigned)chunks, (unsigned)m);
+  if (P <= 8)
+    k_vb_a<T, 8><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+  else if (P <= 16)
+    k_vb_a<T, 16><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+  else if (P <= 32)
+    k_vb_a<T, 32><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+  else
+    k_vb_a<T, 64><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+  // mbar_full lives in mean_m's slot until the refit overwrites it with the cut mean;
+  // a separate buffer keeps the kernels independent.
+  double *mbar_full = scr.part_a + (size_t)chunks * m * (P + 2);
+  k_vb_a_fin<<<(m + 127) / 128, 128, 0, s>>>(m, P, chunks, scr.part_a, mean_lambda,
+                                             mean_log_lambda, mbar_full);
+  const size_t npairs = (size_t)P * (P + 1) / 2;
+  const size_t smem_b = npairs * sizeof(double) + ((size_t)P + (size_t)kSub * P) * sizeof(T) + 16;
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_vb_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_vb_fin, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    configured = true;
+  }
+  k_vb_b<T><<<grid, kVbThreads, smem_b, s>>>(m, P, n, p, w, lambda, theta, mbar_full,
+                                             scr.part_b);
+  const size_t smem_f = ((size_t)P * P * 3 + P) * sizeof(double);
+  k_vb_fin<<<m, 32, smem_f, s>>>(m, P, chunks, p, n_t, s_t, scr.part_b, mean_lambda,
+                                 mean_log_lambda, mbar_full, mean_m, mean_C, mean_n,
+                                 mean_s, mean_Q, series_flags);
+}
+
+template void launch_vb<float>(cudaStream_t, int, int, long, const unsigned *,
+                               const double *, const double *, const double *,
+                               const float *, const float *, VbScratch, double *, double *,
+                               double *, double *, double *, double *, double *, int *);
+template void launch_vb<double>(cudaStream_t, int, int, long, const unsigned *,
+                                const double *, const double *, const double *,
+                                const double *, const double *, VbScratch, double *,
+                                double *, double *, double *, double *, double *, double *,
+                                int *);
+
+}  // namespace sgdlm

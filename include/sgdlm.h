@@ -1,0 +1,161 @@
+/*
+ * sgdlm.h - C ABI of the GB300 SGDLM filtering engine.
+ *
+ * One handle = one engine on one GPU with one CUDA stream, like one
+ * SGDLM::HostWrapper<double> of the reference (rSGDLM/src/SGDLM/HostWrapper.hpp:13-99)
+ * constructed by HostWrapperFactory<double>::create (HostWrapperFactory.cu:5-35).
+ * Every entry point mirrors one method of that interface: same arguments, same
+ * meaning, same column-major host layouts, same state-order rules.  Where the
+ * reference logs an error and returns silently (rSGDLM/src/logger.hpp:160-165,
+ * HostWrapperImpl.cu:1239-1286) these functions log the same condition and return
+ * a non-zero sgdlm_status instead; the state is left unchanged.
+ *
+ * Host arrays are caller-owned, double precision, R column-major:
+ *   m_t P x m, C_t P x P x m, n_t/s_t/beta m, delta P x P x m, p m (unsigned),
+ *   sp P x m (unsigned; values < m*m address (I - Gamma) at row + m*col, any value
+ *   >= m*m - e.g. R's NA_integer_ - marks an external predictor),
+ *   y_t m, F_t P x m, forecast output m x nsim.
+ * Calls are synchronous (like the reference) unless named *_device.
+ */
+#ifndef SGDLM_GB300_H_
+#define SGDLM_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sgdlm_engine *sgdlm_handle;
+
+typedef enum {
+  SGDLM_OK = 0,
+  SGDLM_ERR_BAD_DIM = 1,        /* dimension mismatch (RcppWrapper.cpp:80-92, 170-174, 264-271) */
+  SGDLM_ERR_NOT_INIT = 2,       /* device memory not initialised (HostWrapperImpl.cu:1240-1246) */
+  SGDLM_ERR_WRONG_STATE = 3,    /* prior/posterior order (HostWrapperImpl.cu:1268-1286) */
+  SGDLM_ERR_SIM_NOT_INIT = 4,   /* simulation memory not initialised (HostWrapperImpl.cu:1249-1255) */
+  SGDLM_ERR_DEVICE = 5,         /* CUDA error (the reference only logs these, loggerGPU.cuh:26-60) */
+  SGDLM_ERR_BAD_ARG = 6,        /* null pointer, nsim = 0, invalid parental set */
+  SGDLM_ERR_NO_DEVICE = 7,      /* no CUDA device (HostWrapperImpl.cu:22-25) */
+  SGDLM_ERR_OUT_OF_MEMORY = 8,
+  SGDLM_ERR_UNSUPPORTED = 9     /* size beyond this build's limits (max_p > 64, m > 800) */
+} sgdlm_status;
+
+typedef enum {
+  SGDLM_PRECISION_FP64 = 0,  /* every kernel in FP64 (the reference's DOUBLETYPE=double) */
+  SGDLM_PRECISION_MIXED = 1  /* draws, LU and solves in FP32 (+FP64 refinement);
+                                posterior/prior, log-sum-exp, moments' sums, Newton in FP64 */
+} sgdlm_precision;
+
+/* Reference-behaviour switches (on by default: the drop-in reproduces the
+ * reference's sampling distributions, including these two defects). */
+enum {
+  /* scale_omegas (kernel_functions.cuh:986-1001) is launched with its z index
+   * fixed at 0 (SGDLM.cu:718-722), so only draw 0 of series 0 gets the
+   * 1/sqrt(c lambda) scale; every other evolution innovation stays N(0, W). */
+  SGDLM_COMPAT_UNSCALED_EVOLUTION = 1u,
+  /* make_gamma_1/make_beta (kernel_functions.cuh:644-798) apply Marsaglia-Tsang
+   * to shapes below one without the U^(1/a) boost. */
+  SGDLM_COMPAT_BETA_NO_BOOST = 2u,
+  SGDLM_COMPAT_REFERENCE = 3u,
+  SGDLM_COMPAT_NONE = 0u
+};
+
+typedef struct {
+  /* last computeVBPosterior / computeForecast */
+  double ess;                /* (sum w)^2 / sum w^2 of the normalised IS weights */
+  double sum_det_weights;    /* sum_i |det(I - Gamma_i)| (reference output) */
+  double max_log_det;
+  uint64_t draws_pivoted;    /* draws redone with partial pivoting */
+  uint64_t draws_singular;   /* draws with a singular (I - Gamma): weight 0 / NaN forecast */
+  uint64_t gamma_cap_hits;   /* gamma draws that hit the sampler's attempt cap */
+  uint64_t newton_fallbacks; /* series whose VB Newton solve did not converge */
+  /* CUDA-event timings of the last call's phases, milliseconds */
+  double ms_sample, ms_lu, ms_weights, ms_vb, ms_total;
+  double ms_lu_forecast;
+} sgdlm_stats;
+
+/* ---- lifetime (HostWrapperFactory.cu:5-35, HostWrapperImpl.cu:12-105) ---- */
+int sgdlm_create(size_t no_gpus, sgdlm_handle *out);
+int sgdlm_destroy(sgdlm_handle h);
+int sgdlm_init_memory(sgdlm_handle h, size_t m, size_t max_p);       /* initMemory :130 */
+int sgdlm_clear_memory(sgdlm_handle h);                               /* clearMemory :281 */
+int sgdlm_get_no_series(sgdlm_handle h, size_t *m);                   /* getNoSeries :108 */
+int sgdlm_get_max_p(sgdlm_handle h, size_t *max_p);                   /* getMaxP :115 */
+int sgdlm_get_no_gpus(sgdlm_handle h, size_t *no_gpus);
+int sgdlm_init_sim_memory(sgdlm_handle h, size_t nsim, size_t nsim_batch); /* initSimMemory :321 */
+int sgdlm_clear_sim_memory(sgdlm_handle h);                           /* clearSimMemory :514 */
+int sgdlm_get_nsim(sgdlm_handle h, size_t *nsim);                     /* getNSim :307 */
+int sgdlm_get_nsim_batch(sgdlm_handle h, size_t *nsim_batch);         /* getNSimBatch :314 */
+int sgdlm_is_prior(sgdlm_handle h, int *is_prior);                    /* isPrior :590 */
+int sgdlm_set_is_prior(sgdlm_handle h, int is_prior);                 /* isPrior(bool) :597 */
+
+/* ---- parameters (HostWrapperImpl.cu:604-797); a NULL pointer skips that array ---- */
+int sgdlm_get_parameters(sgdlm_handle h, double *m_t, double *C_t, double *n_t, double *s_t);
+int sgdlm_set_parameters(sgdlm_handle h, const double *m_t, const double *C_t,
+                         const double *n_t, const double *s_t);
+int sgdlm_get_discount_factors(sgdlm_handle h, double *beta, double *delta);
+int sgdlm_set_discount_factors(sgdlm_handle h, const double *beta, const double *delta);
+int sgdlm_get_parental_sets(sgdlm_handle h, unsigned *p, unsigned *sp);
+int sgdlm_set_parental_sets(sgdlm_handle h, const unsigned *p, const unsigned *sp);
+
+/* ---- filtering (HostWrapperImpl.cu:799-1228) ---- */
+int sgdlm_compute_posterior(sgdlm_handle h, const double *y_t, const double *F_t); /* :1024 */
+int sgdlm_compute_vb_posterior(sgdlm_handle h, double *mean_m_t, double *mean_C_t,
+                               double *mean_n_t, double *mean_s_t, double *is_weights,
+                               double *sum_det_weights);                           /* :1060 */
+int sgdlm_compute_prior(sgdlm_handle h, int evolve_forecast_variables);            /* :800 */
+int sgdlm_init_forecast_priors(sgdlm_handle h);                                    /* :540 */
+int sgdlm_evolve_forecast_samples(sgdlm_handle h);                                 /* :880 */
+int sgdlm_compute_forecast(sgdlm_handle h, double *y_tp1, const double *x_tp1,
+                           double *lambdas, double *thetas,
+                           int use_existing_lambdas_and_thetas);                   /* :949 */
+
+/* Copies the current draw buffers to host in the reference's draw-major layouts,
+ * lambdas (m x nsim) and thetas (max_p x m x nsim) as in computeForecastDebug
+ * (RcppWrapper.cpp:557-569), and the last per-draw log|det(I - Gamma)| (nsim).
+ * Any pointer may be NULL. */
+int sgdlm_get_draws(sgdlm_handle h, double *lambdas, double *thetas, double *log_dets);
+
+/* ---- engine options (no counterpart in the reference's interface) ---- */
+int sgdlm_set_precision(sgdlm_handle h, int precision);
+int sgdlm_get_precision(sgdlm_handle h, int *precision);
+int sgdlm_set_compat(sgdlm_handle h, unsigned flags);
+int sgdlm_get_compat(sgdlm_handle h, unsigned *flags);
+/* Random stream: Philox4x32-10 keyed by seed; epoch counts sampling calls.  The
+ * reference seeds cuRAND with 1234 + 100*gpu (HostWrapperImpl.cu:63-64) and
+ * never exposes the state; (seed, epoch) here is a complete checkpoint. */
+int sgdlm_set_rng_state(sgdlm_handle h, uint64_t seed, uint64_t epoch);
+int sgdlm_get_rng_state(sgdlm_handle h, uint64_t *seed, uint64_t *epoch);
+int sgdlm_get_stats(sgdlm_handle h, sgdlm_stats *out);
+int sgdlm_set_log_level(sgdlm_handle h, int level);   /* RcppWrapper.cpp:834-839 */
+int sgdlm_get_log_level(sgdlm_handle h, int *level);  /* RcppWrapper.cpp:827-832 */
+/* Last error message of this handle (empty string if none). */
+const char *sgdlm_last_error(sgdlm_handle h);
+
+/* ---- fused device-resident filter step (GB300 path; asynchronous) ----
+ * One README time step (README.md:103-154) on the handle's stream with no host
+ * synchronisation: computePosterior(y, F) -> computeVBPosterior(nsim) ->
+ * setPosteriorParameters(VB) if ESS > ess_threshold -> computePrior() ->
+ * computeForecast(nsim, x_tp1).  All pointers are device pointers:
+ *   d_y (m), d_F (P x m), d_x (P x m, may be NULL: no forecast),
+ *   d_forecast (m x nsim, may be NULL), d_is_weights (nsim, may be NULL),
+ *   d_step_stats (8 doubles: ESS, sum_det, accepted, max_log_det, ...; may be NULL).
+ * Requires the prior state and initialised simulation memory.  The host-side
+ * prior/posterior flag ends in the prior state, as after the reference's step. */
+int sgdlm_filter_step_device(sgdlm_handle h, const double *d_y, const double *d_F,
+                             const double *d_x, double ess_threshold, double *d_forecast,
+                             double *d_is_weights, double *d_step_stats);
+/* The handle's CUDA stream (cudaStream_t), for events and graph capture. */
+int sgdlm_get_stream(sgdlm_handle h, void **stream);
+/* Blocks until the handle's stream is idle. */
+int sgdlm_synchronize(sgdlm_handle h);
+/* Kernel launches issued by this handle so far (for launch accounting). */
+int sgdlm_get_launch_count(sgdlm_handle h, uint64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGDLM_GB300_H_ */

@@ -1,0 +1,367 @@
+"""Parity of the GB300 CUDA path with the oracle and the reference-kernel fixtures.
+
+Every call goes through the C ABI (ctypes -> libsgdlm_gb300.so).  Tolerances:
+  FP64 mode  : deterministic steps 1e-12 relative; sampled steps compared draw by
+               draw on identical Philox streams, 1e-9 relative (CUDA's and glibc's
+               log/sin/cos differ in the last bits, which the LU and moments carry).
+  mixed mode : draws are FP32 (normals within ~1e-6 relative of FP64); per-draw
+               log|det| within 2e-4 absolute of the FP64 oracle on the same draws;
+               VB moments within 1e-3 relative; refined forecast solves within 1e-5
+               relative of the FP64 solve of the same draws.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gpusgdlm_gb300 import SGDLM
+from oracle_model import OracleSGDLM
+
+pytestmark = pytest.mark.gpu
+NAMES = ["readme", "m20"]
+
+
+def na_sp(sp, m):
+    s = sp.astype(np.float64)
+    s[sp >= m * m] = np.nan
+    return s
+
+
+def model_from(g, precision, seed=1234, epoch=0, beta=None, delta=None):
+    P, m = g["sp"].shape
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents(g["p"], na_sp(g["sp"], m))
+    b = np.full(m, 0.95) if beta is None else beta
+    d = np.full((P, P, m), 0.97) if delta is None else delta
+    s.setDiscountFactors(b, d)
+    s.setRngState(seed, epoch)
+    return s
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_posterior_prior_match_reference(built_lib, golden, name):
+    g = golden(f"{name}_posterior_prior.npz")
+    s = model_from(g, "fp64", beta=g["beta"], delta=g["delta"])
+    s.setPriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    s.computePosterior(g["y"], g["F"])
+    post = s.getParameters()
+    np.testing.assert_allclose(post["m"], g["post_m"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(post["C"], g["post_C"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_array_equal(post["n"], g["post_n"])
+    np.testing.assert_allclose(post["s"], g["post_s"], rtol=1e-12)
+    s.computePrior()
+    pr = s.getParameters()
+    np.testing.assert_allclose(pr["C"], g["prior_C"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_array_equal(pr["n"], g["prior_n"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_vb_fp64_matches_reference(built_lib, golden, name):
+    g = golden(f"{name}_vb_forecast.npz")
+    n, seed, epoch = int(g["n"]), int(g["seed"]), int(g["epoch"])
+    s = model_from(g, "fp64", seed=seed, epoch=epoch)
+    s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    vb = s.computeVBPosterior(n, n)
+    d = s.getDraws()
+    lam_o, th_o, _ = oracle.sample(g["p"], g["m_t"], g["C_t"], g["n_t"], g["s_t"], n, seed, epoch)
+    np.testing.assert_allclose(d["lambdas"], lam_o.T, rtol=1e-13)
+    np.testing.assert_allclose(d["thetas"], th_o.transpose(0, 2, 1), rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(vb["IS_weights"], g["w"], rtol=1e-9)
+    np.testing.assert_allclose(vb["sum_det_weights"], g["sum_w"], rtol=1e-9)
+    np.testing.assert_allclose(vb["m"], g["vb_m"], rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(vb["C"], g["vb_C"], rtol=1e-9, atol=1e-15)
+    np.testing.assert_allclose(vb["n"], g["vb_n"], rtol=1e-9)
+    np.testing.assert_allclose(vb["s"], g["vb_s"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_vb_mixed_matches_oracle_on_device_draws(built_lib, golden, name):
+    g = golden(f"{name}_vb_forecast.npz")
+    n, seed, epoch = int(g["n"]), int(g["seed"]), int(g["epoch"])
+    s = model_from(g, "mixed", seed=seed, epoch=epoch)
+    s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    vb = s.computeVBPosterior(n, n)
+    d = s.getDraws()
+    lam_o, th_o, _ = oracle.sample(g["p"], g["m_t"], g["C_t"], g["n_t"], g["s_t"], n, seed, epoch)
+    # FP32 draws of the same stream
+    np.testing.assert_allclose(d["lambdas"], lam_o.T, rtol=2e-5)
+    np.testing.assert_allclose(d["thetas"], th_o.transpose(0, 2, 1), rtol=2e-4, atol=2e-5)
+    lam = np.asfortranarray(d["lambdas"].T)
+    th = np.asfortranarray(d["thetas"].transpose(0, 2, 1))
+    ld = oracle.logdet(g["sp"], th)
+    np.testing.assert_allclose(d["log_dets"], ld, rtol=0, atol=2e-4)
+    w, sw = oracle.weights(ld)
+    np.testing.assert_allclose(vb["IS_weights"], w, rtol=5e-4)
+    ref = oracle.vb(g["p"], g["n_t"], g["s_t"], w, lam, th)
+    np.testing.assert_allclose(vb["m"], ref["m"], rtol=1e-3, atol=1e-5)
+    np.testing.assert_allclose(vb["C"], ref["C"], rtol=1e-3, atol=1e-7)
+    np.testing.assert_allclose(vb["n"], ref["n"], rtol=1e-3)
+    np.testing.assert_allclose(vb["s"], ref["s"], rtol=1e-3)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_forecast_fp64_matches_reference(built_lib, golden, name):
+    g = golden(f"{name}_vb_forecast.npz")
+    n, seed, epoch = int(g["n"]), int(g["seed"]), int(g["epoch"])
+    s = model_from(g, "fp64", seed=seed, epoch=epoch)
+    s.setPriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    out = s.computeForecastDebug(n, n, g["x"])
+    np.testing.assert_allclose(out["y"], g["y_ref"].T, rtol=1e-9, atol=1e-11)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_forecast_mixed_refined(built_lib, golden, name):
+    g = golden(f"{name}_vb_forecast.npz")
+    n, seed, epoch = int(g["n"]), int(g["seed"]), int(g["epoch"])
+    s = model_from(g, "mixed", seed=seed, epoch=epoch)
+    s.setPriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    out = s.computeForecastDebug(n, n, g["x"])
+    lam = np.asfortranarray(out["lambdas"].T)
+    th = np.asfortranarray(out["thetas"].transpose(0, 2, 1))
+    y, _ = oracle.forecast(g["sp"], lam, th, g["x"], seed, epoch)
+    np.testing.assert_allclose(out["y"], y, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_multistep_forecast_matches_oracle(built_lib, golden, precision):
+    g = golden("m20_vb_forecast.npz")
+    P, m = g["sp"].shape
+    n, seed, epoch = 256, 99, 5
+    x3 = np.asfortranarray(np.stack([g["x"] * (1 + 0.1 * k) for k in range(3)], axis=2))
+    s = model_from(g, precision, seed=seed, epoch=epoch)
+    s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    s.computePrior()
+    y = s.computeForecast(n, n, x3)
+    o = OracleSGDLM(g["p"], g["sp"], np.full(m, 0.95), np.full((P, P, m), 0.97), seed=seed, epoch=epoch)
+    o.set_parameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    o.prior()
+    yo = o.forecast(n, x3)
+    assert y.shape == (m, n, 3)
+    if precision == "fp64":
+        np.testing.assert_allclose(y, yo, rtol=1e-8, atol=1e-10)
+    else:
+        np.testing.assert_allclose(y, yo, rtol=2e-3, atol=2e-4)
+    assert s.getRngState()[1] == epoch + 5
+
+
+def readme_inputs(T, seed=20261203):
+    """The README scenario (README.md:48-154) as arrays."""
+    m = 6
+    counts = [2, 0, 1, 3, 1, 2]
+    sim = [[6], [1, 6, 4], [], [1, 2], [], [2, 4]]
+    p = np.array([c + len(s) for c, s in zip(counts, sim)])
+    P = int(p.max())
+    sp = np.full((P, m), np.nan)
+    for j in range(m):
+        for t, par in enumerate(sim[j]):
+            sp[counts[j] + t, j] = j + m * (par - 1)
+    rng = np.random.default_rng(seed)
+    true_means = np.repeat([0, 0.1, 0.2, 0.15, 0.05], T // 5)
+    y = rng.normal(true_means[:, None], 0.025, size=(T, m))
+
+    def predictors(t, yrow):
+        F = np.zeros((P, m), order="F")
+        F[0:2, 0] = [1, y[t - 1, 0]]
+        F[0, 2] = 1
+        F[0:3, 3] = [1, y[t - 1, 3], true_means[t]]
+        F[0, 4] = 1
+        F[0:2, 5] = [1, y[t - 1, 0]]
+        if yrow is not None:
+            for j in range(m):
+                for t2, par in enumerate(sim[j]):
+                    F[counts[j] + t2, j] = yrow[par - 1]
+        return F
+
+    beta = np.full(m, 0.95)
+    Delta = np.full((P, P, m), 0.95)
+    Delta[:, :, 2] = 0.7
+    Delta[:, :, 4] = 0.9999
+    return dict(m=m, P=P, p=p, sp=sp, y=y, predictors=predictors, beta=beta, Delta=Delta)
+
+
+def test_readme_scenario_fp64_matches_oracle(built_lib):
+    """20 steps of the README loop, GPU vs oracle on identical streams."""
+    T, n = 20, 2000
+    d = readme_inputs(100)
+    m, P = d["m"], d["P"]
+    s = SGDLM(1, strict=True, precision="fp64")
+    s.setSimultaneousParents(d["p"], d["sp"])
+    s.setDiscountFactors(d["beta"], d["Delta"])
+    a, R = np.zeros((P, m)), np.repeat((0.05 * np.eye(P))[:, :, None], m, axis=2)
+    s.setPriorParameters(a, R, np.full(m, 3.0), np.full(m, 0.01))
+    s.setRngState(777, 0)
+    spu = np.where(np.isnan(d["sp"]), 2147483648, np.nan_to_num(d["sp"])).astype(np.uint32)
+    o = OracleSGDLM(d["p"], spu, d["beta"], d["Delta"], seed=777, epoch=0)
+    o.set_parameters(a, R, np.full(m, 3.0), np.full(m, 0.01))
+    for t in range(1, T):
+        F = d["predictors"](t, d["y"][t])
+        s.computePosterior(d["y"][t], F)
+        o.posterior(d["y"][t], F)
+        vb = s.computeVBPosterior(n, n)
+        vo = o.vb(n)
+        np.testing.assert_allclose(vb["IS_weights"], vo["IS_weights"], rtol=1e-8)
+        ess = 1 / np.sum(vb["IS_weights"] ** 2)
+        if ess > n / 2:  # README.md:131
+            s.setPosteriorParameters(vb["m"], vb["C"], vb["n"], vb["s"])
+            o.set_parameters(vo["m"], vo["C"], vo["n"], vo["s"])
+        s.computePrior()
+        o.prior()
+        Fn = d["predictors"](t + 1, None)
+        yf = s.computeForecast(n, n, Fn)
+        yo = o.forecast(n, Fn)
+        np.testing.assert_allclose(yf, yo, rtol=1e-7, atol=1e-9)
+    gp = s.getParameters()
+    np.testing.assert_allclose(gp["m"], o.m_t, rtol=1e-7, atol=1e-10)
+    np.testing.assert_allclose(gp["C"], o.C_t, rtol=1e-7, atol=1e-12)
+    np.testing.assert_allclose(gp["n"], o.n_t, rtol=1e-9)
+    np.testing.assert_allclose(gp["s"], o.s_t, rtol=1e-7)
+
+
+def test_state_machine_and_errors(built_lib, golden):
+    g = golden("readme_vb_forecast.npz")
+    P, m = g["sp"].shape
+    s = SGDLM(1, strict=False, precision="mixed")
+    s.computePosterior(np.zeros(m), np.zeros((P, m)))
+    assert s.last_status == 2  # NOT_INIT (memory not initialised)
+    s.setSimultaneousParents(g["p"], na_sp(g["sp"], m))
+    assert s.last_status == 0
+    s.setDiscountFactors(np.full(m, 0.9), np.full((P, P, m + 1), 0.9))
+    assert s.last_status == 1  # BAD_DIM
+    s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    s.computePosterior(np.zeros(m), np.zeros((P, m)))
+    assert s.last_status == 3  # WRONG_STATE: posterior on posterior
+    before = s.getParameters()
+    s.computeForecast(100, 100, g["x"])
+    assert s.last_status == 3  # forecast needs the prior
+    after = s.getParameters()
+    np.testing.assert_array_equal(before["C"], after["C"])
+    s.computePrior()
+    assert s.isPrior()
+    assert s.computeVBPosterior(100, 100) is None and s.last_status == 3
+    bad = na_sp(g["sp"], m)
+    bad[0, 0] = 0.0  # diagonal entry of (I - Gamma)
+    s.setSimultaneousParents(g["p"], bad)
+    assert s.last_status == 6
+    # round trips
+    par = s.getSimultaneousParents()
+    np.testing.assert_array_equal(par["p"], g["p"])
+    np.testing.assert_array_equal(np.isnan(par["sp"]), g["sp"] >= m * m)
+    df = s.getDiscountFactors()
+    np.testing.assert_array_equal(df["beta"], np.zeros(m))  # the bad call changed nothing
+    s.setLogLevel(7)
+    assert s.getLogLevel() == 5
+    s.clearSimulationMemory()
+    assert s.nsim == 0
+
+
+def test_rng_checkpoint_reproducible(built_lib, golden):
+    g = golden("m20_vb_forecast.npz")
+    outs = []
+    for _ in range(2):
+        s = model_from(g, "mixed", seed=42, epoch=11)
+        s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+        outs.append(s.computeVBPosterior(500, 500))
+        assert s.getRngState() == (42, 12)
+    for k in ("m", "C", "n", "s", "IS_weights"):
+        np.testing.assert_array_equal(outs[0][k], outs[1][k])
+
+
+@pytest.mark.parametrize("n", [1, 37, 1000])
+def test_ragged_draw_counts(built_lib, golden, n):
+    g = golden("readme_vb_forecast.npz")
+    s = model_from(g, "fp64", seed=5, epoch=0)
+    s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    vb = s.computeVBPosterior(n, n)
+    lam, th, _ = oracle.sample(g["p"], g["m_t"], g["C_t"], g["n_t"], g["s_t"], n, 5, 0)
+    ld = oracle.logdet(g["sp"], th)
+    w, sw = oracle.weights(ld)
+    np.testing.assert_allclose(vb["IS_weights"], w, rtol=1e-9)
+    np.testing.assert_allclose(vb["sum_det_weights"], sw, rtol=1e-9)
+
+
+def test_single_series_and_empty_predictors(built_lib):
+    """m = 1 with no parents, and a series with p_j = 0."""
+    s = SGDLM(1, strict=True, precision="fp64")
+    s.setSimultaneousParents([2, 0], np.full((2, 2), np.nan))
+    s.setDiscountFactors([0.95, 0.95], np.full((2, 2, 2), 0.95))
+    C = np.zeros((2, 2, 2)); C[:, :, 0] = 0.1 * np.eye(2)
+    s.setPosteriorParameters(np.array([[0.1, 0.0], [0.2, 0.0]]), C, [10.0, 10.0], [0.01, 0.02])
+    s.setRngState(3, 0)
+    vb = s.computeVBPosterior(300, 300)
+    # no simultaneous parents: det = 1 for every draw, uniform weights
+    np.testing.assert_allclose(vb["IS_weights"], 1.0 / 300, rtol=1e-14)
+    np.testing.assert_allclose(vb["sum_det_weights"], 300.0, rtol=1e-14)
+    assert np.all(vb["C"][:, :, 1] == 0.0)
+    o = OracleSGDLM([2, 0], np.full((2, 2), 2147483648, dtype=np.uint32), [0.95, 0.95],
+                    np.full((2, 2, 2), 0.95), seed=3, epoch=0)
+    o.set_parameters(np.array([[0.1, 0.0], [0.2, 0.0]]), C, [10.0, 10.0], [0.01, 0.02])
+    vo = o.vb(300)
+    np.testing.assert_allclose(vb["n"], vo["n"], rtol=1e-9)
+    np.testing.assert_allclose(vb["s"], vo["s"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pivoting_fallback(built_lib, precision):
+    """A large coefficient below the diagonal forces the partial-pivoting redo."""
+    m, P = 3, 1
+    sp = np.array([[0 + 3 * 1, 1 + 3 * 0, 2 + 3 * 0]], dtype=np.float64)  # 0<-1, 1<-0, 2<-0
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents([1, 1, 1], sp)
+    s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
+    mt = np.array([[0.3, 20.0, -15.0]])
+    C = np.full((1, 1, m), 1e-4)
+    s.setPosteriorParameters(mt, C, np.full(m, 20.0), np.full(m, 1.0))
+    s.setRngState(8, 0)
+    vb = s.computeVBPosterior(200, 200)
+    st = s.getStats()
+    assert st["draws_pivoted"] == 200
+    d = s.getDraws()
+    th = np.asfortranarray(d["thetas"].transpose(0, 2, 1))
+    spu = sp.astype(np.uint32)
+    ld = oracle.logdet(spu, th)
+    np.testing.assert_allclose(d["log_dets"], ld, rtol=1e-5 if precision == "mixed" else 1e-12,
+                               atol=1e-5 if precision == "mixed" else 1e-13)
+    assert np.isfinite(vb["n"]).all()
+
+
+def test_fused_device_step_matches_api_sequence(built_lib):
+    torch = pytest.importorskip("torch")
+    d = readme_inputs(100)
+    m, P, n = d["m"], d["P"], 1024
+    a, R = np.zeros((P, m)), np.repeat((0.05 * np.eye(P))[:, :, None], m, axis=2)
+
+    def fresh():
+        s = SGDLM(1, strict=True, precision="mixed")
+        s.setSimultaneousParents(d["p"], d["sp"])
+        s.setDiscountFactors(d["beta"], d["Delta"])
+        s.setPriorParameters(a, R, np.full(m, 3.0), np.full(m, 0.01))
+        s.setRngState(55, 0)
+        return s
+
+    s1, s2 = fresh(), fresh()
+    s2._ensure_sim(n, n)
+    dev = torch.device("cuda:0")
+    for t in range(1, 6):
+        F = d["predictors"](t, d["y"][t])
+        Fn = d["predictors"](t + 1, None)
+        # API sequence, ESS gate as in README.md:131 with threshold n/2
+        s1.computePosterior(d["y"][t], F)
+        vb = s1.computeVBPosterior(n, n)
+        if 1 / np.sum(vb["IS_weights"] ** 2) > n / 2:
+            s1.setPosteriorParameters(vb["m"], vb["C"], vb["n"], vb["s"])
+        s1.computePrior()
+        y1 = s1.computeForecast(n, n, Fn)
+        # fused device step
+        ty = torch.tensor(d["y"][t], dtype=torch.float64, device=dev)
+        tF = torch.tensor(np.asfortranarray(F).ravel(order="F"), dtype=torch.float64, device=dev)
+        tx = torch.tensor(np.asfortranarray(Fn).ravel(order="F"), dtype=torch.float64, device=dev)
+        tyout = torch.zeros(n * m, dtype=torch.float64, device=dev)
+        tst = torch.zeros(8, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        assert s2.filterStepDevice(ty.data_ptr(), tF.data_ptr(), tx.data_ptr(), n / 2,
+                                   tyout.data_ptr(), None, tst.data_ptr())
+        s2.synchronize()
+        y2 = tyout.cpu().numpy().reshape(m, n, order="F")
+        np.testing.assert_array_equal(y1, y2)
+    p1, p2 = s1.getParameters(), s2.getParameters()
+    for k in ("m", "C", "n", "s"):
+        np.testing.assert_array_equal(p1[k], p2[k])
