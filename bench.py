@@ -1,0 +1,409 @@
+"""SGDLM filtering throughput on GB300: time-steps/s at m = 400 with 10k IS draws.
+
+One time step = computePosterior + computeVBPosterior(10k) + ESS-gated
+setPosteriorParameters + computePrior + computeForecast(10k, 1 step), the loop
+of the reference's README (README.md:103-154), at m = 400 series with
+p_j <= 20 (3 external predictors + Uniform{0..17} simultaneous parents).
+Data: synthetic, simulated from a true SGDLM (Gamma off-diagonals ~ N(0, 0.1^2)
+rescaled to spectral radius 0.5, external coefficients ~ N(0, 0.3^2), precisions
+lambda_j ~ Gamma(5, rate 5/400)); priors a = 0, R = 0.1 I, r = 2, c = 0.0025;
+beta = 0.97, Delta = 0.98.  Seeds are recorded in the output line.
+
+  value : fused device-resident step (sgdlm_filter_step_device), inputs staged in
+          HBM before the timed region;
+  e2e   : the same steps through the C ABI with host buffers (pinned), H2D of
+          y_t, F_t, F_t+1 and D2H of the VB results and the forecast draws inside
+          the timed region.
+--impl reference runs the FP64 CPU implementation of the same step (the oracle
+port: the reference has no CPU path and its CUDA build cannot be built on the
+Arm GPU host) on a bounded sample of draws, on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "time-steps/s at m=400, 10k IS draws"
+LU_FLOPS_PER_DRAW = lambda m: 2.0 / 3.0 * m ** 3  # noqa: E731  dense LU of (I - Gamma)
+
+
+# ----------------------------------------------------------------- workload
+def make_workload(m=400, n_ext=3, kmax=17, T=16, seed=20261203):
+    """True-SGDLM synthetic series (the C1 recipe at m series)."""
+    rng = np.random.default_rng(seed)
+    ks = rng.integers(0, kmax + 1, size=m)
+    p = (n_ext + ks).astype(np.uint32)
+    P = int(n_ext + kmax)
+    NA = 2147483648
+    sp = np.full((P, m), NA, dtype=np.uint32, order="F")
+    Gam = np.zeros((m, m))
+    for j in range(m):
+        others = np.delete(np.arange(m), j)
+        pars = rng.choice(others, size=ks[j], replace=False)
+        for t, par in enumerate(pars):
+            sp[n_ext + t, j] = j + m * par
+            Gam[j, par] = rng.normal(0, 0.1)
+    rho = np.max(np.abs(np.linalg.eigvals(Gam)))
+    if rho > 0.5:
+        Gam *= 0.5 / rho
+    phi = rng.normal(0, 0.3, size=(m, n_ext))
+    lam = rng.gamma(5.0, 1.0 / (5.0 / 400.0), size=m)  # E lambda = 400 (sd 0.05)
+    ImG = np.eye(m) - Gam
+    y = np.zeros((T + 2, m))
+    X = np.zeros((T + 2, m, n_ext))
+    for t in range(1, T + 2):
+        X[t, :, 0] = 1.0
+        X[t, :, 1] = y[t - 1]
+        X[t, :, 2] = rng.normal(0, 1, m)
+        nu = (X[t] * phi).sum(1) + rng.normal(0, 1, m) / np.sqrt(lam)
+        y[t] = np.linalg.solve(ImG, nu)
+
+    def F_of(t, with_parents=True):
+        F = np.zeros((P, m), order="F")
+        F[:n_ext, :] = X[t].T
+        if with_parents:
+            for j in range(m):
+                for k in range(n_ext, p[j]):
+                    F[k, j] = y[t, sp[k, j] // m]
+        return F
+
+    return dict(m=m, P=P, p=p, sp=sp, y=y, F_of=F_of, seed=seed, n_ext=n_ext)
+
+
+def prior_arrays(m, P):
+    a = np.zeros((P, m), order="F")
+    R = np.asfortranarray(np.repeat((0.1 * np.eye(P))[:, :, None], m, axis=2))
+    return a, R, np.full(m, 2.0), np.full(m, 0.0025)
+
+
+# --------------------------------------------------------------- clock sampler
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx, self.rows, self.proc = device_index, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) >= 9:
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d, "of measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "of fallback"
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, rank, world):
+    import torch
+
+    from gpusgdlm_gb300 import SGDLM
+    from gpusgdlm_gb300 import _lib as L
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    wl = make_workload(m=args.m, T=args.warmup + args.steps + 4, seed=args.seed + rank)
+    m, P, n = wl["m"], wl["P"], args.nsim
+    s = SGDLM(1, strict=True, precision=args.precision)
+    s.setSimultaneousParents(wl["p"], np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float))
+    s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+    a, R, r, c = prior_arrays(m, P)
+    s.setPriorParameters(a, R, r, c)
+    s.setRngState(1234 + 100 * rank, 0)
+    s._ensure_sim(n, n)
+    lib, h = s._lib, s._h
+    stream = torch.cuda.ExternalStream(s.stream(), device=dev)
+    ess_thr = n / 2.0
+
+    # stage every step's inputs in HBM
+    nsteps = args.warmup + args.steps
+    ys = torch.tensor(np.stack([wl["y"][t] for t in range(1, nsteps + 1)]), dtype=torch.float64, device=dev)
+    Fs = torch.tensor(np.stack([wl["F_of"](t).ravel(order="F") for t in range(1, nsteps + 1)]),
+                      dtype=torch.float64, device=dev)
+    Xs = torch.tensor(np.stack([wl["F_of"](t + 1, False).ravel(order="F") for t in range(1, nsteps + 1)]),
+                      dtype=torch.float64, device=dev)
+    yout = torch.zeros(n * m, dtype=torch.float64, device=dev)
+    wout = torch.zeros(n, dtype=torch.float64, device=dev)
+    stout = torch.zeros(8, dtype=torch.float64, device=dev)
+
+    def step(t):
+        ok = s.filterStepDevice(ys[t].data_ptr(), Fs[t].data_ptr(), Xs[t].data_ptr(), ess_thr,
+                                yout.data_ptr(), wout.data_ptr(), stout.data_ptr())
+        assert ok
+
+    torch.cuda.synchronize()
+    for t in range(args.warmup):
+        step(t)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = s.launchCount()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for t in range(args.warmup, nsteps):
+        step(t)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = s.launchCount() - launches0
+    barrier(world)
+    clk = clocks.stop()
+    accepted = float(stout[2].item())
+    ess_last = float(stout[0].item())
+
+    # per-kernel timing of the dominant kernel (batched LU) with CUDA events on
+    # the engine's stream, over the same workload (API path records them)
+    lu_ms, vb_ms, sample_ms = [], [], []
+    s.setRngState(999, 0)
+    s.setPosteriorParameters(*[s.getParameters()[k] for k in ("m", "C", "n", "s")])
+    for _ in range(3):
+        s.computeVBPosterior(n, n)
+        st = s.getStats()
+        lu_ms.append(st["ms_lu"]); vb_ms.append(st["ms_vb"]); sample_ms.append(st["ms_sample"])
+        s.setPosteriorParameters(*[s.getParameters()[k] for k in ("m", "C", "n", "s")])
+
+    # e2e through the C ABI with pinned host buffers
+    e2e = run_e2e(args, s, wl, rank, world)
+    return dict(ms=ms, launches=launches, clocks=clk, accepted=accepted, ess=ess_last,
+                lu_ms=statistics.median(lu_ms), vb_ms=statistics.median(vb_ms),
+                sample_ms=statistics.median(sample_ms), e2e=e2e, m=m, P=P)
+
+
+def run_e2e(args, s, wl, rank, world):
+    import torch
+
+    lib, h = s._lib, s._h
+    m, P, n = wl["m"], wl["P"], args.nsim
+    pin = lambda shape: torch.zeros(int(np.prod(shape)), dtype=torch.float64).pin_memory().numpy()  # noqa: E731
+    y_h, F_h, X_h = pin((m,)), pin((P, m)), pin((P, m))
+    om, oC, on, os_, ow, of = pin((P, m)), pin((P, P, m)), pin((m,)), pin((m,)), pin((n,)), pin((m, n))
+    sw = C.c_double()
+    dp = C.POINTER(C.c_double)
+    ptr = lambda a: a.ctypes.data_as(dp)  # noqa: E731
+    a, R, r, c = prior_arrays(m, P)
+    s.setPriorParameters(a, R, r, c)
+    s.setRngState(4321 + rank, 0)
+    h2d = d2h = 0
+    steps = args.e2e_steps
+
+    def one(t):
+        nonlocal h2d, d2h
+        y_h[:] = wl["y"][t]
+        F_h[:] = wl["F_of"](t).ravel(order="F")
+        X_h[:] = wl["F_of"](t + 1, False).ravel(order="F")
+        assert lib.sgdlm_compute_posterior(h, ptr(y_h), ptr(F_h)) == 0
+        assert lib.sgdlm_compute_vb_posterior(h, ptr(om), ptr(oC), ptr(on), ptr(os_), ptr(ow), C.byref(sw)) == 0
+        ess = 1.0 / float(np.dot(ow, ow))
+        b_in = (m + 2 * P * m) * 8
+        b_out = (P * m + P * P * m + 2 * m + n + 1 + n * m) * 8
+        if ess > n / 2:
+            assert lib.sgdlm_set_parameters(h, ptr(om), ptr(oC), ptr(on), ptr(os_)) == 0
+            lib.sgdlm_set_is_prior(h, 0)
+            b_in += (P * m + P * P * m + 2 * m) * 8
+        assert lib.sgdlm_compute_prior(h, 0) == 0
+        assert lib.sgdlm_init_forecast_priors(h) == 0
+        assert lib.sgdlm_compute_forecast(h, ptr(of), ptr(X_h), None, None, 0) == 0
+        return b_in, b_out
+
+    for t in range(1, 3):
+        one(t)
+    barrier(world)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        bi, bo = one(3 + k)
+        h2d += bi; d2h += bo
+    dt = time.perf_counter() - t0
+    return dict(seconds=dt, steps=steps, h2d=h2d / steps, d2h=d2h / steps)
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------- CPU arms
+def run_cpu(m, P_unused, nsim_sample, threads, seed):
+    import oracle
+
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle_model import OracleSGDLM
+
+    wl = make_workload(m=m, T=6, seed=seed)
+    P = wl["P"]
+    o = OracleSGDLM(wl["p"], wl["sp"], np.full(m, 0.97), np.full((P, P, m), 0.98), seed=77, epoch=0,
+                    nthreads=threads)
+    a, R, r, c = prior_arrays(m, P)
+    o.set_parameters(a, R, r, c)
+    t0 = time.perf_counter()
+    o.posterior(wl["y"][1], wl["F_of"](1))
+    vb = o.vb(nsim_sample)
+    if 1.0 / np.sum(vb["IS_weights"] ** 2) > nsim_sample / 2:
+        o.set_parameters(vb["m"], vb["C"], vb["n"], vb["s"])
+    o.prior()
+    o.forecast(nsim_sample, wl["F_of"](2, False))
+    return time.perf_counter() - t0
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(args):
+    threads = host_threads()
+    sample = args.cpu_sample
+    secs = run_cpu(args.m, None, sample, threads, args.seed)
+    per_step = secs * (args.nsim / sample)  # LU work and moments are linear in draws
+    return {"value": 1.0 / per_step, "unit": "time-steps/s", "cores": threads, "kind": "port",
+            "sample": f"one full step with {sample} VB + {sample} forecast draws at m={args.m} "
+                      f"in {secs:.2f} s on {threads} threads (FP64 oracle, OpenMP), "
+                      f"scaled linearly to {args.nsim} draws"}
+
+
+# --------------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--m", type=int, default=400)
+    ap.add_argument("--nsim", type=int, default=10000)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-sample", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    rank = int(os.environ.get("RANK", 0))
+    config = {"workload": f"SGDLM filter step, m={args.m}, p_j<=20 (3 external + Uniform{{0..17}} "
+                          f"simultaneous parents), {args.nsim} IS draws + {args.nsim} 1-step forecast draws",
+              "m": args.m, "max_p": 20, "nsim": args.nsim, "precision": args.precision,
+              "parallelism": f"replicas x{world}", "l2": "working set > L2 (theta draws "
+              f"{args.m * args.nsim * 20 * 4 / 1e6:.0f} MB rewritten per pass)",
+              "seeds": {"data": args.seed, "philox": 1234}}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(args)
+        line = {"metric": METRIC, "value": cb["value"], "unit": "time-steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (true-SGDLM simulation)", "config": config, "impl": "reference",
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "time-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    r = run_gpu(args, rank, world)
+    ms = max_over_ranks(r["ms"], world)
+    e2e_s = max_over_ranks(r["e2e"]["seconds"], world)
+    if rank != 0:
+        return
+    value = world * args.steps / (ms / 1000.0)
+    pk, which = peaks()
+    lu_flops = args.nsim * LU_FLOPS_PER_DRAW(args.m)
+    achieved = lu_flops / (r["lu_ms"] / 1000.0) / 1e12
+    peak = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
+    traffic_file = ROOT / "profiles" / "lu_traffic.json"
+    traffic = None
+    if traffic_file.exists():
+        tj = json.loads(traffic_file.read_text())
+        if tj.get("m") == args.m:
+            traffic = tj["bytes_per_draw"] * args.nsim
+    line = {
+        "metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 draws/LU + f64 state/LSE/Newton" if args.precision == "mixed" else "f64",
+        "data": "synthetic (true-SGDLM simulation)", "config": config,
+        "clocks": r["clocks"], "gpu_launches": r["launches"],
+        "e2e": {"value": world * r["e2e"]["steps"] / e2e_s, "unit": "time-steps/s",
+                "h2d_bytes_per_step": int(r["e2e"]["h2d"]), "d2h_bytes_per_step": int(r["e2e"]["d2h"])},
+        "roofline": {"kernel": "k_lu (batched LU, log|det| of 10k draws)", "bound": "tensor",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "peak_note": f"bf16 dense sustained {which}",
+                     "traffic": traffic, "algorithmic_flops": lu_flops},
+        "phases_ms": {"sample": r["sample_ms"], "lu": r["lu_ms"], "vb": r["vb_ms"]},
+        "is_draws_per_s": value * args.nsim,
+        "ess_last": r["ess"], "accepted_last": r["accepted"],
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -277,7 +277,7 @@ int plan_sim(sgdlm_engine *h, long n, LuPlan *out) {
   LuPlan pl = (h->precision == SGDLM_PRECISION_FP64)
                   ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms)
                   : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms);
-  if (pl.smem > 227 * 1024) {
+  if (pl.smem > 227 * 1024 - 64) {
     char buf[200];
     snprintf(buf, sizeof buf,
              "m = %zu needs %zu bytes of shared memory per LU block at this precision "
@@ -602,7 +602,10 @@ int sgdlm_create(size_t no_gpus, sgdlm_handle *out) {
     return SGDLM_ERR_NO_DEVICE;
   }
   auto h = std::make_unique<sgdlm_engine>();
-  h->device = 0;
+  // The engine lives on the calling thread's current device (device 0 unless the
+  // caller selected another), as the reference's first GPU is device 0
+  // (HostWrapperImpl.cu:39-40).
+  if (cudaGetDevice(&h->device) != cudaSuccess) h->device = 0;
   if (no_gpus != 1)
     h->log(LOG_INFO, "no_gpus = %zu requested; this engine runs on one GPU", no_gpus);
   h->no_gpus = 1;

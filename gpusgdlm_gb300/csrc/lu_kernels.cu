@@ -539,6 +539,7 @@ template <typename T> LuPlan plan_lu(int m, int P, long n, int num_sms) {
   pl.mp = ((m + kB - 1) / kB) * kB;
   pl.block = kThreads;
   pl.smem = Smem(pl.mp, sizeof(T)).total;
+  // k_lu_fallback adds a few bytes of static shared memory on top of pl.smem
   int ctas_per_sm = (int)((227u * 1024u) / (pl.smem + 1024));
   if (ctas_per_sm < 1) ctas_per_sm = 1;
   if (ctas_per_sm > 2) ctas_per_sm = 2;
@@ -556,11 +557,10 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const unsigned *sp,
                const T *theta, T *scratch, double *logdet, int *draw_flags,
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
                GammaRows rows) {
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    configured = true;
-  }
+  // opt in to exactly the shared memory this plan needs (a failure here shows up
+  // as a launch error that the engine reports)
+  if (pl.smem > 48 * 1024)
+    cudaFuncSetAttribute(k_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
   k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.mp, n, sp, theta, scratch,
                                              logdet, draw_flags, x, lambda, key, refine, y, rows);
 }
@@ -570,12 +570,9 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const unsigned
                         const T *theta, T *scratch, double *logdet, int *draw_flags,
                         const double *x, const T *lambda, RngKey key, double *y,
                         GammaRows rows) {
-  static bool configured = false;
-  if (!configured) {
+  if (pl.smem > 48 * 1024)
     cudaFuncSetAttribute(k_lu_fallback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
-    configured = true;
-  }
+                         (int)pl.smem);
   k_lu_fallback<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.mp, n, sp, theta,
                                                       scratch, logdet, draw_flags, x,
                                                       lambda, key, y, rows);

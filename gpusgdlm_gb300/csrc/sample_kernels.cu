@@ -159,13 +159,11 @@ void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                    T *lambda, T *theta, int *draw_flags) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
   const size_t smem = sample_smem<T>(P);
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_sample<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    cudaFuncSetAttribute(k_sample<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    cudaFuncSetAttribute(k_sample<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    cudaFuncSetAttribute(k_sample<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    configured = true;
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_sample<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_sample<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_sample<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_sample<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
   if (P <= 8)
     k_sample<T, 8><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
@@ -188,13 +186,11 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
                    bool compat_beta_no_boost, T *lambda, T *theta, int *draw_flags) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
   const size_t smem = ((size_t)P * P + (size_t)kSampleThreads * P) * sizeof(T);
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_evolve<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    cudaFuncSetAttribute(k_evolve<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    cudaFuncSetAttribute(k_evolve<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    cudaFuncSetAttribute(k_evolve<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 120 * 1024);
-    configured = true;
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_evolve<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_evolve<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_evolve<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_evolve<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
 #define SGDLM_EVOLVE(PM)                                                              \
   k_evolve<T, PM><<<grid, kSampleThreads, smem, s>>>(m, P, n, p, r_t, c_t, beta, UW, \

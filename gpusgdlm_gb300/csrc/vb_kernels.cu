@@ -333,6 +333,10 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
   if (lane == 0) {
     const double El = mean_lambda[j], Ell = mean_log_lambda[j];
     const double pd = (double)p[j];
+    // When the weights collapse onto fewer draws than p_j, V is singular to
+    // working precision and V^-1 is noise; tr(V^-1 V) = p_j is then used as is.
+    bool singular_v = s_bad != 0 || !(fabs(q - (double)pj) <= 1e-8 * (double)(pj > 0 ? pj : 1));
+    if (singular_v) q = (double)pj;
     double mn = n_t[j];
     double fun, dfun, step = 0.0;
     size_t iter = 0;
@@ -343,8 +347,10 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
       step = fun / dfun;
       if (step > mn) step = .5 * mn;
     } while (fabs(fun) > 1e-6 && iter++ < 50);
-    int fl = s_bad ? 1 : 0;
-    if (iter >= 50) {
+    int fl = singular_v ? 1 : 0;
+    // A non-finite iterate ends the reference's loop through the NaN comparison and
+    // would be returned as is; it is treated as non-convergence instead.
+    if (iter >= 50 || !(fabs(mn) < INFINITY)) {
       mn = n_t[j];
       fl |= 2;
     }
@@ -400,15 +406,13 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
                                              mean_log_lambda, mbar_full);
   const size_t npairs = (size_t)P * (P + 1) / 2;
   const size_t smem_b = npairs * sizeof(double) + ((size_t)P + (size_t)kSub * P) * sizeof(T) + 16;
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_vb_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_vb_fin, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    configured = true;
-  }
+  const size_t smem_f = ((size_t)P * P * 3 + P) * sizeof(double);
+  if (smem_b > 48 * 1024)
+    cudaFuncSetAttribute(k_vb_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+  if (smem_f > 48 * 1024)
+    cudaFuncSetAttribute(k_vb_fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
   k_vb_b<T><<<grid, kVbThreads, smem_b, s>>>(m, P, n, p, w, lambda, theta, mbar_full,
                                              scr.part_b);
-  const size_t smem_f = ((size_t)P * P * 3 + P) * sizeof(double);
   k_vb_fin<<<m, 32, smem_f, s>>>(m, P, chunks, p, n_t, s_t, scr.part_b, mean_lambda,
                                  mean_log_lambda, mbar_full, mean_m, mean_C, mean_n,
                                  mean_s, mean_Q, series_flags);

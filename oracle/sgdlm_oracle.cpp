@@ -443,7 +443,9 @@ void orc_vb(int m, int P, const unsigned *p, const double *n_t, const double *s_
       step = fun / dfun;
       if (step > mn) step = .5 * mn;
     } while (std::fabs(fun) > 1e-6 && iter++ < 50);
-    if (iter >= 50) mn = n_t[j];
+    // iteration cap -> prior shape (kernel_functions.cuh:1062-1066); a non-finite
+    // iterate (which the reference would return) is treated the same way
+    if (iter >= 50 || !std::isfinite(mn)) mn = n_t[j];
     double sb = (mn + pd - Qb) / (mn * El);  // compute_mean_s_t (:1071-1085)
     if (sb < 0) sb = s_t[j];
     mean_n[j] = mn;

@@ -9,6 +9,8 @@ Every call goes through the C ABI (ctypes -> libsgdlm_gb300.so).  Tolerances:
                VB moments within 1e-3 relative; refined forecast solves within 1e-5
                relative of the FP64 solve of the same draws.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -220,8 +222,14 @@ def test_state_machine_and_errors(built_lib, golden):
     g = golden("readme_vb_forecast.npz")
     P, m = g["sp"].shape
     s = SGDLM(1, strict=False, precision="mixed")
+    # as in RcppWrapper.cpp:302-306 the dimension check (m = 0 so far) comes first
     s.computePosterior(np.zeros(m), np.zeros((P, m)))
-    assert s.last_status == 2  # NOT_INIT (memory not initialised)
+    assert s.last_status == 1
+    # the engine itself refuses before initMemory (HostWrapperImpl.cu:1240-1246)
+    y, F = np.zeros(m), np.zeros((P, m), order="F")
+    dp = ctypes.POINTER(ctypes.c_double)
+    st = s._lib.sgdlm_compute_posterior(s._h, y.ctypes.data_as(dp), F.ctypes.data_as(dp))
+    assert st == 2  # NOT_INIT
     s.setSimultaneousParents(g["p"], na_sp(g["sp"], m))
     assert s.last_status == 0
     s.setDiscountFactors(np.full(m, 0.9), np.full((P, P, m + 1), 0.9))
@@ -365,3 +373,65 @@ def test_fused_device_step_matches_api_sequence(built_lib):
     p1, p2 = s1.getParameters(), s2.getParameters()
     for k in ("m", "C", "n", "s"):
         np.testing.assert_array_equal(p1[k], p2[k])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_benchmark_size_m400(built_lib, precision):
+    """m = 400, p_j <= 20 (the benchmark's shape): a subset of draws against the oracle,
+    plus size-independent properties over all draws."""
+    import bench
+
+    wl = bench.make_workload(m=400, T=4, seed=11)
+    m, P, n = wl["m"], wl["P"], 1024
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents(wl["p"], np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float))
+    s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+    a, R, r, c = bench.prior_arrays(m, P)
+    s.setPriorParameters(a, R, r, c)
+    s.setRngState(21, 0)
+    s.computePosterior(wl["y"][1], wl["F_of"](1))
+    vb = s.computeVBPosterior(n, n)
+    d = s.getDraws()
+    w = vb["IS_weights"]
+    assert np.all(w >= 0) and abs(w.sum() - 1) < 1e-12
+    assert 1 <= 1 / np.sum(w ** 2) <= n
+    k = 12
+    th = np.asfortranarray(d["thetas"][:, :, :k].transpose(0, 2, 1))
+    ld = oracle.logdet(wl["sp"], th)
+    tol = 1e-10 if precision == "fp64" else 5e-4
+    np.testing.assert_allclose(d["log_dets"][:k], ld, rtol=0, atol=tol)
+    for key in ("m", "C", "n", "s"):  # finite even when the weights collapse
+        assert np.all(np.isfinite(vb[key]))
+    s.computePrior()
+    x = wl["F_of"](2, False)
+    out = s.computeForecastDebug(n, n, x)
+    seed, epoch = 21, 1
+    lam = np.asfortranarray(out["lambdas"][:, :k].T)
+    th = np.asfortranarray(out["thetas"][:, :, :k].transpose(0, 2, 1))
+    y, _ = oracle.forecast(wl["sp"], lam, th, x, seed, epoch)
+    np.testing.assert_allclose(out["y"][:, :k], y, rtol=1e-5 if precision == "mixed" else 1e-9,
+                               atol=1e-6 if precision == "mixed" else 1e-11)
+
+
+def test_dag_parents_have_unit_determinant(built_lib):
+    """Parents only among lower-indexed series: (I - Gamma) is unit lower triangular,
+    det = 1 for every draw, the weights are uniform and ESS = n."""
+    m, P, n = 300, 8, 512
+    rng = np.random.default_rng(3)
+    sp = np.full((P, m), np.nan)
+    p = np.zeros(m, dtype=int)
+    for j in range(m):
+        k = min(j, int(rng.integers(0, 6)))
+        pars = rng.choice(j, size=k, replace=False) if k else []
+        p[j] = 2 + k
+        for t, par in enumerate(pars):
+            sp[2 + t, j] = j + m * par
+    s = SGDLM(1, strict=True, precision="mixed")
+    s.setSimultaneousParents(p, sp)
+    s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
+    C = np.repeat((0.05 * np.eye(P))[:, :, None], m, axis=2)
+    s.setPosteriorParameters(np.full((P, m), 0.1), C, np.full(m, 20.0), np.full(m, 0.01))
+    vb = s.computeVBPosterior(n, n)
+    d = s.getDraws()
+    np.testing.assert_allclose(d["log_dets"], 0.0, atol=1e-5)
+    np.testing.assert_allclose(vb["IS_weights"], 1.0 / n, rtol=1e-4)
