@@ -37,13 +37,6 @@ constexpr int kB = 32;          // LU block size
 constexpr int kThreads = 256;   // 16 x 16 thread grid of the trailing update
 constexpr double kPivotThreshold = 8.0;
 
-template <typename T> struct Tile;
-template <> struct Tile<float> {
-  static constexpr int TM = 8, TN = 8;
-};
-template <> struct Tile<double> {
-  static constexpr int TM = 4, TN = 8;
-};
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -125,42 +118,115 @@ __device__ void build_system(int m, int P, int mp, long n, long i,
   __syncthreads();
 }
 
+// 16-byte vectors of the working precision.
+template <typename T> struct Vec;
+template <> struct Vec<float> {
+  static constexpr int W = 4;
+  __device__ static __forceinline__ void ld(const float *p, float *o) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+  __device__ static __forceinline__ void st(float *p, const float *o) {
+    *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+};
+template <> struct Vec<double> {
+  static constexpr int W = 2;
+  __device__ static __forceinline__ void ld(const double *p, double *o) {
+    const double2 v = *reinterpret_cast<const double2 *>(p);
+    o[0] = v.x; o[1] = v.y;
+  }
+  __device__ static __forceinline__ void st(double *p, const double *o) {
+    *reinterpret_cast<double2 *>(p) = make_double2(o[0], o[1]);
+  }
+};
+
 // Register-tiled trailing update A[r0:, r0:] -= Lp Up over an R x R region.
+// 16 x 16 threads; thread (tr, tc) owns rows {tr*W + a, 16W + tr*W + a} and columns
+// {tc*4 + b, 64 + tc*4 + b} of a (32W) x 128 tile, so every shared-memory read is a
+// 16-byte vector and the 8 threads of each access phase read one contiguous
+// 128-byte line (no bank conflicts); global loads are 16-byte vectors, 16 threads
+// covering 256 contiguous bytes of a column.
 template <typename T>
 __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r0, int R,
                                                 const T *__restrict__ Lp,
                                                 const T *__restrict__ Up, int Rmax) {
-  constexpr int TM = Tile<T>::TM, TN = Tile<T>::TN;
-  constexpr int tileM = 16 * TM, tileN = 16 * TN;
+  using V = Vec<T>;
+  constexpr int W = V::W;
+  constexpr int TM = 2 * W, TN = 8;
+  constexpr int tileM = 32 * W, tileN = 128;
   const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
   for (int tile_r = 0; tile_r < R; tile_r += tileM) {
     for (int tile_c = 0; tile_c < R; tile_c += tileN) {
-      const int rr = tile_r + tr * TM;
-      const int cc = tile_c + tc * TN;
-      if (rr >= R || cc >= R) continue;
+      const int ra = tile_r + tr * W, rb = ra + 16 * W;
+      const int ca = tile_c + tc * 4, cb = ca + 64;
+      if (ra >= R || ca >= R) continue;  // chunk b lies beyond chunk a
+      const bool vb = rb < R, wb = cb < R;
       T acc[TM][TN];
-      T *base = A + (size_t)(r0 + rr) + (size_t)mp * (r0 + cc);
 #pragma unroll
       for (int b = 0; b < TN; ++b) {
+        const int col = (b < 4) ? (ca + b) : (cb + b - 4);
+        const bool cv = (b < 4) || wb;
+        T tmp[W];
+        if (cv) {
+          const T *colp = A + (size_t)mp * (r0 + col) + r0;
+          V::ld(colp + ra, tmp);
 #pragma unroll
-        for (int a = 0; a < TM; ++a) acc[a][b] = base[(size_t)mp * b + a];
+          for (int a = 0; a < W; ++a) acc[a][b] = tmp[a];
+          if (vb) {
+            V::ld(colp + rb, tmp);
+#pragma unroll
+            for (int a = 0; a < W; ++a) acc[W + a][b] = tmp[a];
+          } else {
+#pragma unroll
+            for (int a = 0; a < W; ++a) acc[W + a][b] = T(0);
+          }
+        } else {
+#pragma unroll
+          for (int a = 0; a < TM; ++a) acc[a][b] = T(0);
+        }
       }
-#pragma unroll 4
+#pragma unroll 2
       for (int k = 0; k < kB; ++k) {
-        T l[TM], u[TN];
+        T lv[TM], uv[TN];
+        const T *lrow = Lp + k * Rmax;
+        const T *urow = Up + k * Rmax;
+        V::ld(lrow + ra, lv);
+        if (vb) {
+          V::ld(lrow + rb, lv + W);
+        } else {
 #pragma unroll
-        for (int a = 0; a < TM; ++a) l[a] = Lp[k * Rmax + rr + a];
+          for (int a = 0; a < W; ++a) lv[W + a] = T(0);
+        }
 #pragma unroll
-        for (int b = 0; b < TN; ++b) u[b] = Up[k * Rmax + cc + b];
+        for (int q = 0; q < 4; q += W) V::ld(urow + ca + q, uv + q);
+        if (wb) {
+#pragma unroll
+          for (int q = 0; q < 4; q += W) V::ld(urow + cb + q, uv + 4 + q);
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) uv[4 + q] = T(0);
+        }
 #pragma unroll
         for (int a = 0; a < TM; ++a)
 #pragma unroll
-          for (int b = 0; b < TN; ++b) acc[a][b] -= l[a] * u[b];
+          for (int b = 0; b < TN; ++b) acc[a][b] -= lv[a] * uv[b];
       }
 #pragma unroll
       for (int b = 0; b < TN; ++b) {
+        const bool cv = (b < 4) || wb;
+        if (!cv) continue;
+        const int col = (b < 4) ? (ca + b) : (cb + b - 4);
+        T *colp = A + (size_t)mp * (r0 + col) + r0;
+        T tmp[W];
 #pragma unroll
-        for (int a = 0; a < TM; ++a) base[(size_t)mp * b + a] = acc[a][b];
+        for (int a = 0; a < W; ++a) tmp[a] = acc[a][b];
+        V::st(colp + ra, tmp);
+        if (vb) {
+#pragma unroll
+          for (int a = 0; a < W; ++a) tmp[a] = acc[W + a][b];
+          V::st(colp + rb, tmp);
+        }
       }
     }
   }
@@ -258,7 +324,7 @@ __device__ void residual(int m, int P, int mp, long n, long i, GammaRows rows,
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     k_lu(int m, int P, int mp, long n, const unsigned *__restrict__ sp,
          const T *__restrict__ theta, T *__restrict__ scratch, double *__restrict__ logdet,
          int *__restrict__ draw_flags, const double *__restrict__ x,
@@ -305,8 +371,9 @@ __global__ void __launch_bounds__(kThreads)
         const T u = D[lane * (kB + 1) + lane];
         if (!(finite_t(u) && u != T(0))) bad = true;
         ld += warp_sum_d(log(fabs((double)u)));
-        for (int c = 0; c < kB; ++c)
-          A[(size_t)(k0 + lane) + (size_t)mp * (k0 + c)] = D[lane * (kB + 1) + c];
+        if (solve)
+          for (int c = 0; c < kB; ++c)
+            A[(size_t)(k0 + lane) + (size_t)mp * (k0 + c)] = D[lane * (kB + 1) + c];
         if (solve) {
           // right-hand side block: z_k <- L_kk^-1 z_k (unit lower, from shared D)
           T w = z[k0 + lane];
@@ -318,44 +385,50 @@ __global__ void __launch_bounds__(kThreads)
         }
       }
       __syncthreads();
-      // (b) column panel rows r0.. and (c) row panel columns r0..
+      // (b) column panel rows r0.. -> Lp and (c) row panel columns r0.. -> Up, solved
+      // in place in shared memory (thread t owns column t of Lp or Up); the factors
+      // go back to global memory only when a solve needs them later.
       for (int t = tid; t < 2 * R; t += blockDim.x) {
-        T v[kB];
         if (t < R) {
           const int row = r0 + t;
-#pragma unroll
-          for (int c = 0; c < kB; ++c) v[c] = A[(size_t)row + (size_t)mp * (k0 + c)];
-#pragma unroll
+          T *lp = Lp + t;
+#pragma unroll 8
+          for (int c = 0; c < kB; ++c) lp[c * Rmax] = A[(size_t)row + (size_t)mp * (k0 + c)];
           for (int c = 0; c < kB; ++c) {
-            T acc = v[c];
-#pragma unroll
-            for (int cp = 0; cp < c; ++cp) acc -= v[cp] * D[cp * (kB + 1) + c];
+            T acc = lp[c * Rmax];
+#pragma unroll 4
+            for (int cp = 0; cp < c; ++cp) acc -= lp[cp * Rmax] * D[cp * (kB + 1) + c];
             acc = acc / D[c * (kB + 1) + c];
-            v[c] = acc;
+            lp[c * Rmax] = acc;
             if (!(dabs(acc) <= tau)) bad = true;
-          }
-#pragma unroll
-          for (int c = 0; c < kB; ++c) {
-            Lp[c * Rmax + t] = v[c];
-            A[(size_t)row + (size_t)mp * (k0 + c)] = v[c];
+            if (solve) A[(size_t)row + (size_t)mp * (k0 + c)] = acc;
           }
         } else {
           const int tt = t - R;
           const int col = r0 + tt;
           T *colp = A + (size_t)mp * col + k0;
+          T *up = Up + tt;
 #pragma unroll
-          for (int r = 0; r < kB; ++r) v[r] = colp[r];
+          for (int r = 0; r < kB; r += Vec<T>::W) {
+            T v[Vec<T>::W];
+            Vec<T>::ld(colp + r, v);
 #pragma unroll
-          for (int r = 0; r < kB; ++r) {
-            T acc = v[r];
-#pragma unroll
-            for (int rp = 0; rp < r; ++rp) acc -= D[r * (kB + 1) + rp] * v[rp];
-            v[r] = acc;
+            for (int q = 0; q < Vec<T>::W; ++q) up[(r + q) * Rmax] = v[q];
           }
+          for (int r = 1; r < kB; ++r) {
+            T acc = up[r * Rmax];
+#pragma unroll 4
+            for (int rp = 0; rp < r; ++rp) acc -= D[r * (kB + 1) + rp] * up[rp * Rmax];
+            up[r * Rmax] = acc;
+          }
+          if (solve) {
 #pragma unroll
-          for (int r = 0; r < kB; ++r) {
-            Up[r * Rmax + tt] = v[r];
-            colp[r] = v[r];
+            for (int r = 0; r < kB; r += Vec<T>::W) {
+              T v[Vec<T>::W];
+#pragma unroll
+              for (int q = 0; q < Vec<T>::W; ++q) v[q] = up[(r + q) * Rmax];
+              Vec<T>::st(colp + r, v);
+            }
           }
         }
       }
