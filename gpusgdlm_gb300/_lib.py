@@ -102,6 +102,8 @@ SIGNATURES = {
     "sgdlm_get_stream": [_H, C.POINTER(C.c_void_p)],
     "sgdlm_synchronize": [_H],
     "sgdlm_get_launch_count": [_H, _Pu64],
+    "sgdlm_log_det_noalloc": [_sz, _sz, _sz, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                              C.c_void_p],
 }
 
 _lib = None

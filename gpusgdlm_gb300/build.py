@@ -23,6 +23,7 @@ SOURCES = [
     "lu_kernels.cu",
     "vb_kernels.cu",
     "engine.cu",
+    "noalloc.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]

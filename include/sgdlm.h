@@ -147,6 +147,18 @@ const char *sgdlm_last_error(sgdlm_handle h);
 int sgdlm_filter_step_device(sgdlm_handle h, const double *d_y, const double *d_F,
                              const double *d_x, double ess_threshold, double *d_forecast,
                              double *d_is_weights, double *d_step_stats);
+/* log|det(I - Gamma_i)| of n draws for callers that cannot allocate device
+ * memory (no counterpart in the reference).  Inputs and outputs are the
+ * caller's device buffers: d_theta FP32 draws, series-major (m, n, max_p) as the
+ * engine stores them; d_sp the parental sets (max_p x m, as in
+ * sgdlm_set_parental_sets); d_log_det (n doubles) and d_flags (n ints, per-draw
+ * status bits) receive the results.  The LU working matrices live in a 16 MiB
+ * static device array instead of allocated scratch, which limits m to 2048.
+ * The first call on a device looks that array up (make it outside stream
+ * capture); calls that overlap on the GPU share the array and race.  Runs on
+ * `stream` (a cudaStream_t) and returns without synchronising. */
+int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const float *d_theta,
+                          const unsigned *d_sp, double *d_log_det, int *d_flags, void *stream);
 /* The handle's CUDA stream (cudaStream_t), for events and graph capture. */
 int sgdlm_get_stream(sgdlm_handle h, void **stream);
 /* Blocks until the handle's stream is idle. */

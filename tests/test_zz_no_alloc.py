@@ -1,0 +1,87 @@
+"""The allocation-free log|det| entry point (sgdlm_log_det_noalloc).
+
+It serves callers that must not allocate device memory; its LU working
+matrices live in a static device array.  Checked here against the engine's own
+log|det| of the same draws (the regular entry point, which allocates its
+scratch), on two calls in a row, since the static array keeps the previous
+call's contents.  This file runs last so that a failure here comes after every
+other test has run.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gpusgdlm_gb300 import SGDLM
+from gpusgdlm_gb300 import _lib as L
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine_draws(m, P, p, sp, mt, C, n, precision="mixed", seed=17):
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents(p, sp)
+    s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
+    s.setPosteriorParameters(mt, C, np.full(m, 20.0), np.full(m, 0.01))
+    s.setRngState(seed, 0)
+    s.computeVBPosterior(n, n)
+    d = s.getDraws()
+    st = s.getStats()
+    s.close()
+    return d, st
+
+
+def _call_noalloc(m, P, n, theta_sm, sp_u32):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    th = torch.tensor(theta_sm, dtype=torch.float32, device=dev)
+    sp = torch.tensor(sp_u32.view(np.int32).ravel(order="F"), dtype=torch.int32, device=dev)
+    outs = []
+    for _ in range(2):
+        ld = torch.full((n,), np.nan, dtype=torch.float64, device=dev)
+        fl = torch.full((n,), -1, dtype=torch.int32, device=dev)
+        st = L.lib().sgdlm_log_det_noalloc(m, P, n, ctypes.c_void_p(th.data_ptr()),
+                                           ctypes.c_void_p(sp.data_ptr()),
+                                           ctypes.c_void_p(ld.data_ptr()),
+                                           ctypes.c_void_p(fl.data_ptr()), None)
+        assert st == 0
+        torch.cuda.synchronize()
+        outs.append((ld.cpu().numpy(), fl.cpu().numpy()))
+    return outs
+
+
+def _series_major(thetas_ref_layout):
+    # (max_p, m, n) reference layout -> (m, n, max_p) series-major, FP32 exact
+    return np.ascontiguousarray(thetas_ref_layout.transpose(1, 2, 0)).astype(np.float32)
+
+
+def test_noalloc_matches_engine_m400():
+    import bench
+
+    wl = bench.make_workload(m=400, T=3, seed=5)
+    m, P, n = wl["m"], wl["P"], 700
+    sp = np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float)
+    mt = np.full((P, m), 0.05)
+    C = np.repeat((0.002 * np.eye(P))[:, :, None], m, axis=2)
+    d, _ = _engine_draws(m, P, wl["p"], sp, mt, C, n)
+    for ld, fl in _call_noalloc(m, P, n, _series_major(d["thetas"]), wl["sp"]):
+        np.testing.assert_allclose(ld, d["log_dets"], rtol=0, atol=2e-4)
+        assert np.all(fl >= 0)
+
+
+def test_noalloc_matches_engine_with_pivoting():
+    m, P, n = 3, 1, 300
+    sp = np.array([[0 + 3 * 1, 1 + 3 * 0, 2 + 3 * 0]], dtype=np.float64)
+    mt = np.array([[0.3, 20.0, -15.0]])
+    C = np.full((1, 1, m), 1e-4)
+    d, st = _engine_draws(m, P, [1, 1, 1], sp, mt, C, n)
+    assert st["draws_pivoted"] == n
+    for ld, fl in _call_noalloc(m, P, n, _series_major(d["thetas"]), sp.astype(np.uint32)):
+        np.testing.assert_allclose(ld, d["log_dets"], rtol=0, atol=2e-4)
+        assert np.all(fl & 8)  # every draw went through the pivoting redo
+
+
+def test_noalloc_rejects_oversized_m():
+    dummy = ctypes.c_void_p(16)  # never dereferenced: the size check comes first
+    st = L.lib().sgdlm_log_det_noalloc(3000, 4, 10, dummy, dummy, dummy, dummy, None)
+    assert st == 9  # SGDLM_ERR_UNSUPPORTED
