@@ -90,6 +90,8 @@ SIGNATURES = {
     "sgdlm_set_precision": [_H, _i],
     "sgdlm_get_precision": [_H, _Pi],
     "sgdlm_set_compat": [_H, _u],
+    "sgdlm_set_elimination_levels": [_H, _i],
+    "sgdlm_get_elimination_info": [_H, _Pi, _Pi],
     "sgdlm_get_compat": [_H, C.POINTER(C.c_uint)],
     "sgdlm_set_rng_state": [_H, _u64, _u64],
     "sgdlm_get_rng_state": [_H, _Pu64, _Pu64],

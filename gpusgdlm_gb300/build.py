@@ -23,6 +23,7 @@ SOURCES = [
     "lu_kernels.cu",
     "vb_kernels.cu",
     "engine.cu",
+    "elimination.cu",
     "noalloc.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/sgdlm.h"
+#include "elimination.hpp"
 #include "kernels.hpp"
 
 using namespace sgdlm;
@@ -85,6 +86,11 @@ struct sgdlm_engine {
   DevBuf<unsigned> p, sp;
   DevBuf<int> g_rowptr;
   DevBuf<int2> g_ent;
+  // sparse pre-elimination plan of (I - Gamma) (elimination.hpp)
+  int elim_levels = 4;
+  EliminationPlanHost eplan;
+  DevBuf<int> elim_buf;
+  EliminationPlan elim_dev{};
   DevBuf<double> y_t, F_t, x_t;
   DevBuf<double> fm_t, fC_t, fn_t, fs_t, fW_t;
   DevBuf<double> U64;
@@ -203,6 +209,74 @@ int upload_gamma_rows(sgdlm_engine *h) {
   return SGDLM_OK;
 }
 
+// Plans the sparse pre-elimination for the current parental sets and uploads it
+// as one int array.
+int upload_elimination(sgdlm_engine *h) {
+  const int m = (int)h->m, P = (int)h->P;
+  h->eplan = plan_elimination(m, P, h->h_sp, h->elim_levels);
+  const EliminationPlanHost &pl = h->eplan;
+  std::vector<int> buf;
+  std::vector<size_t> offs;
+  auto put = [&](const void *data, size_t n_ints) {
+    while (buf.size() % 4) buf.push_back(0);
+    offs.push_back(buf.size());
+    const int *p = static_cast<const int *>(data);
+    buf.insert(buf.end(), p, p + n_ints);
+  };
+  put(pl.l0_e.data(), pl.l0_e.size());
+  put(pl.lev_entry.data(), pl.lev_entry.size());
+  put(pl.ent_out.data(), pl.ent_out.size());
+  put(pl.ent_base.data(), pl.ent_base.size());
+  put(pl.ent_tptr.data(), pl.ent_tptr.size());
+  put(pl.terms.data(), pl.terms.size() * 3);
+  put(pl.lev_piv.data(), pl.lev_piv.size());
+  put(pl.piv.data(), pl.piv.size());
+  put(pl.lev_fwd_nodes.data(), pl.lev_fwd_nodes.size());
+  put(pl.fwd_node.data(), pl.fwd_node.size());
+  put(pl.fwd_ptr.data(), pl.fwd_ptr.size());
+  put(pl.fwd.data(), pl.fwd.size() * 3);
+  put(pl.lev_bwd_nodes.data(), pl.lev_bwd_nodes.size());
+  put(pl.bwd_node.data(), pl.bwd_node.size());
+  put(pl.bwd_diag.data(), pl.bwd_diag.size());
+  put(pl.bwd_ptr.data(), pl.bwd_ptr.size());
+  put(pl.bwd.data(), pl.bwd.size() * 2);
+  put(pl.core_node.data(), pl.core_node.size());
+  put(pl.core_ent.data(), pl.core_ent.size() * 3);
+  while (buf.size() % 4) buf.push_back(0);
+  CK(h->elim_buf.alloc(buf.size()));
+  CK(cudaMemcpy(h->elim_buf.ptr, buf.data(), buf.size() * sizeof(int), cudaMemcpyHostToDevice));
+  const int *b = h->elim_buf.ptr;
+  EliminationPlan &d = h->elim_dev;
+  d.m = m;
+  d.P = P;
+  d.nlev = pl.nlev;
+  d.nv = pl.nv;
+  d.nnz0 = (int)pl.l0_e.size();
+  d.core_n = pl.core_n;
+  d.n_core_ent = (int)pl.core_ent.size();
+  size_t k = 0;
+  d.l0_e = b + offs[k++];
+  d.lev_entry = b + offs[k++];
+  d.ent_out = b + offs[k++];
+  d.ent_base = b + offs[k++];
+  d.ent_tptr = b + offs[k++];
+  d.terms = reinterpret_cast<const int3 *>(b + offs[k++]);
+  d.lev_piv = b + offs[k++];
+  d.piv = b + offs[k++];
+  d.lev_fwd_nodes = b + offs[k++];
+  d.fwd_node = b + offs[k++];
+  d.fwd_ptr = b + offs[k++];
+  d.fwd = reinterpret_cast<const int3 *>(b + offs[k++]);
+  d.lev_bwd_nodes = b + offs[k++];
+  d.bwd_node = b + offs[k++];
+  d.bwd_diag = b + offs[k++];
+  d.bwd_ptr = b + offs[k++];
+  d.bwd = reinterpret_cast<const int2 *>(b + offs[k++]);
+  d.core_node = b + offs[k++];
+  d.core_ent = reinterpret_cast<const int3 *>(b + offs[k++]);
+  return SGDLM_OK;
+}
+
 int alloc_state(sgdlm_engine *h) {
   const size_t m = h->m, P = h->P;
   CK(h->m_t.alloc(P * m));
@@ -238,7 +312,9 @@ int alloc_state(sgdlm_engine *h) {
   h->h_sp.assign(P * m, 0xFFFFFFFFu);
   // Parental sets default to "no simultaneous parents" (all external).
   CK(cudaMemcpy(h->sp.ptr, h->h_sp.data(), P * m * sizeof(unsigned), cudaMemcpyHostToDevice));
-  return upload_gamma_rows(h);
+  int st = upload_gamma_rows(h);
+  if (st) return st;
+  return upload_elimination(h);
 }
 
 void release_sim(sgdlm_engine *h) {
@@ -268,21 +344,25 @@ void release_all(sgdlm_engine *h) {
   h->sp.release();
   h->g_rowptr.release();
   h->g_ent.release();
+  h->elim_buf.release();
+  h->elim_dev = EliminationPlan{};
   h->series_flags.release();
   h->dev_epoch.release();
   h->mem_init = false;
 }
 
 int plan_sim(sgdlm_engine *h, long n, LuPlan *out) {
+  const int core_n = h->eplan.core_n > 0 ? h->eplan.core_n : (int)h->m;
+  const int nv = h->eplan.nv;
   LuPlan pl = (h->precision == SGDLM_PRECISION_FP64)
-                  ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms)
-                  : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms);
-  if (pl.smem > 227 * 1024 - 64) {
+                  ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv)
+                  : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv);
+  if (pl.smem > 227 * 1024 - 64 || pl.smem_fallback > 227 * 1024 - 64) {
     char buf[200];
     snprintf(buf, sizeof buf,
              "m = %zu needs %zu bytes of shared memory per LU block at this precision "
              "(limit 232448); use the mixed precision or a smaller m",
-             h->m, pl.smem);
+             h->m, std::max(pl.smem, pl.smem_fallback));
     return h->fail(SGDLM_ERR_UNSUPPORTED, buf);
   }
   *out = pl;
@@ -299,7 +379,7 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   h->chunks = (int)vb_chunks((long)nsim);
   CK(h->lambda.alloc(m * nsim * ts));
   CK(h->theta.alloc(m * nsim * P * ts));
-  CK(h->lu_scratch.alloc((size_t)pl.grid * pl.scratch_elems_per_cta * ts));
+  CK(h->lu_scratch.alloc(pl.scratch_elems_total * ts));
   CK(h->logdet.alloc(nsim));
   CK(h->w.alloc(nsim));
   CK(h->y_fc.alloc(nsim * m));
@@ -307,6 +387,20 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   CK(h->part_a.alloc((size_t)h->chunks * m * (P + 2) + m * P));
   CK(h->part_b.alloc((size_t)h->chunks * m * P * P));
   h->nsim = nsim;
+  return SGDLM_OK;
+}
+
+// Re-sizes the LU scratch after the elimination plan changed (simulation memory
+// already allocated).
+int replan_sim(sgdlm_engine *h) {
+  if (!h->sim_init) return SGDLM_OK;
+  LuPlan pl;
+  int st = plan_sim(h, (long)h->nsim, &pl);
+  if (st) return st;
+  if (pl.scratch_elems_total * h->tsize() > h->lu_scratch.count) {
+    CK(h->lu_scratch.alloc(pl.scratch_elems_total * h->tsize()));
+  }
+  h->plan = pl;
   return SGDLM_OK;
 }
 
@@ -355,8 +449,9 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   const long n = (long)h->nsim;
   const bool refine = (h->precision != SGDLM_PRECISION_FP64);
   const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr};
-  launch_lu<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta), as<T>(h->lu_scratch),
-               h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key, refine, y, rows);
+  launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
+               as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
+               refine, y, rows);
   launch_lu_fallback<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta),
                         as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
                         as<T>(h->lambda), key, y, rows);
@@ -794,6 +889,8 @@ int sgdlm_set_parental_sets(sgdlm_handle h, const unsigned *p, const unsigned *s
     if ((st = h2d(h, h->sp.ptr, sp, m * P * sizeof(unsigned)))) return st;
     if ((st = sync(h))) return st;
     if ((st = upload_gamma_rows(h))) return st;
+    if ((st = upload_elimination(h))) return st;
+    if ((st = replan_sim(h))) return st;
   }
   return sync(h);
 }
@@ -908,6 +1005,24 @@ int sgdlm_set_precision(sgdlm_handle h, int precision) {
   }
   return SGDLM_OK;
 }
+int sgdlm_set_elimination_levels(sgdlm_handle h, int levels) {
+  HCHECK(h);
+  if (levels < 0 || levels > 16) return h->fail(SGDLM_ERR_BAD_ARG, "levels must be in 0..16");
+  h->elim_levels = levels;
+  if (!h->mem_init) return SGDLM_OK;
+  cudaStreamSynchronize(h->stream);
+  int st = upload_elimination(h);
+  if (st) return st;
+  return replan_sim(h);
+}
+
+int sgdlm_get_elimination_info(sgdlm_handle h, int *levels, int *core_n) {
+  HCHECK(h);
+  if (levels) *levels = h->eplan.nlev;
+  if (core_n) *core_n = h->eplan.core_n;
+  return SGDLM_OK;
+}
+
 int sgdlm_get_precision(sgdlm_handle h, int *precision) {
   HCHECK(h);
   if (!precision) return SGDLM_ERR_BAD_ARG;

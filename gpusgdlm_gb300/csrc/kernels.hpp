@@ -70,12 +70,17 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
 // (a4)/(a8) batched LU of (I - Gamma_i): log|det| per draw, and optionally the
 // forecast solve y_i = (I - Gamma_i)^-1 nu_i with one refinement step.
 struct LuPlan {
-  int m, P, mp;      // mp = m rounded up to the 32-wide block size
-  int grid, block;   // persistent grid
-  size_t smem;       // dynamic shared memory per CTA
-  size_t scratch_elems_per_cta;
+  int m, P;
+  int mp;              // m rounded up to the 32-wide block size (pivoting redo)
+  int dp;              // dense core rounded up to 32 (fast pass)
+  int grid, block;     // persistent grid of the fast pass
+  int fb_grid;         // grid of the pivoting redo
+  size_t smem, smem_fallback;
+  size_t scratch_elems_per_cta;  // dense core + per-draw values of the sparse levels
+  size_t scratch_elems_total;    // covers both passes
 };
-template <typename T> LuPlan plan_lu(int m, int P, long n, int num_sms);
+// core_n / nv come from the elimination plan (core_n = m, nv = 0 without one).
+template <typename T> LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv);
 // Row-wise list of the Gamma entries of (I - Gamma): for row r, entries
 // rowptr[r] .. rowptr[r+1]-1 are (e = j*P + k, column).  Built on the host from
 // the parental sets; gives the forecast residual a fixed summation order.
@@ -83,9 +88,10 @@ struct GammaRows {
   const int *rowptr;  // m + 1
   const int2 *ent;    // nnz
 };
+struct EliminationPlan;
 template <typename T>
-void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const unsigned *sp,
-               const T *theta, T *scratch, double *logdet, int *draw_flags,
+void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan &ep,
+               const unsigned *sp, const T *theta, T *scratch, double *logdet, int *draw_flags,
                // forecast solve (x == nullptr: log|det| only)
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
                GammaRows rows);

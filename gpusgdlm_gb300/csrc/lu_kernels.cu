@@ -1,5 +1,4 @@
-// Batched LU of (I - Gamma_i), one matrix per draw: log|det| for the importance
-// weights, and for forecasts the solve y_i = (I - Gamma_i)^-1 nu_i.
+// Batched log|det(I - Gamma_i)| and forecast solves y_i = (I - Gamma_i)^-1 nu_i.
 //
 // The reference zeroes 2*nsim_batch dense m x m FP64 matrices in HBM, scatters
 // the parents, calls cublasDgetrfBatched through a pointer array and, for
@@ -7,26 +6,30 @@
 // (rSGDLM/src/SGDLM/SGDLM.cu:231-323, 555-620; kernel_functions.cuh:810-842,
 // 905-926; HostWrapperImpl.cu:375-377).
 //
-// Here a persistent CTA owns one draw at a time and one private m_p x m_p slab of
-// scratch (m_p = m rounded up to 32; the padding is identity, which changes
-// neither det nor the solve).  With one slab per resident CTA the whole working
-// set of the LU (about 100 MB at m = 400 in FP32) stays in the 126 MB L2.
-// The factorisation is a right-looking blocked LU with 32 x 32 blocks:
-//   (a) one warp factors the diagonal block in shared memory;
-//   (b) the column panel L = A U^-1 and (c) the row panel U = L^-1 A, one
-//       row/column per thread, land in shared memory;
-//   (d) the trailing update A -= L U is a register-tiled FMA loop over
-//       128 x 128 tiles (8 x 8 per thread) fed from those shared panels.
-// (I - Gamma) is diagonally dominant for the parent graphs SGDLM is used with, so
-// the blocked pass does not pivot; it checks every multiplier against
-// kPivotThreshold and flags the draw when one is larger (or a pivot is zero or
-// not finite).  Flagged draws are redone by k_lu_fallback with partial pivoting,
-// as getrf would.  |det| does not depend on the pivot order.
-//
-// For forecasts the right-hand side rides along as an extra column held in
-// shared memory, so the factorisation also produces L^-1 nu; a blocked back
-// substitution gives y0, an FP64 residual nu - (I - Gamma) y0 is formed from the
-// sparse parent list, and one refinement solve with the same factors corrects y0.
+// Here a persistent CTA owns one draw at a time and one private slab of scratch.
+//  1. Sparse pre-elimination (elimination.hpp): the host planned levels of
+//     independent sets; the CTA evaluates that program on the draw's values
+//     (vals), accumulating sum log|pivot| of the eliminated nodes.  The
+//     remaining core (about 260 of 400 nodes at m = 400) is scattered into a
+//     dense d_p x d_p matrix (d_p = core size rounded up to 32, identity padding).
+//  2. Right-looking blocked LU of the core with 32 x 32 blocks:
+//     (a) one warp factors the diagonal block in shared memory;
+//     (b) the column panel L = A U^-1 and (c) the row panel U = L^-1 A, solved
+//         in place in shared memory (one row / column per thread);
+//     (d) the trailing update A -= L U: a register-tiled FMA loop over
+//         (32W) x 128 tiles with 16-byte conflict-free shared and global loads.
+//     The blocked pass does not pivot: (I - Gamma) is diagonally dominant in the
+//     filtering regime.  Every multiplier (sparse levels included) is checked
+//     against kPivotThreshold; a draw with a larger one, or a zero / non-finite
+//     pivot, is flagged and redone by k_lu_fallback with partial pivoting on the
+//     full matrix (getrf semantics).  |det| does not depend on the pivot order.
+//  3. Forecasts: the right-hand side goes through the levels' forward program,
+//     rides along the core factorisation, is back-substituted through the core
+//     and the levels; an FP64 residual nu - (I - Gamma) y0 from the sparse parent
+//     rows drives one refinement solve with the same factors.
+#include <algorithm>
+
+#include "elimination.hpp"
 #include "kernels.hpp"
 #include "rng.cuh"
 
@@ -36,7 +39,6 @@ namespace {
 constexpr int kB = 32;          // LU block size
 constexpr int kThreads = 256;   // 16 x 16 thread grid of the trailing update
 constexpr double kPivotThreshold = 8.0;
-
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -48,12 +50,25 @@ template <typename T> __device__ __forceinline__ bool finite_t(T v) {
   return v == v && dabs(v) <= (T)3.0e38;
 }
 
-// Shared-memory carve-up (all offsets in bytes, 16-byte aligned).
+// Deterministic block-wide sum (fixed order); `red` holds 32 doubles.
+__device__ double block_sum_det(double v, double *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum_d(v);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+  return t;
+}
+
+// Shared-memory carve-up (byte offsets, 16-byte aligned).  dp is the padded
+// dense size, m the number of nodes (forecast vectors are node-indexed).
 struct Smem {
   int Rmax;
-  size_t off_D, off_Lp, off_Up, off_z, off_zu, off_nu, off_res, off_red, total;
-  __host__ __device__ Smem(int mp, size_t tsz) {
-    Rmax = mp - kB > 0 ? mp - kB : kB;
+  size_t off_D, off_Lp, off_Up, off_z, off_nu, off_res, off_zf, off_yf, off_yd, off_red, total;
+  __host__ __device__ Smem(int dp, int m, size_t tsz) {
+    Rmax = dp - kB > 0 ? dp - kB : kB;
     size_t o = 0;
     auto take = [&](size_t bytes) {
       const size_t at = o;
@@ -63,26 +78,45 @@ struct Smem {
     off_D = take((size_t)kB * (kB + 1) * tsz);
     off_Lp = take((size_t)kB * Rmax * tsz);
     off_Up = take((size_t)kB * Rmax * tsz);
-    off_z = take((size_t)mp * tsz);
-    off_zu = take((size_t)kB * tsz);
-    off_nu = take((size_t)mp * sizeof(double));
-    off_res = take((size_t)mp * sizeof(double));
+    off_z = take((size_t)dp * tsz);
+    off_nu = take((size_t)m * sizeof(double));
+    off_res = take((size_t)m * sizeof(double));
+    off_zf = take((size_t)m * tsz);
+    off_yf = take((size_t)m * tsz);
+    off_yd = take((size_t)m * tsz);
     off_red = take(64 * sizeof(double));
     total = o;
   }
 };
 
-// Writes the identity plus the scattered -theta entries of draw i into A, and for
-// forecasts nu_i into nu (double) and z (working precision).
-// fillGammas (kernel_functions.cuh:822-842), batchedComputeNuPlusMu (:1156-1178).
+// nu_j = z/sqrt(lambda) + sum over external predictors x_jk theta_jk for draw i
+// (batchedComputeNuPlusMu, kernel_functions.cuh:1156-1178), into nu (double).
 template <typename T>
-__device__ void build_system(int m, int P, int mp, long n, long i,
-                             const unsigned *__restrict__ sp, const T *__restrict__ theta,
-                             T *__restrict__ A, const double *__restrict__ x,
-                             const T *__restrict__ lambda, RngKey key, double *nu, T *z) {
+__device__ void forecast_rhs(int m, int P, long n, long i, const unsigned *__restrict__ sp,
+                             const T *__restrict__ theta, const double *__restrict__ x,
+                             const T *__restrict__ lambda, RngKey key, double *nu) {
+  const uint32_t ep = key_epoch(key);
+  const size_t mm = (size_t)m * m;
+  for (int j = threadIdx.x; j < m; j += blockDim.x) {
+    const U4 g = philox((uint32_t)i, (uint32_t)j, tag_sub(TAG_NU, 0), ep, key.k0, key.k1);
+    T z0, z1;
+    box_muller<T>(g.x, g.y, z0, z1);
+    const T lam = lambda[(size_t)j * n + i];
+    double v = (double)(z0 / dev_sqrt(lam));
+    const T *th = theta + ((size_t)j * n + i) * P;
+    for (int k = 0; k < P; ++k)
+      if ((size_t)sp[(size_t)j * P + k] >= mm) v += x[(size_t)j * P + k] * (double)th[k];
+    nu[j] = v;
+  }
+}
+
+// Writes the identity plus the scattered -theta entries of draw i into the full
+// mp x mp matrix A (fillGammas, kernel_functions.cuh:822-842).
+template <typename T>
+__device__ void build_full(int m, int P, int mp, long n, long i, const unsigned *__restrict__ sp,
+                           const T *__restrict__ theta, T *__restrict__ A) {
   const int tid = threadIdx.x;
-  const size_t elems = (size_t)mp * mp;
-  const size_t n16 = elems * sizeof(T) / 16;
+  const size_t n16 = (size_t)mp * mp * sizeof(T) / 16;
   uint4 *A16 = reinterpret_cast<uint4 *>(A);
   for (size_t e = tid; e < n16; e += blockDim.x) A16[e] = make_uint4(0, 0, 0, 0);
   __syncthreads();
@@ -94,25 +128,6 @@ __device__ void build_system(int m, int P, int mp, long n, long i,
       const int j = e / P, k = e % P;
       const int row = (int)(pos % (unsigned)m), col = (int)(pos / (unsigned)m);
       A[row + (size_t)mp * col] = -theta[((size_t)j * n + i) * P + k];
-    }
-  }
-  if (x != nullptr) {
-    const uint32_t ep = key_epoch(key);
-    for (int r = tid; r < mp; r += blockDim.x) {
-      double v = 0.0;
-      if (r < m) {
-        const int j = r;
-        const U4 g = philox((uint32_t)i, (uint32_t)j, tag_sub(TAG_NU, 0), ep, key.k0, key.k1);
-        T z0, z1;
-        box_muller<T>(g.x, g.y, z0, z1);
-        const T lam = lambda[(size_t)j * n + i];
-        v = (double)(z0 / dev_sqrt(lam));
-        const T *th = theta + ((size_t)j * n + i) * P;
-        for (int k = 0; k < P; ++k)
-          if ((size_t)sp[(size_t)j * P + k] >= mm) v += x[(size_t)j * P + k] * (double)th[k];
-      }
-      nu[r] = v;
-      z[r] = (T)v;
     }
   }
   __syncthreads();
@@ -232,43 +247,30 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
   }
 }
 
-// Unit-lower forward substitution of the 32-vector v (lane r holds v_r) with the
-// diagonal block of A at k0 (strictly lower part = L).
+// Copies the 32 x 32 diagonal block at k0 of the stored factors into D (warp 0).
 template <typename T>
-__device__ __forceinline__ T warp_forward_unit(const T *__restrict__ A, int mp, int k0,
-                                               T v) {
+__device__ __forceinline__ void load_diag_block(const T *__restrict__ A, int mp, int k0, T *D) {
   const int lane = threadIdx.x & 31;
-  for (int c = 0; c < kB; ++c) {
-    const T vc = __shfl_sync(0xffffffffu, v, c);
-    if (lane > c) v -= A[(size_t)(k0 + lane) + (size_t)mp * (k0 + c)] * vc;
-  }
-  return v;
-}
-
-// Upper back substitution of the 32-vector v with the diagonal block at k0.
-template <typename T>
-__device__ __forceinline__ T warp_backward_upper(const T *__restrict__ A, int mp, int k0,
-                                                 T v) {
-  const int lane = threadIdx.x & 31;
-  for (int c = kB - 1; c >= 0; --c) {
-    if (lane == c) v /= A[(size_t)(k0 + c) + (size_t)mp * (k0 + c)];
-    const T vc = __shfl_sync(0xffffffffu, v, c);
-    if (lane < c) v -= A[(size_t)(k0 + lane) + (size_t)mp * (k0 + c)] * vc;
-  }
-  return v;
+  for (int c = 0; c < kB; ++c) D[lane * (kB + 1) + c] = A[(size_t)(k0 + lane) + (size_t)mp * (k0 + c)];
+  __syncwarp();
 }
 
 // Solves U v = v in place (v in shared memory, length mp) with the stored factors.
 template <typename T>
-__device__ void block_back_solve(const T *__restrict__ A, int mp, T *v) {
-  const int tid = threadIdx.x;
+__device__ void block_back_solve(const T *__restrict__ A, int mp, T *v, T *D) {
+  const int tid = threadIdx.x, lane = tid & 31;
   const int nbk = mp / kB;
   for (int kb = nbk - 1; kb >= 0; --kb) {
     const int k0 = kb * kB;
     if (tid < 32) {
-      T w = v[k0 + tid];
-      w = warp_backward_upper(A, mp, k0, w);
-      v[k0 + tid] = w;
+      load_diag_block(A, mp, k0, D);
+      T w = v[k0 + lane];
+      for (int c = kB - 1; c >= 0; --c) {
+        if (lane == c) w /= D[c * (kB + 1) + c];
+        const T wc = __shfl_sync(0xffffffffu, w, c);
+        if (lane < c) w -= D[lane * (kB + 1) + c] * wc;
+      }
+      v[k0 + lane] = w;
     }
     __syncthreads();
     for (int r = tid; r < k0; r += blockDim.x) {
@@ -282,15 +284,19 @@ __device__ void block_back_solve(const T *__restrict__ A, int mp, T *v) {
 
 // Solves L v = v in place (unit lower, stored factors).
 template <typename T>
-__device__ void block_forward_solve(const T *__restrict__ A, int mp, T *v) {
-  const int tid = threadIdx.x;
+__device__ void block_forward_solve(const T *__restrict__ A, int mp, T *v, T *D) {
+  const int tid = threadIdx.x, lane = tid & 31;
   const int nbk = mp / kB;
   for (int kb = 0; kb < nbk; ++kb) {
     const int k0 = kb * kB;
     if (tid < 32) {
-      T w = v[k0 + tid];
-      w = warp_forward_unit(A, mp, k0, w);
-      v[k0 + tid] = w;
+      load_diag_block(A, mp, k0, D);
+      T w = v[k0 + lane];
+      for (int c = 0; c < kB; ++c) {
+        const T wc = __shfl_sync(0xffffffffu, w, c);
+        if (lane > c) w -= D[lane * (kB + 1) + c] * wc;
+      }
+      v[k0 + lane] = w;
     }
     __syncthreads();
     for (int r = k0 + kB + tid; r < mp; r += blockDim.x) {
@@ -302,21 +308,53 @@ __device__ void block_forward_solve(const T *__restrict__ A, int mp, T *v) {
   }
 }
 
-// res = nu - (I - Gamma) y for the unpermuted system, in FP64, one thread per row
-// summing that row's Gamma entries in a fixed order (deterministic).
+// Forward program of the sparse levels on the node-indexed vector z.
 template <typename T>
-__device__ void residual(int m, int P, int mp, long n, long i, GammaRows rows,
-                         const T *__restrict__ theta, const double *nu, const T *y,
-                         double *res) {
-  for (int r = threadIdx.x; r < mp; r += blockDim.x) {
-    double v = 0.0;
-    if (r < m) {
-      v = nu[r] - (double)y[r];
-      for (int q = rows.rowptr[r]; q < rows.rowptr[r + 1]; ++q) {
-        const int2 ec = rows.ent[q];
-        const int j = ec.x / P, k = ec.x % P;
-        v += (double)theta[((size_t)j * n + i) * P + k] * (double)y[ec.y];
+__device__ void levels_forward(const EliminationPlan &ep, const T *__restrict__ vals, T *z) {
+  for (int lev = 0; lev < ep.nlev; ++lev) {
+    for (int g = ep.lev_fwd_nodes[lev] + threadIdx.x; g < ep.lev_fwd_nodes[lev + 1]; g += blockDim.x) {
+      const int r = ep.fwd_node[g];
+      T acc = z[r];
+      for (int q = ep.fwd_ptr[g]; q < ep.fwd_ptr[g + 1]; ++q) {
+        const int3 f = ep.fwd[q];
+        acc -= vals[f.x] / vals[f.z] * z[f.y];
       }
+      z[r] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// Backward program of the sparse levels: y[t] for eliminated nodes from the
+// forward-eliminated z and the already known y of later nodes.
+template <typename T>
+__device__ void levels_backward(const EliminationPlan &ep, const T *__restrict__ vals,
+                                const T *z, T *y) {
+  for (int lev = ep.nlev - 1; lev >= 0; --lev) {
+    for (int g = ep.lev_bwd_nodes[lev] + threadIdx.x; g < ep.lev_bwd_nodes[lev + 1]; g += blockDim.x) {
+      const int t = ep.bwd_node[g];
+      T acc = z[t];
+      for (int q = ep.bwd_ptr[g]; q < ep.bwd_ptr[g + 1]; ++q) {
+        const int2 b = ep.bwd[q];
+        acc -= vals[b.x] * y[b.y];
+      }
+      y[t] = acc / vals[ep.bwd_diag[g]];
+    }
+    __syncthreads();
+  }
+}
+
+// res = nu - (I - Gamma) y in FP64, one thread per row summing that row's Gamma
+// entries in a fixed order (deterministic).
+template <typename T>
+__device__ void residual(int m, int P, long n, long i, GammaRows rows,
+                         const T *__restrict__ theta, const double *nu, const T *y, double *res) {
+  for (int r = threadIdx.x; r < m; r += blockDim.x) {
+    double v = nu[r] - (double)y[r];
+    for (int q = rows.rowptr[r]; q < rows.rowptr[r + 1]; ++q) {
+      const int2 ec = rows.ent[q];
+      const int j = ec.x / P, k = ec.x % P;
+      v += (double)theta[((size_t)j * n + i) * P + k] * (double)y[ec.y];
     }
     res[r] = v;
   }
@@ -325,38 +363,108 @@ __device__ void residual(int m, int P, int mp, long n, long i, GammaRows rows,
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
-    k_lu(int m, int P, int mp, long n, const unsigned *__restrict__ sp,
-         const T *__restrict__ theta, T *__restrict__ scratch, double *__restrict__ logdet,
-         int *__restrict__ draw_flags, const double *__restrict__ x,
-         const T *__restrict__ lambda, RngKey key, bool refine, double *__restrict__ y,
-         GammaRows rows) {
+    k_lu(int m, int P, int dp, size_t per_cta, long n, EliminationPlan ep,
+         const unsigned *__restrict__ sp, const T *__restrict__ theta, T *__restrict__ scratch,
+         double *__restrict__ logdet, int *__restrict__ draw_flags,
+         const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
+         double *__restrict__ y, GammaRows rows) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Smem L(mp, sizeof(T));
+  const Smem L(dp, m, sizeof(T));
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);
   T *Lp = reinterpret_cast<T *>(smem_raw + L.off_Lp);
   T *Up = reinterpret_cast<T *>(smem_raw + L.off_Up);
   T *z = reinterpret_cast<T *>(smem_raw + L.off_z);
   double *nu = reinterpret_cast<double *>(smem_raw + L.off_nu);
   double *res = reinterpret_cast<double *>(smem_raw + L.off_res);
-  int *sflag = reinterpret_cast<int *>(smem_raw + L.off_red);
+  T *zf = reinterpret_cast<T *>(smem_raw + L.off_zf);
+  T *yf = reinterpret_cast<T *>(smem_raw + L.off_yf);
+  T *yd = reinterpret_cast<T *>(smem_raw + L.off_yd);
+  double *red = reinterpret_cast<double *>(smem_raw + L.off_red);
   const int Rmax = L.Rmax;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  T *A = scratch + (size_t)blockIdx.x * mp * mp;
-  const int nbk = mp / kB;
+  T *A = scratch + (size_t)blockIdx.x * per_cta;
+  T *vals = A + (size_t)dp * dp;
+  const int nbk = dp / kB;
   const bool solve = (x != nullptr);
   const T tau = (T)kPivotThreshold;
+  __shared__ int sflag;
 
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
-    if (tid == 0) *sflag = 0;
-    build_system<T>(m, P, mp, n, i, sp, theta, A, x, lambda, key, nu, z);
-    double ld = 0.0;  // warp 0's running sum of log|u_kk|
+    if (tid == 0) sflag = 0;
     bool bad = false;
+    double ld_part = 0.0;  // this thread's share of sum log|pivot| of the levels
+    // ---- build: zero the core, level-0 values, forecast right-hand side
+    const bool planned = (ep.core_ent != nullptr);
+    if (planned) {
+      const size_t n16 = (size_t)dp * dp * sizeof(T) / 16;
+      uint4 *A16 = reinterpret_cast<uint4 *>(A);
+      for (size_t e = tid; e < n16; e += blockDim.x) A16[e] = make_uint4(0, 0, 0, 0);
+      for (int r = tid; r < m; r += blockDim.x) vals[r] = T(1);
+      for (int k = tid; k < ep.nnz0; k += blockDim.x) {
+        const int e = ep.l0_e[k];
+        const int j = e / P, kk = e % P;
+        vals[m + k] = -theta[((size_t)j * n + i) * P + kk];
+      }
+    } else {
+      // no plan: the whole matrix is the core, scattered from the parental sets
+      build_full<T>(m, P, dp, n, i, sp, theta, A);
+    }
+    if (solve) forecast_rhs<T>(m, P, n, i, sp, theta, x, lambda, key, nu);
+    __syncthreads();
+    if (solve) {
+      for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)nu[r];
+    }
+    // ---- sparse levels
+    for (int lev = 0; lev < ep.nlev; ++lev) {
+      for (int q = ep.lev_entry[lev] + tid; q < ep.lev_entry[lev + 1]; q += blockDim.x) {
+        const int base = ep.ent_base[q];
+        T v = base >= 0 ? vals[base] : T(0);
+        for (int t = ep.ent_tptr[q]; t < ep.ent_tptr[q + 1]; ++t) {
+          const int3 tm = ep.terms[t];
+          const T l = vals[tm.x] / vals[tm.z];
+          if (!(dabs(l) <= tau)) bad = true;
+          v -= l * vals[tm.y];
+        }
+        vals[ep.ent_out[q]] = v;
+      }
+      for (int q = ep.lev_piv[lev] + tid; q < ep.lev_piv[lev + 1]; q += blockDim.x) {
+        const T pv = vals[ep.piv[q]];
+        if (!(finite_t(pv) && pv != T(0))) bad = true;
+        ld_part += log(fabs((double)pv));
+      }
+      if (solve) {
+        __syncthreads();
+        for (int g = ep.lev_fwd_nodes[lev] + tid; g < ep.lev_fwd_nodes[lev + 1]; g += blockDim.x) {
+          const int r = ep.fwd_node[g];
+          T acc = zf[r];
+          for (int q = ep.fwd_ptr[g]; q < ep.fwd_ptr[g + 1]; ++q) {
+            const int3 f = ep.fwd[q];
+            acc -= vals[f.x] / vals[f.z] * zf[f.y];
+          }
+          zf[r] = acc;
+        }
+      }
+      __syncthreads();
+    }
+    // ---- dense core: scatter, identity padding, core right-hand side
+    if (planned) {
+      for (int q = tid; q < ep.n_core_ent; q += blockDim.x) {
+        const int3 ce = ep.core_ent[q];
+        A[ce.y + (size_t)dp * ce.z] = vals[ce.x];
+      }
+      for (int r = ep.core_n + tid; r < dp; r += blockDim.x) A[(size_t)r * dp + r] = T(1);
+    }
+    if (solve)
+      for (int r = tid; r < dp; r += blockDim.x)
+        z[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
+    __syncthreads();
+    double ld = 0.0;  // warp 0's running sum of log|u_kk|
     for (int kb = 0; kb < nbk; ++kb) {
-      const int k0 = kb * kB, r0 = k0 + kB, R = mp - r0;
+      const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
       // (a) diagonal block, warp 0, row per lane
       if (warp == 0) {
         for (int c = 0; c < kB; ++c)
-          D[lane * (kB + 1) + c] = A[(size_t)(k0 + lane) + (size_t)mp * (k0 + c)];
+          D[lane * (kB + 1) + c] = A[(size_t)(k0 + lane) + (size_t)dp * (k0 + c)];
         __syncwarp();
         for (int k = 0; k < kB; ++k) {
           const T piv = D[k * (kB + 1) + k];
@@ -371,10 +479,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         const T u = D[lane * (kB + 1) + lane];
         if (!(finite_t(u) && u != T(0))) bad = true;
         ld += warp_sum_d(log(fabs((double)u)));
-        if (solve)
-          for (int c = 0; c < kB; ++c)
-            A[(size_t)(k0 + lane) + (size_t)mp * (k0 + c)] = D[lane * (kB + 1) + c];
         if (solve) {
+          for (int c = 0; c < kB; ++c)
+            A[(size_t)(k0 + lane) + (size_t)dp * (k0 + c)] = D[lane * (kB + 1) + c];
           // right-hand side block: z_k <- L_kk^-1 z_k (unit lower, from shared D)
           T w = z[k0 + lane];
           for (int c = 0; c < kB; ++c) {
@@ -393,7 +500,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
           const int row = r0 + t;
           T *lp = Lp + t;
 #pragma unroll 8
-          for (int c = 0; c < kB; ++c) lp[c * Rmax] = A[(size_t)row + (size_t)mp * (k0 + c)];
+          for (int c = 0; c < kB; ++c) lp[c * Rmax] = A[(size_t)row + (size_t)dp * (k0 + c)];
           for (int c = 0; c < kB; ++c) {
             T acc = lp[c * Rmax];
 #pragma unroll 4
@@ -401,12 +508,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
             acc = acc / D[c * (kB + 1) + c];
             lp[c * Rmax] = acc;
             if (!(dabs(acc) <= tau)) bad = true;
-            if (solve) A[(size_t)row + (size_t)mp * (k0 + c)] = acc;
+            if (solve) A[(size_t)row + (size_t)dp * (k0 + c)] = acc;
           }
         } else {
           const int tt = t - R;
           const int col = r0 + tt;
-          T *colp = A + (size_t)mp * col + k0;
+          T *colp = A + (size_t)dp * col + k0;
           T *up = Up + tt;
 #pragma unroll
           for (int r = 0; r < kB; r += Vec<T>::W) {
@@ -442,38 +549,48 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
             z[r0 + t] -= acc;
           }
         }
-        trailing_update<T>(A, mp, r0, R, Lp, Up, Rmax);
+        trailing_update<T>(A, dp, r0, R, Lp, Up, Rmax);
       }
       __syncthreads();
     }
-    if (bad) atomicOr(sflag, 1);
-    __syncthreads();
-    const bool flagged = (*sflag != 0);
+    if (bad) atomicOr(&sflag, 1);
+    const double ld_levels = block_sum_det(ld_part, red);  // contains __syncthreads
+    const bool flagged = (sflag != 0);
     if (tid == 0) {
-      logdet[i] = ld;
+      logdet[i] = ld + ld_levels;
       if (flagged) atomicOr(&draw_flags[i], DRAW_FLAG_PIVOT);
     }
     if (solve && !flagged) {
-      block_back_solve<T>(A, mp, z);  // z = y0
+      block_back_solve<T>(A, dp, z, D);  // core part of y0
+      for (int r = tid; r < ep.core_n; r += blockDim.x) yf[planned ? ep.core_node[r] : r] = z[r];
+      __syncthreads();
+      levels_backward<T>(ep, vals, zf, yf);
       if (refine) {
-        residual<T>(m, P, mp, n, i, rows, theta, nu, z, res);
-        T *d = Up;  // the row-panel buffer (32 x Rmax >= m_p) holds the correction
-        for (int r = tid; r < mp; r += blockDim.x) d[r] = (T)res[r];
+        residual<T>(m, P, n, i, rows, theta, nu, yf, res);
+        for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)res[r];
         __syncthreads();
-        block_forward_solve<T>(A, mp, d);
-        block_back_solve<T>(A, mp, d);
+        levels_forward<T>(ep, vals, zf);
+        T *d = Up;  // the row-panel buffer (32 x Rmax >= d_p) holds the core correction
+        for (int r = tid; r < dp; r += blockDim.x)
+          d[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
+        __syncthreads();
+        block_forward_solve<T>(A, dp, d, D);
+        block_back_solve<T>(A, dp, d, D);
+        for (int r = tid; r < ep.core_n; r += blockDim.x) yd[planned ? ep.core_node[r] : r] = d[r];
+        __syncthreads();
+        levels_backward<T>(ep, vals, zf, yd);
         for (int r = tid; r < m; r += blockDim.x)
-          y[(size_t)i * m + r] = (double)z[r] + (double)d[r];
+          y[(size_t)i * m + r] = (double)yf[r] + (double)yd[r];
       } else {
-        for (int r = tid; r < m; r += blockDim.x) y[(size_t)i * m + r] = (double)z[r];
+        for (int r = tid; r < m; r += blockDim.x) y[(size_t)i * m + r] = (double)yf[r];
       }
     }
     __syncthreads();
   }
 }
 
-// Partial-pivoting LU for the draws the blocked pass flagged (getrf semantics).
-// Unblocked and slow; it only runs on the rare draws whose (I - Gamma) is not
+// Partial-pivoting LU of the full matrix for the draws the fast pass flagged
+// (getrf semantics).  Unblocked; it runs only on draws whose (I - Gamma) is not
 // diagonally dominant enough for the no-pivot pass.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -483,13 +600,14 @@ __global__ void __launch_bounds__(kThreads)
                   const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
                   double *__restrict__ y, GammaRows rows) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Smem L(mp, sizeof(T));
+  const Smem L(mp, m, sizeof(T));
   T *z = reinterpret_cast<T *>(smem_raw + L.off_z);
   double *nu = reinterpret_cast<double *>(smem_raw + L.off_nu);
   double *res = reinterpret_cast<double *>(smem_raw + L.off_res);
   double *red = reinterpret_cast<double *>(smem_raw + L.off_red);  // 64 doubles
   int *perm = reinterpret_cast<int *>(smem_raw + L.off_Lp);        // mp ints
   T *d = reinterpret_cast<T *>(smem_raw + L.off_Up);               // mp values
+  T *D = reinterpret_cast<T *>(smem_raw + L.off_D);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = blockDim.x >> 5;
   T *A = scratch + (size_t)blockIdx.x * mp * mp;
@@ -499,7 +617,12 @@ __global__ void __launch_bounds__(kThreads)
 
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
     if (!(draw_flags[i] & DRAW_FLAG_PIVOT)) continue;
-    build_system<T>(m, P, mp, n, i, sp, theta, A, x, lambda, key, nu, z);
+    build_full<T>(m, P, mp, n, i, sp, theta, A);
+    if (solve) {
+      forecast_rhs<T>(m, P, n, i, sp, theta, x, lambda, key, nu);
+      __syncthreads();
+      for (int r = tid; r < mp; r += blockDim.x) z[r] = (r < m) ? (T)nu[r] : T(0);
+    }
     for (int r = tid; r < mp; r += blockDim.x) perm[r] = r;
     if (tid == 0) s_singular = false;
     __syncthreads();
@@ -561,8 +684,7 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
       const T piv = A[(size_t)k + (size_t)mp * k];
       ld += log(fabs((double)piv));
-      for (int r = k + 1 + tid; r < mp; r += blockDim.x)
-        A[(size_t)r + (size_t)mp * k] /= piv;
+      for (int r = k + 1 + tid; r < mp; r += blockDim.x) A[(size_t)r + (size_t)mp * k] /= piv;
       __syncthreads();
       const int rem = mp - k - 1;
       for (long e = tid; e < (long)rem * rem; e += blockDim.x) {
@@ -570,8 +692,7 @@ __global__ void __launch_bounds__(kThreads)
         A[(size_t)r + (size_t)mp * c] -= A[(size_t)r + (size_t)mp * k] * A[(size_t)k + (size_t)mp * c];
       }
       if (solve) {
-        for (int r = k + 1 + tid; r < mp; r += blockDim.x)
-          z[r] -= A[(size_t)r + (size_t)mp * k] * z[k];
+        for (int r = k + 1 + tid; r < mp; r += blockDim.x) z[r] -= A[(size_t)r + (size_t)mp * k] * z[k];
       }
       __syncthreads();
     }
@@ -589,12 +710,12 @@ __global__ void __launch_bounds__(kThreads)
       if (s_singular) {
         for (int r = tid; r < m; r += blockDim.x) y[(size_t)i * m + r] = NAN;
       } else {
-        block_back_solve<T>(A, mp, z);
-        residual<T>(m, P, mp, n, i, rows, theta, nu, z, res);
-        for (int r = tid; r < mp; r += blockDim.x) d[r] = (T)res[perm[r]];
+        block_back_solve<T>(A, mp, z, D);
+        residual<T>(m, P, n, i, rows, theta, nu, z, res);
+        for (int r = tid; r < mp; r += blockDim.x) d[r] = (perm[r] < m) ? (T)res[perm[r]] : T(0);
         __syncthreads();
-        block_forward_solve<T>(A, mp, d);
-        block_back_solve<T>(A, mp, d);
+        block_forward_solve<T>(A, mp, d, D);
+        block_back_solve<T>(A, mp, d, D);
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)z[r] + (double)d[r];
       }
@@ -605,37 +726,53 @@ __global__ void __launch_bounds__(kThreads)
 
 }  // namespace
 
-template <typename T> LuPlan plan_lu(int m, int P, long n, int num_sms) {
+template <typename T>
+LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv) {
   LuPlan pl{};
   pl.m = m;
   pl.P = P;
   pl.mp = ((m + kB - 1) / kB) * kB;
+  pl.dp = ((core_n + kB - 1) / kB) * kB;
+  if (pl.dp < kB) pl.dp = kB;
   pl.block = kThreads;
-  pl.smem = Smem(pl.mp, sizeof(T)).total;
-  // k_lu_fallback adds a few bytes of static shared memory on top of pl.smem
+  pl.smem = Smem(pl.dp, m, sizeof(T)).total;
+  pl.smem_fallback = Smem(pl.mp, m, sizeof(T)).total;
   int ctas_per_sm = (int)((227u * 1024u) / (pl.smem + 1024));
   if (ctas_per_sm < 1) ctas_per_sm = 1;
   if (ctas_per_sm > 2) ctas_per_sm = 2;
+  if (sizeof(T) == 8) ctas_per_sm = 1;
   long grid = (long)num_sms * ctas_per_sm;
   if (grid > n) grid = n;
   if (grid < 1) grid = 1;
   pl.grid = (int)grid;
-  pl.scratch_elems_per_cta = (size_t)pl.mp * pl.mp;
-  (void)P;
+  pl.scratch_elems_per_cta = (size_t)pl.dp * pl.dp + (((size_t)nv + 3) / 4) * 4;
+  const size_t total = pl.scratch_elems_per_cta * pl.grid;
+  const size_t full = (size_t)pl.mp * pl.mp;
+  long fb = num_sms;
+  if (fb > n) fb = n;
+  // the redo needs a full m_p x m_p slab per CTA; it shares the slab array
+  if ((size_t)fb * full > total) {
+    const long fit = (long)(total / full);
+    fb = std::max(fit, std::min(fb, 16L));
+  }
+  if (fb < 1) fb = 1;
+  pl.fb_grid = (int)fb;
+  pl.scratch_elems_total = std::max(total, (size_t)pl.fb_grid * full);
   return pl;
 }
 
 template <typename T>
-void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const unsigned *sp,
-               const T *theta, T *scratch, double *logdet, int *draw_flags,
+void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &ep,
+               const unsigned *sp, const T *theta, T *scratch, double *logdet, int *draw_flags,
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
                GammaRows rows) {
   // opt in to exactly the shared memory this plan needs (a failure here shows up
   // as a launch error that the engine reports)
   if (pl.smem > 48 * 1024)
     cudaFuncSetAttribute(k_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
-  k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.mp, n, sp, theta, scratch,
-                                             logdet, draw_flags, x, lambda, key, refine, y, rows);
+  k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta, n, ep,
+                                             sp, theta, scratch, logdet, draw_flags, x, lambda,
+                                             key, refine, y, rows);
 }
 
 template <typename T>
@@ -643,29 +780,28 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const unsigned
                         const T *theta, T *scratch, double *logdet, int *draw_flags,
                         const double *x, const T *lambda, RngKey key, double *y,
                         GammaRows rows) {
-  if (pl.smem > 48 * 1024)
+  if (pl.smem_fallback > 48 * 1024)
     cudaFuncSetAttribute(k_lu_fallback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)pl.smem);
-  k_lu_fallback<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.mp, n, sp, theta,
-                                                      scratch, logdet, draw_flags, x,
-                                                      lambda, key, y, rows);
+                         (int)pl.smem_fallback);
+  k_lu_fallback<T><<<pl.fb_grid, pl.block, pl.smem_fallback, s>>>(
+      pl.m, pl.P, pl.mp, n, sp, theta, scratch, logdet, draw_flags, x, lambda, key, y, rows);
 }
 
-template LuPlan plan_lu<float>(int, int, long, int);
-template LuPlan plan_lu<double>(int, int, long, int);
-template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const unsigned *,
-                               const float *, float *, double *, int *, const double *,
-                               const float *, RngKey, bool, double *, GammaRows);
-template void launch_lu<double>(cudaStream_t, const LuPlan &, long, const unsigned *,
-                                const double *, double *, double *, int *, const double *,
-                                const double *, RngKey, bool, double *, GammaRows);
-template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long,
-                                        const unsigned *, const float *, float *, double *,
-                                        int *, const double *, const float *, RngKey,
-                                        double *, GammaRows);
-template void launch_lu_fallback<double>(cudaStream_t, const LuPlan &, long,
-                                         const unsigned *, const double *, double *,
-                                         double *, int *, const double *, const double *,
-                                         RngKey, double *, GammaRows);
+template LuPlan plan_lu<float>(int, int, long, int, int, int);
+template LuPlan plan_lu<double>(int, int, long, int, int, int);
+template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
+                               const unsigned *, const float *, float *, double *, int *,
+                               const double *, const float *, RngKey, bool, double *, GammaRows);
+template void launch_lu<double>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
+                                const unsigned *, const double *, double *, double *, int *,
+                                const double *, const double *, RngKey, bool, double *,
+                                GammaRows);
+template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long, const unsigned *,
+                                        const float *, float *, double *, int *, const double *,
+                                        const float *, RngKey, double *, GammaRows);
+template void launch_lu_fallback<double>(cudaStream_t, const LuPlan &, long, const unsigned *,
+                                         const double *, double *, double *, int *,
+                                         const double *, const double *, RngKey, double *,
+                                         GammaRows);
 
 }  // namespace sgdlm

@@ -28,6 +28,7 @@
 #include <mutex>
 
 #include "../../include/sgdlm.h"
+#include "elimination.hpp"
 #include "kernels.hpp"
 
 namespace {
@@ -69,10 +70,13 @@ extern "C" int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const flo
     return reject(SGDLM_ERR_DEVICE, "no usable current device");
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return reject(SGDLM_ERR_DEVICE, "cannot query the device");
-  LuPlan pl = plan_lu<float>((int)m, (int)max_p, (long)n, sms);
+  // no elimination plan here (planning needs host memory and a device upload):
+  // the whole matrix is the dense core, scattered straight from d_sp
+  LuPlan pl = plan_lu<float>((int)m, (int)max_p, (long)n, sms, (int)m, 0);
   if (pl.smem > 227 * 1024 - 64) return reject(SGDLM_ERR_UNSUPPORTED, "m too large for one LU block");
   const long max_ctas = (long)(kNoAllocScratchBytes / slab);
   if (pl.grid > max_ctas) pl.grid = (int)max_ctas;
+  if (pl.fb_grid > max_ctas) pl.fb_grid = (int)max_ctas;
   void *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
@@ -93,8 +97,12 @@ extern "C" int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const flo
     return reject(SGDLM_ERR_DEVICE, "cannot clear the flag array");
   const RngKey no_key{0, 0, 0, nullptr};
   const GammaRows no_rows{nullptr, nullptr};
-  launch_lu<float>(s, pl, (long)n, d_sp, d_theta, (float *)scratch, d_log_det, d_flags, nullptr,
-                   nullptr, no_key, false, nullptr, no_rows);
+  EliminationPlan no_plan{};
+  no_plan.m = (int)m;
+  no_plan.P = (int)max_p;
+  no_plan.core_n = (int)m;
+  launch_lu<float>(s, pl, (long)n, no_plan, d_sp, d_theta, (float *)scratch, d_log_det, d_flags,
+                   nullptr, nullptr, no_key, false, nullptr, no_rows);
   launch_lu_fallback<float>(s, pl, (long)n, d_sp, d_theta, (float *)scratch, d_log_det, d_flags,
                             nullptr, nullptr, no_key, nullptr, no_rows);
   const cudaError_t e = cudaGetLastError();

@@ -325,6 +325,15 @@ class SGDLM:
     def setCompat(self, flags: int):
         self._lib.sgdlm_set_compat(self._h, int(flags))
 
+    def setEliminationLevels(self, levels: int):
+        """Sparse pre-elimination levels before the dense LU (0 = dense LU only)."""
+        self._check(self._lib.sgdlm_set_elimination_levels(self._h, int(levels)))
+
+    def getEliminationInfo(self):
+        lv, core = C.c_int(), C.c_int()
+        self._lib.sgdlm_get_elimination_info(self._h, C.byref(lv), C.byref(core))
+        return {"levels": int(lv.value), "core_n": int(core.value)}
+
     def setRngState(self, seed: int, epoch: int = 0):
         self._check(self._lib.sgdlm_set_rng_state(self._h, int(seed), int(epoch)))
 

@@ -122,6 +122,12 @@ int sgdlm_get_draws(sgdlm_handle h, double *lambdas, double *thetas, double *log
 int sgdlm_set_precision(sgdlm_handle h, int precision);
 int sgdlm_get_precision(sgdlm_handle h, int *precision);
 int sgdlm_set_compat(sgdlm_handle h, unsigned flags);
+/* Levels of sparse pre-elimination of (I - Gamma) before the dense LU (default 4;
+ * 0 = dense LU of the whole matrix).  Each level eliminates a greedy independent
+ * set of the parent graph; results are equal up to rounding. */
+int sgdlm_set_elimination_levels(sgdlm_handle h, int levels);
+/* Levels actually planned and the size of the remaining dense core. */
+int sgdlm_get_elimination_info(sgdlm_handle h, int *levels, int *core_n);
 int sgdlm_get_compat(sgdlm_handle h, unsigned *flags);
 /* Random stream: Philox4x32-10 keyed by seed; epoch counts sampling calls.  The
  * reference seeds cuRAND with 1234 + 100*gpu (HostWrapperImpl.cu:63-64) and
