@@ -18,11 +18,11 @@ EliminationPlanHost plan_elimination(int m, int P, const std::vector<unsigned> &
   pl.m = m;
   pl.P = P;
   const size_t mm = (size_t)m * m;
-  // current pattern: row r -> (col -> vals index), col c -> (row -> vals index)
+  // current pattern: row r -> (col -> slot), col c -> (row -> slot)
   std::vector<std::map<int, int>> rows(m), cols(m);
   std::vector<int> diag(m);
-  for (int r = 0; r < m; ++r) diag[r] = r;
-  int nv = m;
+  for (int r = 0; r < m; ++r) diag[r] = (int)kSlotDiag0 + r;
+  int nv = (int)kSlotDiag0 + m;
   for (int e = 0; e < m * P; ++e) {
     const unsigned pos = sp[e];
     if ((size_t)pos >= mm) continue;
@@ -32,15 +32,18 @@ EliminationPlanHost plan_elimination(int m, int P, const std::vector<unsigned> &
     pl.l0_e.push_back(e);
     ++nv;
   }
-  std::vector<char> active(m, 1);
-  int n_active = m;
-  pl.lev_entry.push_back(0);
-  pl.ent_tptr.push_back(0);
   pl.lev_piv.push_back(0);
+  pl.lev_scale.push_back(0);
+  pl.lev_chunk.push_back(0);
+  pl.chunk_tofs.push_back(0);
   pl.lev_fwd_nodes.push_back(0);
   pl.fwd_ptr.push_back(0);
   pl.lev_bwd_nodes.push_back(0);
   pl.bwd_ptr.push_back(0);
+  std::vector<char> active(m, 1);
+  int n_active = m;
+  // slot indices and node numbers are stored in 16 bits
+  if (nv > kMaxSlots || m > 0xFFFF) max_levels = 0;
 
   for (int lev = 0; lev < max_levels; ++lev) {
     // greedy independent set, ascending degree in the symmetrised active graph
@@ -68,65 +71,100 @@ EliminationPlanHost plan_elimination(int m, int P, const std::vector<unsigned> &
     if ((int)S.size() == n_active) S.pop_back();  // keep a non-empty dense core
     if (S.empty() || (double)S.size() < kMinLevelShare * n_active) break;
     std::sort(S.begin(), S.end());
-    // terms of the new entries, in a deterministic order
-    std::map<std::pair<int, int>, std::vector<int3>> acc;
-    for (int t : S) {
+    auto keep = [&](int v) { return active[v] && !inS[v]; };
+    // terms of the updated entries, in a deterministic order
+    std::map<std::pair<int, int>, std::vector<unsigned>> acc;
+    for (int t : S)
       for (auto &rq : cols[t]) {
-        const int r = rq.first;
-        if (!active[r] || inS[r]) continue;
-        for (auto &cq : rows[t]) {
-          const int c = cq.first;
-          if (!active[c] || inS[c]) continue;
-          acc[{r, c}].push_back(make_int3(rq.second, cq.second, diag[t]));
-        }
+        if (!keep(rq.first)) continue;
+        for (auto &cq : rows[t])
+          if (keep(cq.first))
+            acc[{rq.first, cq.first}].push_back(pack16((unsigned)rq.second, (unsigned)cq.second));
       }
+    int fill = 0;
+    for (auto &kv : acc) {
+      const int r = kv.first.first, c = kv.first.second;
+      if (r != c && !rows[r].count(c)) ++fill;
     }
-    // forward and backward solve programs use this level's values
-    std::map<int, std::vector<int3>> fwd_by_row;
+    if (nv + fill > kMaxSlots) break;  // the slots would not fit 16 bits
+
+    for (int t : S) pl.piv.push_back(diag[t]);
     for (int t : S)
       for (auto &rq : cols[t])
-        if (active[rq.first] && !inS[rq.first])
-          fwd_by_row[rq.first].push_back(make_int3(rq.second, t, diag[t]));
+        if (keep(rq.first)) pl.scale.push_back(pack16((unsigned)rq.second, (unsigned)diag[t]));
+    // forward program, grouped by the updated node
+    std::map<int, std::vector<unsigned>> fwd_by_row;
+    for (int t : S)
+      for (auto &rq : cols[t])
+        if (keep(rq.first)) fwd_by_row[rq.first].push_back(pack16((unsigned)rq.second, (unsigned)t));
     for (auto &kv : fwd_by_row) {
       pl.fwd_node.push_back(kv.first);
-      for (const int3 &f : kv.second) pl.fwd.push_back(f);
+      for (unsigned f : kv.second) pl.fwd.push_back(f);
       pl.fwd_ptr.push_back((int)pl.fwd.size());
     }
     for (int t : S) {
-      pl.piv.push_back(diag[t]);
       pl.bwd_node.push_back(t);
       pl.bwd_diag.push_back(diag[t]);
       for (auto &cq : rows[t])
-        if (active[cq.first] && !inS[cq.first]) pl.bwd.push_back(make_int2(cq.second, cq.first));
+        if (keep(cq.first)) pl.bwd.push_back(pack16((unsigned)cq.second, (unsigned)cq.first));
       pl.bwd_ptr.push_back((int)pl.bwd.size());
     }
+    // entries: updated in place, or a fresh slot for fill-in (base = constant 0)
+    struct Entry {
+      unsigned out, base;
+      const std::vector<unsigned> *terms;
+    };
+    std::vector<Entry> ents;
+    ents.reserve(acc.size());
     for (auto &kv : acc) {
       const int r = kv.first.first, c = kv.first.second;
-      int base;
+      int slot;
+      unsigned base;
       if (r == c) {
-        base = diag[r];
+        slot = diag[r];
+        base = (unsigned)slot;
       } else {
         auto it = rows[r].find(c);
-        base = (it == rows[r].end()) ? -1 : it->second;
+        if (it != rows[r].end()) {
+          slot = it->second;
+          base = (unsigned)slot;
+        } else {
+          slot = nv++;
+          base = kSlotZero;
+          rows[r][c] = slot;
+          cols[c][r] = slot;
+        }
       }
-      const int q = nv++;
-      pl.ent_out.push_back(q);
-      pl.ent_base.push_back(base);
-      for (const int3 &tm : kv.second) pl.terms.push_back(tm);
-      pl.ent_tptr.push_back((int)pl.terms.size());
-      if (r == c) {
-        diag[r] = q;
-      } else {
-        rows[r][c] = q;
-        cols[c][r] = q;
+      ents.push_back(Entry{(unsigned)slot, base, &kv.second});
+      pl.n_terms += kv.second.size();
+    }
+    // chunks of 32 lanes with similar term counts
+    std::stable_sort(ents.begin(), ents.end(), [](const Entry &a, const Entry &b) {
+      return a.terms->size() > b.terms->size();
+    });
+    for (size_t c0 = 0; c0 < ents.size(); c0 += 32) {
+      size_t K = 0;
+      for (size_t l = 0; l < 32 && c0 + l < ents.size(); ++l) K = std::max(K, ents[c0 + l].terms->size());
+      const size_t tofs = pl.terms.size();
+      pl.terms.resize(tofs + 32 * K, pack16(kSlotZero, kSlotZero));
+      for (size_t l = 0; l < 32; ++l) {
+        if (c0 + l < ents.size()) {
+          const Entry &e = ents[c0 + l];
+          pl.ent.push_back(pack16(e.out, e.base));
+          for (size_t k = 0; k < e.terms->size(); ++k) pl.terms[tofs + 32 * k + l] = (*e.terms)[k];
+        } else {
+          pl.ent.push_back(pack16(kSlotNone, kSlotZero));
+        }
       }
+      pl.chunk_tofs.push_back((int)pl.terms.size());
     }
     for (int t : S) {
       active[t] = 0;
       --n_active;
     }
-    pl.lev_entry.push_back((int)pl.ent_out.size());
     pl.lev_piv.push_back((int)pl.piv.size());
+    pl.lev_scale.push_back((int)pl.scale.size());
+    pl.lev_chunk.push_back((int)pl.chunk_tofs.size() - 1);
     pl.lev_fwd_nodes.push_back((int)pl.fwd_node.size());
     pl.lev_bwd_nodes.push_back((int)pl.bwd_node.size());
     ++pl.nlev;
@@ -139,11 +177,17 @@ EliminationPlanHost plan_elimination(int m, int P, const std::vector<unsigned> &
       pl.core_node.push_back(r);
     }
   pl.core_n = (int)pl.core_node.size();
-  for (int r : pl.core_node) {
-    const int pr = pl.node_core[r];
-    pl.core_ent.push_back(make_int3(diag[r], pr, pr));
-    for (auto &cq : rows[r])
-      if (active[cq.first]) pl.core_ent.push_back(make_int3(cq.second, pr, pl.node_core[cq.first]));
+  pl.dp = std::max(32, (pl.core_n + 31) / 32 * 32);
+  if (pl.nlev > 0) {
+    const size_t dp = (size_t)pl.dp;
+    pl.core_map.assign(dp * dp, (uint16_t)kSlotZero);
+    for (int r : pl.core_node) {
+      const int pr = pl.node_core[r];
+      pl.core_map[pr + dp * pr] = (uint16_t)diag[r];
+      for (auto &cq : rows[r])
+        if (active[cq.first]) pl.core_map[pr + dp * pl.node_core[cq.first]] = (uint16_t)cq.second;
+    }
+    for (size_t pr = pl.core_n; pr < dp; ++pr) pl.core_map[pr + dp * pr] = (uint16_t)kSlotOne;
   }
   return pl;
 }

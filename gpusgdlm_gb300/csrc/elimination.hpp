@@ -5,17 +5,28 @@
 // host plans a sequence of elimination levels: at each level it picks a greedy
 // independent set S of the current sparsity graph (no edge between two members
 // of S, so the S x S block is diagonal) and eliminates it,
-//   M'[r][c] = M[r][c] - sum_{t in S} M[r][t] M[t][c] / M[t][t],
+//   L[r][t]  = M[r][t] / M[t][t]                       (t in S, r not in S)
+//   M'[r][c] = M[r][c] - sum_{t in S} L[r][t] M[t][c],
 //   log|det M| = sum_{t in S} log|M[t][t]| + log|det M'|.
 // This is a symmetric permutation plus exact block elimination, so |det| is
-// unchanged; what is left (the "core") goes to the blocked dense LU.  At m = 400
-// with ~8.5 parents per series two levels shrink the dense core from 400 to
-// about 260 nodes.
+// unchanged; what is left (the "core") goes to the dense LU.  At m = 400 with
+// ~8.5 parents per series four levels shrink the dense core from 400 to about
+// 210 nodes.
 //
-// The plan is a small program over a per-draw value array `vals`:
-//   vals[0 .. m)          diagonal of (I - Gamma) = 1
-//   vals[m .. m + nnz0)   off-diagonal entries, -theta[e]   (e = j*max_p + k)
-//   then the entries each level creates (in level order).
+// The plan is a small program over a per-draw array of value slots `vals`.
+// Every matrix position owns one slot for its whole life: an entry that a level
+// updates is overwritten in place, a fill-in entry gets a fresh slot, and a
+// multiplier L[r][t] replaces M[r][t] in its slot.  Slot indices fit 16 bits.
+//   slot 0             constant 0 (padding terms read it; never written)
+//   slot 1             constant 1 (identity padding of the dense core)
+//   slots 2 .. 2+m     diagonal of (I - Gamma) = 1 (then updated in place)
+//   slots 2+m ..       level-0 off-diagonals -theta[e] (e = j*max_p + k)
+//   then the fill-in each level creates.
+// A level runs as: pivots and multipliers (scale), barrier, new entries,
+// barrier.  Entries are grouped in chunks of 32 (one per warp lane), sorted by
+// term count so that a chunk's lanes do the same number of terms; a chunk's
+// terms are stored term-major (term k of lane l at chunk_tofs + 32 k + l) so
+// that each load of the program is one coalesced 128-byte line.
 #pragma once
 #include <cstdint>
 #include <vector>
@@ -24,55 +35,68 @@
 
 namespace sgdlm {
 
+constexpr unsigned kSlotZero = 0, kSlotOne = 1, kSlotDiag0 = 2;
+constexpr unsigned kSlotNone = 0xFFFFu;  // padding lane of a chunk: no store
+constexpr int kMaxSlots = 0xFFFF;        // slots 0 .. 0xFFFE
+
+inline unsigned pack16(unsigned lo, unsigned hi) { return (lo & 0xFFFFu) | (hi << 16); }
+
 struct EliminationPlanHost {
   int m = 0, P = 0;
   int nlev = 0;
-  int nv = 0;                      // values per draw
-  std::vector<int> l0_e;           // nnz0 theta indices of the level-0 entries
-  std::vector<int> lev_entry;      // nlev+1 offsets into entries (computed entries per level)
-  std::vector<int> ent_out;        // vals index written by computed entry
-  std::vector<int> ent_base;       // vals index of M[r][c] at the previous level, or -1
-  std::vector<int> ent_tptr;       // term ranges, size #entries + 1
-  std::vector<int3> terms;         // (M[r][t], M[t][c], M[t][t]) vals indices
-  std::vector<int> lev_piv;        // nlev+1 offsets into piv
-  std::vector<int> piv;            // vals index of M[t][t] of eliminated nodes
-  // forward (RHS) program, grouped by the updated node r:
-  //   z[r] -= sum_t M[r][t] / M[t][t] * z[t]
-  std::vector<int> lev_fwd_nodes;  // nlev+1 offsets into fwd_node
-  std::vector<int> fwd_node;       // r
-  std::vector<int> fwd_ptr;        // term ranges per node (size #nodes + 1)
-  std::vector<int3> fwd;           // (vals M[r][t], t, vals M[t][t])
-  // backward program: y[t] = (z[t] - sum M[t][c] y[c]) / M[t][t]
-  std::vector<int> lev_bwd_nodes;  // nlev+1 offsets into bwd_node
-  std::vector<int> bwd_node;       // t
-  std::vector<int> bwd_diag;       // vals M[t][t]
-  std::vector<int> bwd_ptr;        // term ranges per node (size #nodes + 1)
-  std::vector<int2> bwd;           // (vals M[t][c], c)
+  int nv = 0;                        // slots per draw
+  std::vector<int> l0_e;             // theta index e of slot kSlotDiag0 + m + k
+  // per level (nlev + 1 offsets each)
+  std::vector<int> lev_piv;          // -> piv
+  std::vector<int> piv;              // slot of M[t][t] of the eliminated nodes
+  std::vector<int> lev_scale;        // -> scale
+  std::vector<unsigned> scale;       // (slot M[r][t] | slot M[t][t] << 16): M[r][t] /= M[t][t]
+  std::vector<int> lev_chunk;        // -> chunks
+  std::vector<int> chunk_tofs;       // #chunks + 1 offsets into terms (multiples of 32)
+  std::vector<unsigned> ent;         // 32 per chunk: (out slot | base slot << 16)
+  std::vector<unsigned> terms;       // (slot L[r][t] | slot M[t][c] << 16)
+  // forward (right-hand side) program, grouped by the updated node r:
+  //   z[r] -= sum_t L[r][t] z[t]
+  std::vector<int> lev_fwd_nodes;    // -> fwd_node
+  std::vector<int> fwd_node;         // r
+  std::vector<int> fwd_ptr;          // term ranges per node (size #nodes + 1)
+  std::vector<unsigned> fwd;         // (slot L[r][t] | t << 16)
+  // backward program: y[t] = (z[t] - sum_c M[t][c] y[c]) / M[t][t]
+  std::vector<int> lev_bwd_nodes;    // -> bwd_node
+  std::vector<int> bwd_node;         // t
+  std::vector<int> bwd_diag;         // slot M[t][t]
+  std::vector<int> bwd_ptr;          // term ranges per node (size #nodes + 1)
+  std::vector<unsigned> bwd;         // (slot M[t][c] | c << 16)
   // dense core
   int core_n = 0;
-  std::vector<int> core_node;      // core position -> node
-  std::vector<int> node_core;      // node -> core position or -1
-  std::vector<int3> core_ent;      // (vals index, core row, core col), off-diagonal + diagonal
+  int dp = 0;                        // core_n rounded up to 32
+  std::vector<int> core_node;        // core position -> node
+  std::vector<int> node_core;        // node -> core position or -1
+  std::vector<uint16_t> core_map;    // dp x dp (column-major) slot of each core cell
+  size_t n_terms = 0;                // unpadded term count (for reporting)
 };
 
 // Device copy of the plan (pointers into one allocation owned by the engine).
+// core_map == nullptr means "no plan": the whole matrix is the dense core.
 struct EliminationPlan {
-  int m, P, nlev, nv, nnz0, core_n, n_core_ent;
+  int m, P, nlev, nv, nnz0, core_n;
   const int *l0_e;
-  const int *lev_entry, *ent_out, *ent_base, *ent_tptr;
-  const int3 *terms;
   const int *lev_piv, *piv;
+  const int *lev_scale;
+  const unsigned *scale;
+  const int *lev_chunk, *chunk_tofs;
+  const unsigned *ent, *terms;
   const int *lev_fwd_nodes, *fwd_node, *fwd_ptr;
-  const int3 *fwd;
+  const unsigned *fwd;
   const int *lev_bwd_nodes, *bwd_node, *bwd_diag, *bwd_ptr;
-  const int2 *bwd;
+  const unsigned *bwd;
   const int *core_node;
-  const int3 *core_ent;
+  const uint16_t *core_map;
 };
 
 // Builds the plan from the parental sets (sp: max_p x m, entries < m*m address
-// (I - Gamma) at row + m*col).  max_levels = 0 gives the plain dense LU of the
-// whole matrix.
+// (I - Gamma) at row + m*col).  max_levels = 0, or parental sets with more than
+// kMaxSlots values, give no levels (the plain dense LU of the whole matrix).
 EliminationPlanHost plan_elimination(int m, int P, const std::vector<unsigned> &sp,
                                      int max_levels);
 

@@ -224,56 +224,60 @@ int upload_elimination(sgdlm_engine *h) {
     buf.insert(buf.end(), p, p + n_ints);
   };
   put(pl.l0_e.data(), pl.l0_e.size());
-  put(pl.lev_entry.data(), pl.lev_entry.size());
-  put(pl.ent_out.data(), pl.ent_out.size());
-  put(pl.ent_base.data(), pl.ent_base.size());
-  put(pl.ent_tptr.data(), pl.ent_tptr.size());
-  put(pl.terms.data(), pl.terms.size() * 3);
   put(pl.lev_piv.data(), pl.lev_piv.size());
   put(pl.piv.data(), pl.piv.size());
+  put(pl.lev_scale.data(), pl.lev_scale.size());
+  put(pl.scale.data(), pl.scale.size());
+  put(pl.lev_chunk.data(), pl.lev_chunk.size());
+  put(pl.chunk_tofs.data(), pl.chunk_tofs.size());
+  put(pl.ent.data(), pl.ent.size());
+  put(pl.terms.data(), pl.terms.size());
   put(pl.lev_fwd_nodes.data(), pl.lev_fwd_nodes.size());
   put(pl.fwd_node.data(), pl.fwd_node.size());
   put(pl.fwd_ptr.data(), pl.fwd_ptr.size());
-  put(pl.fwd.data(), pl.fwd.size() * 3);
+  put(pl.fwd.data(), pl.fwd.size());
   put(pl.lev_bwd_nodes.data(), pl.lev_bwd_nodes.size());
   put(pl.bwd_node.data(), pl.bwd_node.size());
   put(pl.bwd_diag.data(), pl.bwd_diag.size());
   put(pl.bwd_ptr.data(), pl.bwd_ptr.size());
-  put(pl.bwd.data(), pl.bwd.size() * 2);
+  put(pl.bwd.data(), pl.bwd.size());
   put(pl.core_node.data(), pl.core_node.size());
-  put(pl.core_ent.data(), pl.core_ent.size() * 3);
+  put(pl.core_map.data(), (pl.core_map.size() + 1) / 2);  // two 16-bit slots per int
   while (buf.size() % 4) buf.push_back(0);
   CK(h->elim_buf.alloc(buf.size()));
   CK(cudaMemcpy(h->elim_buf.ptr, buf.data(), buf.size() * sizeof(int), cudaMemcpyHostToDevice));
   const int *b = h->elim_buf.ptr;
+  auto u = [&](size_t k) { return reinterpret_cast<const unsigned *>(b + offs[k]); };
   EliminationPlan &d = h->elim_dev;
+  d = EliminationPlan{};
   d.m = m;
   d.P = P;
   d.nlev = pl.nlev;
-  d.nv = pl.nv;
+  d.nv = pl.nlev > 0 ? pl.nv : 0;
   d.nnz0 = (int)pl.l0_e.size();
-  d.core_n = pl.core_n;
-  d.n_core_ent = (int)pl.core_ent.size();
+  d.core_n = pl.nlev > 0 ? pl.core_n : m;
   size_t k = 0;
   d.l0_e = b + offs[k++];
-  d.lev_entry = b + offs[k++];
-  d.ent_out = b + offs[k++];
-  d.ent_base = b + offs[k++];
-  d.ent_tptr = b + offs[k++];
-  d.terms = reinterpret_cast<const int3 *>(b + offs[k++]);
   d.lev_piv = b + offs[k++];
   d.piv = b + offs[k++];
+  d.lev_scale = b + offs[k++];
+  d.scale = u(k++);
+  d.lev_chunk = b + offs[k++];
+  d.chunk_tofs = b + offs[k++];
+  d.ent = u(k++);
+  d.terms = u(k++);
   d.lev_fwd_nodes = b + offs[k++];
   d.fwd_node = b + offs[k++];
   d.fwd_ptr = b + offs[k++];
-  d.fwd = reinterpret_cast<const int3 *>(b + offs[k++]);
+  d.fwd = u(k++);
   d.lev_bwd_nodes = b + offs[k++];
   d.bwd_node = b + offs[k++];
   d.bwd_diag = b + offs[k++];
   d.bwd_ptr = b + offs[k++];
-  d.bwd = reinterpret_cast<const int2 *>(b + offs[k++]);
+  d.bwd = u(k++);
   d.core_node = b + offs[k++];
-  d.core_ent = reinterpret_cast<const int3 *>(b + offs[k++]);
+  // without levels the whole matrix is the dense core, built from the parental sets
+  d.core_map = pl.nlev > 0 ? reinterpret_cast<const uint16_t *>(b + offs[k]) : nullptr;
   return SGDLM_OK;
 }
 
@@ -352,8 +356,8 @@ void release_all(sgdlm_engine *h) {
 }
 
 int plan_sim(sgdlm_engine *h, long n, LuPlan *out) {
-  const int core_n = h->eplan.core_n > 0 ? h->eplan.core_n : (int)h->m;
-  const int nv = h->eplan.nv;
+  const int core_n = h->elim_dev.core_n > 0 ? h->elim_dev.core_n : (int)h->m;
+  const int nv = h->elim_dev.nv;
   LuPlan pl = (h->precision == SGDLM_PRECISION_FP64)
                   ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv)
                   : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv);

@@ -8,25 +8,32 @@
 //
 // Here a persistent CTA owns one draw at a time and one private slab of scratch.
 //  1. Sparse pre-elimination (elimination.hpp): the host planned levels of
-//     independent sets; the CTA evaluates that program on the draw's values
-//     (vals), accumulating sum log|pivot| of the eliminated nodes.  The
-//     remaining core (about 260 of 400 nodes at m = 400) is scattered into a
-//     dense d_p x d_p matrix (d_p = core size rounded up to 32, identity padding).
-//  2. Right-looking blocked LU of the core with 32 x 32 blocks:
-//     (a) one warp factors the diagonal block in shared memory;
-//     (b) the column panel L = A U^-1 and (c) the row panel U = L^-1 A, solved
-//         in place in shared memory (one row / column per thread);
-//     (d) the trailing update A -= L U: a register-tiled FMA loop over
+//     independent sets; the CTA runs that program over the draw's value slots
+//     (in shared memory when they fit), accumulating sum log|pivot| of the
+//     eliminated nodes.  The remaining core (about 210 of 400 nodes at m = 400)
+//     is written as a dense d_p x d_p matrix through the plan's slot map
+//     (d_p = core size rounded up to 32, identity padding).
+//  2. Block elimination of the core with 32 x 32 blocks, no chains of
+//     dependent scalar solves:
+//     (a) one warp inverts the diagonal block D in registers by Gauss-Jordan
+//         elimination (its pivots are the LU pivots, so they give log|det|),
+//         while the other warps stage the column panel C and the row panel B
+//         in shared memory;
+//     (b) all warps form the multipliers C D^-1 (a 32-wide GEMM);
+//     (c) the trailing update E -= (C D^-1) B: a register-tiled FMA loop over
 //         (32W) x 128 tiles with 16-byte conflict-free shared and global loads.
-//     The blocked pass does not pivot: (I - Gamma) is diagonally dominant in the
-//     filtering regime.  Every multiplier (sparse levels included) is checked
-//     against kPivotThreshold; a draw with a larger one, or a zero / non-finite
-//     pivot, is flagged and redone by k_lu_fallback with partial pivoting on the
-//     full matrix (getrf semantics).  |det| does not depend on the pivot order.
+//     The pass does not pivot: (I - Gamma) is diagonally dominant in the
+//     filtering regime.  Every multiplier (the levels', the diagonal blocks'
+//     and C D^-1) is checked against kPivotThreshold; a draw with a larger one,
+//     or a zero / non-finite pivot, is flagged and redone by k_lu_fallback with
+//     partial pivoting on the full matrix (getrf semantics).  |det| does not
+//     depend on the elimination order.
 //  3. Forecasts: the right-hand side goes through the levels' forward program,
-//     rides along the core factorisation, is back-substituted through the core
-//     and the levels; an FP64 residual nu - (I - Gamma) y0 from the sparse parent
-//     rows drives one refinement solve with the same factors.
+//     rides along the block elimination (b2 -= C D^-1 b1), and the back solve
+//     x1 = D^-1 (b1 - B x2) runs block by block with the stored D^-1, C D^-1 and
+//     B; then the levels' backward program.  An FP64 residual
+//     nu - (I - Gamma) y0 from the sparse parent rows drives one refinement
+//     solve with the same factors.
 #include <algorithm>
 
 #include "elimination.hpp"
@@ -36,19 +43,26 @@
 namespace sgdlm {
 namespace {
 
-constexpr int kB = 32;          // LU block size
+constexpr int kB = 32;          // block size
 constexpr int kThreads = 256;   // 16 x 16 thread grid of the trailing update
+constexpr int kWarps = kThreads / 32;
 constexpr double kPivotThreshold = 8.0;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kDs = 36;  // row stride of D^-1 in shared memory (16-byte rows, 4-way store conflicts)
+constexpr int kUs = 36;  // stride of the row panel B, stored column by column: B[c][t] at t*kUs + c
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
   return v;
 }
 template <typename T> __device__ __forceinline__ T dabs(T v) { return v < T(0) ? -v : v; }
 template <typename T> __device__ __forceinline__ bool finite_t(T v) {
   return v == v && dabs(v) <= (T)3.0e38;
 }
+// log|v| in the working precision, returned in double for the FP64 sums
+__device__ __forceinline__ double log_abs(float v) { return (double)logf(fabsf(v)); }
+__device__ __forceinline__ double log_abs(double v) { return log(fabs(v)); }
 
 // Deterministic block-wide sum (fixed order); `red` holds 32 doubles.
 __device__ double block_sum_det(double v, double *red) {
@@ -63,11 +77,16 @@ __device__ double block_sum_det(double v, double *red) {
 }
 
 // Shared-memory carve-up (byte offsets, 16-byte aligned).  dp is the padded
-// dense size, m the number of nodes (forecast vectors are node-indexed).
+// dense size, m the number of nodes (forecast vectors are node-indexed).  The
+// panel buffers Lp (C, column-major, 32 x Rmax) / Up (B, Rmax columns of kUs)
+// and the value slots of the sparse levels (nv_smem of them, 0 when they live in
+// global memory) share one region: the slots are dead while the panels are in
+// use.  pcol / prow receive the pivot columns / rows of the Gauss-Jordan steps.
 struct Smem {
   int Rmax;
-  size_t off_D, off_Lp, off_Up, off_z, off_nu, off_res, off_zf, off_yf, off_yd, off_red, total;
-  __host__ __device__ Smem(int dp, int m, size_t tsz) {
+  size_t off_D, off_pcol, off_prow, off_Lp, off_Up, off_vals, off_z, off_nu, off_res, off_zf,
+      off_yf, off_yd, off_red, off_bsum, total;
+  __host__ __device__ Smem(int dp, int m, size_t tsz, int nv_smem) {
     Rmax = dp - kB > 0 ? dp - kB : kB;
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -75,15 +94,43 @@ struct Smem {
       o += (bytes + 15) & ~(size_t)15;
       return at;
     };
-    off_D = take((size_t)kB * (kB + 1) * tsz);
-    off_Lp = take((size_t)kB * Rmax * tsz);
-    off_Up = take((size_t)kB * Rmax * tsz);
+    off_D = take((size_t)kB * kDs * tsz);
+    off_pcol = take((size_t)kB * kB * tsz);
+    off_prow = take((size_t)kB * kB * tsz);
+    const size_t panels = ((size_t)kB * Rmax + (size_t)Rmax * kUs) * tsz;
+    const size_t vals = (((size_t)nv_smem + 3) / 4) * 4 * tsz;
+    off_Lp = take(panels > vals ? panels : vals);
+    off_Up = off_Lp + (size_t)kB * Rmax * tsz;
+    off_vals = off_Lp;
     off_z = take((size_t)dp * tsz);
     off_nu = take((size_t)m * sizeof(double));
     off_res = take((size_t)m * sizeof(double));
     off_zf = take((size_t)m * tsz);
     off_yf = take((size_t)m * tsz);
     off_yd = take((size_t)m * tsz);
+    off_red = take(64 * sizeof(double));
+    off_bsum = take((size_t)kWarps * kB * tsz);
+    total = o;
+  }
+};
+
+// Shared memory of the pivoting redo: the right-hand side and correction, the
+// permutation, one diagonal block and the FP64 forecast vectors.
+struct FallbackSmem {
+  size_t off_D, off_z, off_d, off_perm, off_nu, off_res, off_red, total;
+  __host__ __device__ FallbackSmem(int mp, int m, size_t tsz) {
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      const size_t at = o;
+      o += (bytes + 15) & ~(size_t)15;
+      return at;
+    };
+    off_D = take((size_t)kB * (kB + 1) * tsz);
+    off_z = take((size_t)mp * tsz);
+    off_d = take((size_t)mp * tsz);
+    off_perm = take((size_t)mp * sizeof(int));
+    off_nu = take((size_t)m * sizeof(double));
+    off_res = take((size_t)m * sizeof(double));
     off_red = take(64 * sizeof(double));
     total = o;
   }
@@ -156,12 +203,28 @@ template <> struct Vec<double> {
   }
 };
 
-// Register-tiled trailing update A[r0:, r0:] -= Lp Up over an R x R region.
-// 16 x 16 threads; thread (tr, tc) owns rows {tr*W + a, 16W + tr*W + a} and columns
-// {tc*4 + b, 64 + tc*4 + b} of a (32W) x 128 tile, so every shared-memory read is a
-// 16-byte vector and the 8 threads of each access phase read one contiguous
-// 128-byte line (no bank conflicts); global loads are 16-byte vectors, 16 threads
-// covering 256 contiguous bytes of a column.
+// Two consecutive values (8 or 16 bytes) from shared memory.
+template <typename T> struct Pair;
+template <> struct Pair<float> {
+  __device__ static __forceinline__ void ld(const float *p, float *o) {
+    const float2 v = *reinterpret_cast<const float2 *>(p);
+    o[0] = v.x; o[1] = v.y;
+  }
+};
+template <> struct Pair<double> {
+  __device__ static __forceinline__ void ld(const double *p, double *o) {
+    const double2 v = *reinterpret_cast<const double2 *>(p);
+    o[0] = v.x; o[1] = v.y;
+  }
+};
+
+// Register-tiled trailing update A[r0:, r0:] -= Lp B over an R x R region, B
+// (32 x R) read from Up[t * kUs + c].  16 x 16 threads; thread (tr, tc) owns rows
+// {tr*W + a, 16W + tr*W + a} and columns {tc*4 + b, 64 + tc*4 + b} of a
+// (32W) x 128 tile.  Lp reads are 16-byte vectors, the 8 threads of each access
+// phase reading one contiguous 128-byte line; B is read two k at a time (two
+// distinct addresses per warp).  Global loads are 16-byte
+// vectors, 16 threads covering 256 contiguous bytes of a column.
 template <typename T>
 __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r0, int R,
                                                 const T *__restrict__ Lp,
@@ -201,31 +264,35 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
           for (int a = 0; a < TM; ++a) acc[a][b] = T(0);
         }
       }
-#pragma unroll 2
-      for (int k = 0; k < kB; ++k) {
-        T lv[TM], uv[TN];
-        const T *lrow = Lp + k * Rmax;
-        const T *urow = Up + k * Rmax;
-        V::ld(lrow + ra, lv);
-        if (vb) {
-          V::ld(lrow + rb, lv + W);
-        } else {
+#pragma unroll 1
+      for (int k2 = 0; k2 < kB; k2 += 2) {
+        T u2[TN][2];
 #pragma unroll
-          for (int a = 0; a < W; ++a) lv[W + a] = T(0);
+        for (int b = 0; b < TN; ++b) {
+          const int col = (b < 4) ? (ca + b) : (cb + b - 4);
+          if ((b < 4) || wb) {
+            Pair<T>::ld(Up + col * kUs + k2, u2[b]);
+          } else {
+            u2[b][0] = T(0);
+            u2[b][1] = T(0);
+          }
         }
 #pragma unroll
-        for (int q = 0; q < 4; q += W) V::ld(urow + ca + q, uv + q);
-        if (wb) {
+        for (int kk = 0; kk < 2; ++kk) {
+          T lv[TM];
+          const T *lrow = Lp + (k2 + kk) * Rmax;
+          V::ld(lrow + ra, lv);
+          if (vb) {
+            V::ld(lrow + rb, lv + W);
+          } else {
 #pragma unroll
-          for (int q = 0; q < 4; q += W) V::ld(urow + cb + q, uv + 4 + q);
-        } else {
+            for (int a = 0; a < W; ++a) lv[W + a] = T(0);
+          }
 #pragma unroll
-          for (int q = 0; q < 4; ++q) uv[4 + q] = T(0);
+          for (int a = 0; a < TM; ++a)
+#pragma unroll
+            for (int b = 0; b < TN; ++b) acc[a][b] -= lv[a] * u2[b][kk];
         }
-#pragma unroll
-        for (int a = 0; a < TM; ++a)
-#pragma unroll
-          for (int b = 0; b < TN; ++b) acc[a][b] -= lv[a] * uv[b];
       }
 #pragma unroll
       for (int b = 0; b < TN; ++b) {
@@ -247,6 +314,232 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
   }
 }
 
+// Asynchronous global -> shared copies (cp.async), so that the panel staging
+// overlaps the Gauss-Jordan steps.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// Issues the copies of the column panel C (rows r0.., columns k0..k0+31) into
+// Lp[c * Rmax + t] and of the row panel B (rows k0..k0+31, columns r0..) into
+// Up[t * kUs + c]; both are 16-byte pieces of contiguous global columns.
+template <typename T>
+__device__ __forceinline__ void stage_panels_async(const T *__restrict__ A, int dp, int k0, int r0,
+                                                   int R, T *Lp, T *Up, int Rmax) {
+  constexpr int W = Vec<T>::W;
+  const int RW = R / W, nc = kB * RW;
+  for (int u = threadIdx.x; u < nc; u += blockDim.x) {
+    const int c = u / RW, tw = u - c * RW;
+    cp_async16(Lp + c * Rmax + tw * W, A + (size_t)(r0 + tw * W) + (size_t)dp * (k0 + c));
+  }
+  constexpr int QW = kB / W;
+  for (int u = threadIdx.x; u < R * QW; u += blockDim.x) {
+    const int t = u / QW, q = u - t * QW;
+    cp_async16(Up + t * kUs + q * W, A + (size_t)(k0 + q * W) + (size_t)dp * (r0 + t));
+  }
+}
+
+// Reciprocal on the elimination's critical path.  FP32: the hardware
+// approximation refined by one Newton-Raphson step, r' = r + r (1 - x r) (the
+// classical quadratically convergent reciprocal iteration), accurate to about
+// 1 ulp; FP64: the IEEE quotient.
+__device__ __forceinline__ float rcp_fast(float x) {
+  const float r = __fdividef(1.0f, x);
+  return fmaf(r, fmaf(-x, r, 1.0f), r);
+}
+__device__ __forceinline__ double rcp_fast(double x) { return 1.0 / x; }
+
+// In-register inverse of a 4 x 4 block by Gauss-Jordan elimination without
+// pivoting (m[q][q'] = row q, column q').
+template <typename T>
+__device__ __forceinline__ void invert4(T (&m)[4][4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T rp = rcp_fast(m[k][k]);
+    T rk[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) rk[j] = (j == k) ? rp : m[k][j] * rp;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i == k) continue;
+      const T f = m[i][k];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) m[i][j] = (j == k) ? -f * rp : m[i][j] - f * rk[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) m[k][j] = rk[j];
+  }
+}
+
+// Gauss-Jordan inversion (no pivoting) of the 32 x 32 block D by all eight warps,
+// with 4 x 4 pivot blocks: thread (lane i, warp w) holds a[s] = D[i][w + 8s].
+// Super-step K (pivot rows / columns c0 = 4K .. 4K+3) publishes the pivot
+// columns in pcol[c][*] (from warps 4(K%2) .. +3) and the pivot rows in
+// prowT[c][c0 ..] (from lanes c0 .. c0+3), then every thread inverts the pivot
+// block P itself and updates its four entries:
+//   i, c outside the block:  a -= M[i][K] P^-1 M[K][c]
+//   i in the block:          row (P^-1 M[K][*]) of the scaled pivot rows
+//   c in the block:          -(M[i][K] P^-1), resp. P^-1 itself.
+// Each super-step writes its own pcol / prowT entries, so one barrier per
+// super-step suffices; eight in all.  pcol keeps the pivot columns as published
+// (the Schur complement's columns, for the LU check).  On return
+// a[s] = (D^-1)[i][w + 8s].
+template <typename T>
+__device__ __forceinline__ void gauss_jordan_invert(T (&a)[4], T *pcol, T *prowT) {
+  using V = Vec<T>;
+  const int i = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll 1
+  for (int K = 0; K < kB / 4; ++K) {
+    const int c0 = 4 * K, sK = K >> 1, w0 = (K & 1) * 4;
+    const bool inK = (i >= c0 && i < c0 + 4);
+    if (w >= w0 && w < w0 + 4)
+      pcol[(c0 + w - w0) * kB + i] = sK == 0 ? a[0] : sK == 1 ? a[1] : sK == 2 ? a[2] : a[3];
+    if (inK) {
+#pragma unroll
+      for (int s = 0; s < 4; ++s) prowT[(w + 8 * s) * kB + i] = a[s];
+    }
+    __syncthreads();
+    T Pm[4][4];
+#pragma unroll
+    for (int qc = 0; qc < 4; ++qc) {
+      T col[4];
+#pragma unroll
+      for (int q = 0; q < 4; q += V::W) V::ld(prowT + (c0 + qc) * kB + c0 + q, col + q);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Pm[q][qc] = col[q];
+    }
+    invert4<T>(Pm);
+    // g = f P^-1 with f = M[i][K] (rows outside the block) or the unit vector e_qi
+    const int qi = i - c0;
+    T f[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) f[q] = inK ? (q == qi ? T(1) : T(0)) : pcol[(c0 + q) * kB + i];
+    T g[4];
+#pragma unroll
+    for (int qc = 0; qc < 4; ++qc) {
+      T acc = T(0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc += f[q] * Pm[q][qc];
+      g[qc] = acc;
+    }
+    const T sgn = inK ? T(1) : T(-1);
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      const int c = w + 8 * s;
+      if (s == sK && w >= w0 && w < w0 + 4) {
+        const int qc = w - w0;
+        const T gq = qc == 0 ? g[0] : qc == 1 ? g[1] : qc == 2 ? g[2] : g[3];
+        a[s] = sgn * gq;
+      } else {
+        T r[4];
+#pragma unroll
+        for (int q = 0; q < 4; q += V::W) V::ld(prowT + c * kB + c0 + q, r + q);
+        const T dot = g[0] * r[0] + g[1] * r[1] + g[2] * r[2] + g[3] * r[3];
+        a[s] = (inK ? T(0) : a[s]) + sgn * dot;
+      }
+    }
+  }
+}
+
+// No-pivot check and log|det| share of the block from the published pivot data:
+// thread (row r = lane, super-step K = warp) redoes the 4 x 4 LU of that
+// super-step's pivot block P and flags a zero / non-finite pivot or a scalar LU
+// multiplier above tau (below the diagonal inside P, or M[r][K] U_P^-1 for rows
+// r below the block).  Lane 0 of each warp returns sum log|u_qq| of its block.
+template <typename T>
+__device__ __forceinline__ double pivot_blocks_check(const T *pcol, const T *prowT, T tau,
+                                                     bool &bad) {
+  const int r = threadIdx.x & 31, K = threadIdx.x >> 5, c0 = 4 * K;
+  T U[4][4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int qc = 0; qc < 4; ++qc) U[q][qc] = prowT[(c0 + qc) * kB + c0 + q];
+  T Lq[4][4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (!(finite_t(U[k][k]) && U[k][k] != T(0))) bad = true;
+    const T rp = rcp_fast(U[k][k]);
+#pragma unroll
+    for (int q = k + 1; q < 4; ++q) {
+      const T l = U[q][k] * rp;
+      Lq[q][k] = l;
+#pragma unroll
+      for (int qc = k + 1; qc < 4; ++qc) U[q][qc] -= l * U[k][qc];
+    }
+  }
+  if (r >= c0 && r < c0 + 4) {
+    const int qr = r - c0;
+#pragma unroll
+    for (int q = 1; q < 4; ++q)
+#pragma unroll
+      for (int k = 0; k < q; ++k)
+        if (q == qr && !(dabs(Lq[q][k]) <= tau)) bad = true;
+  } else if (r >= c0 + 4) {
+    T l[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      T x = pcol[(c0 + q) * kB + r];
+#pragma unroll
+      for (int k = 0; k < q; ++k) x -= l[k] * U[k][q];
+      l[q] = x / U[q][q];
+      if (!(dabs(l[q]) <= tau)) bad = true;
+    }
+  }
+  double ld = 0.0;
+  if (r == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ld += log_abs(U[q][q]);
+  }
+  return ld;
+}
+
+// Back solve of the block elimination, in place on v (length dp, shared):
+// for k = last .. 0:  x_k = D_k^-1 (v_k - B_k x_{>k}), with D_k^-1 stored in the
+// diagonal block and B_k (rows of block k, columns beyond it) untouched in A.
+template <typename T>
+__device__ void be_back_solve(const T *__restrict__ A, int dp, T *v, T *bsum) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int kb = dp / kB - 1; kb >= 0; --kb) {
+    const int k0 = kb * kB, r0 = k0 + kB;
+    T acc = T(0);
+    for (int col = r0 + warp; col < dp; col += kWarps)
+      acc += A[(size_t)(k0 + lane) + (size_t)dp * col] * v[col];
+    bsum[warp * kB + lane] = acc;
+    __syncthreads();
+    if (warp == 0) {
+      T w = v[k0 + lane];
+#pragma unroll
+      for (int s = 0; s < kWarps; ++s) w -= bsum[s * kB + lane];
+      T xk = T(0);
+#pragma unroll 8
+      for (int c = 0; c < kB; ++c)
+        xk += A[(size_t)(k0 + lane) + (size_t)dp * (k0 + c)] * __shfl_sync(kFull, w, c);
+      v[k0 + lane] = xk;
+    }
+    __syncthreads();
+  }
+}
+
+// Forward sweep of the block elimination: v_{>k} -= (C_k D_k^-1) v_k, block by block.
+template <typename T>
+__device__ void be_forward(const T *__restrict__ A, int dp, T *v) {
+  for (int kb = 0; kb < dp / kB - 1; ++kb) {
+    const int k0 = kb * kB, r0 = k0 + kB;
+    for (int t = threadIdx.x; t < dp - r0; t += blockDim.x) {
+      T acc = T(0);
+#pragma unroll 8
+      for (int c = 0; c < kB; ++c) acc += A[(size_t)(r0 + t) + (size_t)dp * (k0 + c)] * v[k0 + c];
+      v[r0 + t] -= acc;
+    }
+    __syncthreads();
+  }
+}
+
 // Copies the 32 x 32 diagonal block at k0 of the stored factors into D (warp 0).
 template <typename T>
 __device__ __forceinline__ void load_diag_block(const T *__restrict__ A, int mp, int k0, T *D) {
@@ -255,7 +548,8 @@ __device__ __forceinline__ void load_diag_block(const T *__restrict__ A, int mp,
   __syncwarp();
 }
 
-// Solves U v = v in place (v in shared memory, length mp) with the stored factors.
+// Solves U v = v in place (v in shared memory, length mp) with the triangular
+// factors of the pivoting redo.
 template <typename T>
 __device__ void block_back_solve(const T *__restrict__ A, int mp, T *v, T *D) {
   const int tid = threadIdx.x, lane = tid & 31;
@@ -267,7 +561,7 @@ __device__ void block_back_solve(const T *__restrict__ A, int mp, T *v, T *D) {
       T w = v[k0 + lane];
       for (int c = kB - 1; c >= 0; --c) {
         if (lane == c) w /= D[c * (kB + 1) + c];
-        const T wc = __shfl_sync(0xffffffffu, w, c);
+        const T wc = __shfl_sync(kFull, w, c);
         if (lane < c) w -= D[lane * (kB + 1) + c] * wc;
       }
       v[k0 + lane] = w;
@@ -282,7 +576,7 @@ __device__ void block_back_solve(const T *__restrict__ A, int mp, T *v, T *D) {
   }
 }
 
-// Solves L v = v in place (unit lower, stored factors).
+// Solves L v = v in place (unit lower, triangular factors of the pivoting redo).
 template <typename T>
 __device__ void block_forward_solve(const T *__restrict__ A, int mp, T *v, T *D) {
   const int tid = threadIdx.x, lane = tid & 31;
@@ -293,7 +587,7 @@ __device__ void block_forward_solve(const T *__restrict__ A, int mp, T *v, T *D)
       load_diag_block(A, mp, k0, D);
       T w = v[k0 + lane];
       for (int c = 0; c < kB; ++c) {
-        const T wc = __shfl_sync(0xffffffffu, w, c);
+        const T wc = __shfl_sync(kFull, w, c);
         if (lane > c) w -= D[lane * (kB + 1) + c] * wc;
       }
       v[k0 + lane] = w;
@@ -308,19 +602,28 @@ __device__ void block_forward_solve(const T *__restrict__ A, int mp, T *v, T *D)
   }
 }
 
-// Forward program of the sparse levels on the node-indexed vector z.
+__device__ __forceinline__ int lo16(unsigned w) { return (int)(w & 0xFFFFu); }
+__device__ __forceinline__ int hi16(unsigned w) { return (int)(w >> 16); }
+
+// Forward program of one level on the node-indexed vector z: z[r] -= L[r][t] z[t].
 template <typename T>
-__device__ void levels_forward(const EliminationPlan &ep, const T *__restrict__ vals, T *z) {
-  for (int lev = 0; lev < ep.nlev; ++lev) {
-    for (int g = ep.lev_fwd_nodes[lev] + threadIdx.x; g < ep.lev_fwd_nodes[lev + 1]; g += blockDim.x) {
-      const int r = ep.fwd_node[g];
-      T acc = z[r];
-      for (int q = ep.fwd_ptr[g]; q < ep.fwd_ptr[g + 1]; ++q) {
-        const int3 f = ep.fwd[q];
-        acc -= vals[f.x] / vals[f.z] * z[f.y];
-      }
-      z[r] = acc;
+__device__ __forceinline__ void level_forward(const EliminationPlan &ep, int lev, const T *vals,
+                                              T *z) {
+  for (int g = ep.lev_fwd_nodes[lev] + threadIdx.x; g < ep.lev_fwd_nodes[lev + 1]; g += blockDim.x) {
+    const int r = ep.fwd_node[g];
+    T acc = z[r];
+    for (int q = ep.fwd_ptr[g]; q < ep.fwd_ptr[g + 1]; ++q) {
+      const unsigned f = ep.fwd[q];
+      acc -= vals[lo16(f)] * z[hi16(f)];
     }
+    z[r] = acc;
+  }
+}
+
+template <typename T>
+__device__ void levels_forward(const EliminationPlan &ep, const T *vals, T *z) {
+  for (int lev = 0; lev < ep.nlev; ++lev) {
+    level_forward<T>(ep, lev, vals, z);
     __syncthreads();
   }
 }
@@ -328,15 +631,14 @@ __device__ void levels_forward(const EliminationPlan &ep, const T *__restrict__ 
 // Backward program of the sparse levels: y[t] for eliminated nodes from the
 // forward-eliminated z and the already known y of later nodes.
 template <typename T>
-__device__ void levels_backward(const EliminationPlan &ep, const T *__restrict__ vals,
-                                const T *z, T *y) {
+__device__ void levels_backward(const EliminationPlan &ep, const T *vals, const T *z, T *y) {
   for (int lev = ep.nlev - 1; lev >= 0; --lev) {
     for (int g = ep.lev_bwd_nodes[lev] + threadIdx.x; g < ep.lev_bwd_nodes[lev + 1]; g += blockDim.x) {
       const int t = ep.bwd_node[g];
       T acc = z[t];
       for (int q = ep.bwd_ptr[g]; q < ep.bwd_ptr[g + 1]; ++q) {
-        const int2 b = ep.bwd[q];
-        acc -= vals[b.x] * y[b.y];
+        const unsigned b = ep.bwd[q];
+        acc -= vals[lo16(b)] * y[hi16(b)];
       }
       y[t] = acc / vals[ep.bwd_diag[g]];
     }
@@ -361,16 +663,33 @@ __device__ void residual(int m, int P, long n, long i, GammaRows rows,
   __syncthreads();
 }
 
+// Copies n values between shared and global memory (16-byte vectors; both
+// buffers hold n rounded up to 4 values).
+template <typename T>
+__device__ __forceinline__ void copy_vals(T *__restrict__ dst, const T *__restrict__ src, int n) {
+  using V = Vec<T>;
+  const int nvec = ((n + 3) / 4) * 4 / V::W;
+  for (int q = threadIdx.x; q < nvec; q += blockDim.x) {
+    T t[V::W];
+    V::ld(src + q * V::W, t);
+    V::st(dst + q * V::W, t);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
-    k_lu(int m, int P, int dp, size_t per_cta, long n, EliminationPlan ep,
+    k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, long n, EliminationPlan ep,
          const unsigned *__restrict__ sp, const T *__restrict__ theta, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
          const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
          double *__restrict__ y, GammaRows rows) {
+  using V = Vec<T>;
+  constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Smem L(dp, m, sizeof(T));
-  T *D = reinterpret_cast<T *>(smem_raw + L.off_D);
+  const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0);
+  T *D = reinterpret_cast<T *>(smem_raw + L.off_D);  // D^-1, row-major, stride kB
+  T *pcol = reinterpret_cast<T *>(smem_raw + L.off_pcol);
+  T *prow = reinterpret_cast<T *>(smem_raw + L.off_prow);
   T *Lp = reinterpret_cast<T *>(smem_raw + L.off_Lp);
   T *Up = reinterpret_cast<T *>(smem_raw + L.off_Up);
   T *z = reinterpret_cast<T *>(smem_raw + L.off_z);
@@ -380,10 +699,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   T *yf = reinterpret_cast<T *>(smem_raw + L.off_yf);
   T *yd = reinterpret_cast<T *>(smem_raw + L.off_yd);
   double *red = reinterpret_cast<double *>(smem_raw + L.off_red);
+  T *bsum = reinterpret_cast<T *>(smem_raw + L.off_bsum);
   const int Rmax = L.Rmax;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T *A = scratch + (size_t)blockIdx.x * per_cta;
-  T *vals = A + (size_t)dp * dp;
+  T *vals_g = A + (size_t)dp * dp;
+  const bool planned = (ep.core_map != nullptr);
+  T *vals = vals_smem ? reinterpret_cast<T *>(smem_raw + L.off_vals) : vals_g;
   const int nbk = dp / kB;
   const bool solve = (x != nullptr);
   const T tau = (T)kPivotThreshold;
@@ -392,176 +714,198 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
     if (tid == 0) sflag = 0;
     bool bad = false;
-    double ld_part = 0.0;  // this thread's share of sum log|pivot| of the levels
-    // ---- build: zero the core, level-0 values, forecast right-hand side
-    const bool planned = (ep.core_ent != nullptr);
+    double ld_part = 0.0;  // this thread's share of sum log|pivot| (levels and core)
+    // ---- build: value slots of level 0, forecast right-hand side
     if (planned) {
-      const size_t n16 = (size_t)dp * dp * sizeof(T) / 16;
-      uint4 *A16 = reinterpret_cast<uint4 *>(A);
-      for (size_t e = tid; e < n16; e += blockDim.x) A16[e] = make_uint4(0, 0, 0, 0);
-      for (int r = tid; r < m; r += blockDim.x) vals[r] = T(1);
-      for (int k = tid; k < ep.nnz0; k += blockDim.x) {
-        const int e = ep.l0_e[k];
-        const int j = e / P, kk = e % P;
-        vals[m + k] = -theta[((size_t)j * n + i) * P + kk];
+      for (int s = tid; s < (int)kSlotDiag0 + m; s += blockDim.x) vals[s] = (s == 0) ? T(0) : T(1);
+      for (int k0 = tid; k0 < ep.nnz0; k0 += 4 * kThreads) {
+        int e[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) e[h] = (k0 + h * kThreads < ep.nnz0) ? ep.l0_e[k0 + h * kThreads] : -1;
+        T th[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          th[h] = T(0);
+          if (e[h] >= 0) th[h] = theta[((size_t)(e[h] / P) * n + i) * P + e[h] % P];
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+          if (e[h] >= 0) vals[kSlotDiag0 + m + k0 + h * kThreads] = -th[h];
       }
     } else {
       // no plan: the whole matrix is the core, scattered from the parental sets
       build_full<T>(m, P, dp, n, i, sp, theta, A);
     }
-    if (solve) forecast_rhs<T>(m, P, n, i, sp, theta, x, lambda, key, nu);
-    __syncthreads();
     if (solve) {
+      forecast_rhs<T>(m, P, n, i, sp, theta, x, lambda, key, nu);
       for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)nu[r];
     }
+    __syncthreads();
     // ---- sparse levels
     for (int lev = 0; lev < ep.nlev; ++lev) {
-      for (int q = ep.lev_entry[lev] + tid; q < ep.lev_entry[lev + 1]; q += blockDim.x) {
-        const int base = ep.ent_base[q];
-        T v = base >= 0 ? vals[base] : T(0);
-        for (int t = ep.ent_tptr[q]; t < ep.ent_tptr[q + 1]; ++t) {
-          const int3 tm = ep.terms[t];
-          const T l = vals[tm.x] / vals[tm.z];
-          if (!(dabs(l) <= tau)) bad = true;
-          v -= l * vals[tm.y];
-        }
-        vals[ep.ent_out[q]] = v;
-      }
       for (int q = ep.lev_piv[lev] + tid; q < ep.lev_piv[lev + 1]; q += blockDim.x) {
         const T pv = vals[ep.piv[q]];
         if (!(finite_t(pv) && pv != T(0))) bad = true;
-        ld_part += log(fabs((double)pv));
+        ld_part += log_abs(pv);
       }
-      if (solve) {
-        __syncthreads();
-        for (int g = ep.lev_fwd_nodes[lev] + tid; g < ep.lev_fwd_nodes[lev + 1]; g += blockDim.x) {
-          const int r = ep.fwd_node[g];
-          T acc = zf[r];
-          for (int q = ep.fwd_ptr[g]; q < ep.fwd_ptr[g + 1]; ++q) {
-            const int3 f = ep.fwd[q];
-            acc -= vals[f.x] / vals[f.z] * zf[f.y];
-          }
-          zf[r] = acc;
-        }
+      for (int q = ep.lev_scale[lev] + tid; q < ep.lev_scale[lev + 1]; q += blockDim.x) {
+        const unsigned w = ep.scale[q];
+        const T l = vals[lo16(w)] / vals[hi16(w)];
+        if (!(dabs(l) <= tau)) bad = true;
+        vals[lo16(w)] = l;
       }
       __syncthreads();
-    }
-    // ---- dense core: scatter, identity padding, core right-hand side
-    if (planned) {
-      for (int q = tid; q < ep.n_core_ent; q += blockDim.x) {
-        const int3 ce = ep.core_ent[q];
-        A[ce.y + (size_t)dp * ce.z] = vals[ce.x];
+      // new entries: each warp runs four chunks at a time (independent loads in flight)
+      const int c_end = ep.lev_chunk[lev + 1];
+      for (int c = ep.lev_chunk[lev] + warp; c < c_end; c += 4 * kWarps) {
+        unsigned e[4];
+        const unsigned *tp[4];
+        int K[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int ch = c + h * kWarps;
+          e[h] = kSlotNone;  // no store, base = constant 0
+          K[h] = 0;
+          tp[h] = ep.terms;
+          if (ch < c_end) {
+            e[h] = ep.ent[(size_t)ch * 32 + lane];
+            const int t0 = ep.chunk_tofs[ch];
+            K[h] = (ep.chunk_tofs[ch + 1] - t0) >> 5;
+            tp[h] = ep.terms + t0 + lane;
+          }
+        }
+        T v[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) v[h] = vals[hi16(e[h])];
+        const int Kmax = max(max(K[0], K[1]), max(K[2], K[3]));
+#pragma unroll 2
+        for (int k = 0; k < Kmax; ++k) {
+          unsigned w[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) w[h] = (k < K[h]) ? tp[h][32 * k] : 0u;
+#pragma unroll
+          for (int h = 0; h < 4; ++h) v[h] -= vals[lo16(w[h])] * vals[hi16(w[h])];
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+          if ((unsigned)lo16(e[h]) != kSlotNone) vals[lo16(e[h])] = v[h];
       }
-      for (int r = ep.core_n + tid; r < dp; r += blockDim.x) A[(size_t)r * dp + r] = T(1);
+      if (solve) level_forward<T>(ep, lev, vals, zf);
+      __syncthreads();
+    }
+    // ---- dense core through the slot map; core right-hand side
+    if (planned) {
+      const uint2 *map4 = reinterpret_cast<const uint2 *>(ep.core_map);
+      const int nq = dp * dp / 4;
+      for (int q0 = tid; q0 < nq; q0 += 4 * kThreads) {
+        uint2 w[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int q = q0 + h * kThreads;
+          w[h] = q < nq ? map4[q] : make_uint2(0u, 0u);
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int q = q0 + h * kThreads;
+          if (q < nq) {
+            T v4[4] = {vals[lo16(w[h].x)], vals[hi16(w[h].x)], vals[lo16(w[h].y)], vals[hi16(w[h].y)]};
+#pragma unroll
+            for (int g = 0; g < 4; g += W) V::st(A + (size_t)q * 4 + g, v4 + g);
+          }
+        }
+      }
+      if (solve && vals_smem) copy_vals<T>(vals_g, vals, ep.nv);  // the solves need them later
     }
     if (solve)
       for (int r = tid; r < dp; r += blockDim.x)
         z[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
     __syncthreads();
-    double ld = 0.0;  // warp 0's running sum of log|u_kk|
     for (int kb = 0; kb < nbk; ++kb) {
       const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
-      // (a) diagonal block, warp 0, row per lane
-      if (warp == 0) {
-        for (int c = 0; c < kB; ++c)
-          D[lane * (kB + 1) + c] = A[(size_t)(k0 + lane) + (size_t)dp * (k0 + c)];
-        __syncwarp();
-        for (int k = 0; k < kB; ++k) {
-          const T piv = D[k * (kB + 1) + k];
-          if (lane > k) {
-            const T l = D[lane * (kB + 1) + k] / piv;
-            D[lane * (kB + 1) + k] = l;
-            if (!(dabs(l) <= tau)) bad = true;
-            for (int c = k + 1; c < kB; ++c) D[lane * (kB + 1) + c] -= l * D[k * (kB + 1) + c];
-          }
-          __syncwarp();
-        }
-        const T u = D[lane * (kB + 1) + lane];
-        if (!(finite_t(u) && u != T(0))) bad = true;
-        ld += warp_sum_d(log(fabs((double)u)));
+      // (a) panels C and B in flight while all warps invert D by Gauss-Jordan
+      if (R > 0) stage_panels_async<T>(A, dp, k0, r0, R, Lp, Up, Rmax);
+      {
+        T a[4];
+        const T *dcol = A + (size_t)(k0 + lane) + (size_t)dp * k0;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) a[s] = dcol[(size_t)dp * (warp + 8 * s)];
+        gauss_jordan_invert<T>(a, pcol, prow);
+        ld_part += pivot_blocks_check<T>(pcol, prow, tau, bad);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) D[lane * kDs + warp + 8 * s] = a[s];
         if (solve) {
-          for (int c = 0; c < kB; ++c)
-            A[(size_t)(k0 + lane) + (size_t)dp * (k0 + c)] = D[lane * (kB + 1) + c];
-          // right-hand side block: z_k <- L_kk^-1 z_k (unit lower, from shared D)
-          T w = z[k0 + lane];
-          for (int c = 0; c < kB; ++c) {
-            const T wc = __shfl_sync(0xffffffffu, w, c);
-            if (lane > c) w -= D[lane * (kB + 1) + c] * wc;
-          }
-          z[k0 + lane] = w;
+          T *dc = A + (size_t)(k0 + lane) + (size_t)dp * k0;
+#pragma unroll
+          for (int s = 0; s < 4; ++s) dc[(size_t)dp * (warp + 8 * s)] = a[s];
         }
       }
+      cp_async_wait_all();
       __syncthreads();
-      // (b) column panel rows r0.. -> Lp and (c) row panel columns r0.. -> Up, solved
-      // in place in shared memory (thread t owns column t of Lp or Up); the factors
-      // go back to global memory only when a solve needs them later.
-      for (int t = tid; t < 2 * R; t += blockDim.x) {
-        if (t < R) {
-          const int row = r0 + t;
-          T *lp = Lp + t;
-#pragma unroll 8
-          for (int c = 0; c < kB; ++c) lp[c * Rmax] = A[(size_t)row + (size_t)dp * (k0 + c)];
-          for (int c = 0; c < kB; ++c) {
-            T acc = lp[c * Rmax];
-#pragma unroll 4
-            for (int cp = 0; cp < c; ++cp) acc -= lp[cp * Rmax] * D[cp * (kB + 1) + c];
-            acc = acc / D[c * (kB + 1) + c];
-            lp[c * Rmax] = acc;
-            if (!(dabs(acc) <= tau)) bad = true;
-            if (solve) A[(size_t)row + (size_t)dp * (k0 + c)] = acc;
-          }
-        } else {
-          const int tt = t - R;
-          const int col = r0 + tt;
-          T *colp = A + (size_t)dp * col + k0;
-          T *up = Up + tt;
-#pragma unroll
-          for (int r = 0; r < kB; r += Vec<T>::W) {
-            T v[Vec<T>::W];
-            Vec<T>::ld(colp + r, v);
-#pragma unroll
-            for (int q = 0; q < Vec<T>::W; ++q) up[(r + q) * Rmax] = v[q];
-          }
-          for (int r = 1; r < kB; ++r) {
-            T acc = up[r * Rmax];
-#pragma unroll 4
-            for (int rp = 0; rp < r; ++rp) acc -= D[r * (kB + 1) + rp] * up[rp * Rmax];
-            up[r * Rmax] = acc;
-          }
-          if (solve) {
-#pragma unroll
-            for (int r = 0; r < kB; r += Vec<T>::W) {
-              T v[Vec<T>::W];
-#pragma unroll
-              for (int q = 0; q < Vec<T>::W; ++q) v[q] = up[(r + q) * Rmax];
-              Vec<T>::st(colp + r, v);
-            }
-          }
-        }
-      }
-      __syncthreads();
-      // (d) trailing update, plus the right-hand side below the block
       if (R > 0) {
+        // (b) Lp <- C D^-1 in place: warp (half, quarter) owns 32 rows x 8 columns
+        // of each 64-row round; a round reads its rows completely before writing.
+        const int qc = (warp >> 1) * 8;
+        for (int t0 = 0; t0 < R; t0 += 64) {
+          const int t = t0 + (warp & 1) * 32 + lane;
+          const bool act = t < R;
+          T o[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) o[j] = T(0);
+          if (act) {
+#pragma unroll 8
+            for (int c = 0; c < kB; ++c) {
+              const T lv = Lp[c * Rmax + t];
+              T dv[8];
+#pragma unroll
+              for (int j = 0; j < 8; j += W) V::ld(D + c * kDs + qc + j, dv + j);
+#pragma unroll
+              for (int j = 0; j < 8; ++j) o[j] += lv * dv[j];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              if (!(dabs(o[j]) <= tau)) bad = true;
+          }
+          __syncthreads();
+          if (act) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) Lp[(qc + j) * Rmax + t] = o[j];
+          }
+        }
+        __syncthreads();
         if (solve) {
+          // keep C D^-1 for the solves; the right-hand side rides along
+          const int RW = R / W;
+          for (int u = tid; u < kB * RW; u += blockDim.x) {
+            const int c = u / RW, tw = u - c * RW;
+            T v[W];
+            V::ld(Lp + c * Rmax + tw * W, v);
+            V::st(A + (size_t)(r0 + tw * W) + (size_t)dp * (k0 + c), v);
+          }
           for (int t = tid; t < R; t += blockDim.x) {
             T acc = T(0);
-            for (int k = 0; k < kB; ++k) acc += Lp[k * Rmax + t] * z[k0 + k];
+#pragma unroll 8
+            for (int c = 0; c < kB; ++c) acc += Lp[c * Rmax + t] * z[k0 + c];
             z[r0 + t] -= acc;
           }
         }
+        // (c) trailing update E -= (C D^-1) B
         trailing_update<T>(A, dp, r0, R, Lp, Up, Rmax);
       }
       __syncthreads();
     }
     if (bad) atomicOr(&sflag, 1);
-    const double ld_levels = block_sum_det(ld_part, red);  // contains __syncthreads
+    const double ld_total = block_sum_det(ld_part, red);  // contains __syncthreads
     const bool flagged = (sflag != 0);
     if (tid == 0) {
-      logdet[i] = ld + ld_levels;
+      logdet[i] = ld_total;
       if (flagged) atomicOr(&draw_flags[i], DRAW_FLAG_PIVOT);
     }
     if (solve && !flagged) {
-      block_back_solve<T>(A, dp, z, D);  // core part of y0
+      if (planned && vals_smem) {
+        copy_vals<T>(vals, vals_g, ep.nv);
+        __syncthreads();
+      }
+      be_back_solve<T>(A, dp, z, bsum);  // core part of y0
       for (int r = tid; r < ep.core_n; r += blockDim.x) yf[planned ? ep.core_node[r] : r] = z[r];
       __syncthreads();
       levels_backward<T>(ep, vals, zf, yf);
@@ -570,13 +914,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)res[r];
         __syncthreads();
         levels_forward<T>(ep, vals, zf);
-        T *d = Up;  // the row-panel buffer (32 x Rmax >= d_p) holds the core correction
         for (int r = tid; r < dp; r += blockDim.x)
-          d[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
+          z[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
         __syncthreads();
-        block_forward_solve<T>(A, dp, d, D);
-        block_back_solve<T>(A, dp, d, D);
-        for (int r = tid; r < ep.core_n; r += blockDim.x) yd[planned ? ep.core_node[r] : r] = d[r];
+        be_forward<T>(A, dp, z);
+        be_back_solve<T>(A, dp, z, bsum);
+        for (int r = tid; r < ep.core_n; r += blockDim.x) yd[planned ? ep.core_node[r] : r] = z[r];
         __syncthreads();
         levels_backward<T>(ep, vals, zf, yd);
         for (int r = tid; r < m; r += blockDim.x)
@@ -600,13 +943,13 @@ __global__ void __launch_bounds__(kThreads)
                   const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
                   double *__restrict__ y, GammaRows rows) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Smem L(mp, m, sizeof(T));
+  const FallbackSmem L(mp, m, sizeof(T));
   T *z = reinterpret_cast<T *>(smem_raw + L.off_z);
   double *nu = reinterpret_cast<double *>(smem_raw + L.off_nu);
   double *res = reinterpret_cast<double *>(smem_raw + L.off_res);
   double *red = reinterpret_cast<double *>(smem_raw + L.off_red);  // 64 doubles
-  int *perm = reinterpret_cast<int *>(smem_raw + L.off_Lp);        // mp ints
-  T *d = reinterpret_cast<T *>(smem_raw + L.off_Up);               // mp values
+  int *perm = reinterpret_cast<int *>(smem_raw + L.off_perm);
+  T *d = reinterpret_cast<T *>(smem_raw + L.off_d);
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = blockDim.x >> 5;
@@ -639,8 +982,8 @@ __global__ void __launch_bounds__(kThreads)
         }
       }
       for (int o = 16; o > 0; o >>= 1) {
-        const double ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+        const double ov = __shfl_xor_sync(kFull, best, o);
+        const int oi = __shfl_xor_sync(kFull, bidx, o);
         if (ov > best || (ov == best && oi < bidx)) {
           best = ov;
           bidx = oi;
@@ -724,6 +1067,13 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Shared memory a CTA may use when `per_sm` CTAs share one SM (228 KB per SM,
+// 1 KB of it reserved per CTA; 227 KB at most per CTA).
+size_t smem_budget(int per_sm) {
+  const size_t b = 233472u / (size_t)per_sm - 1024u;
+  return b < 232448u ? b : 232448u;
+}
+
 }  // namespace
 
 template <typename T>
@@ -735,11 +1085,13 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv) {
   pl.dp = ((core_n + kB - 1) / kB) * kB;
   if (pl.dp < kB) pl.dp = kB;
   pl.block = kThreads;
-  pl.smem = Smem(pl.dp, m, sizeof(T)).total;
-  pl.smem_fallback = Smem(pl.mp, m, sizeof(T)).total;
-  int ctas_per_sm = (int)((227u * 1024u) / (pl.smem + 1024));
-  if (ctas_per_sm < 1) ctas_per_sm = 1;
-  if (ctas_per_sm > 2) ctas_per_sm = 2;
+  // value slots in shared memory when that keeps the target occupancy
+  const int target = sizeof(T) == 4 ? 2 : 1;
+  const size_t with_vals = Smem(pl.dp, m, sizeof(T), nv).total;
+  pl.vals_smem = (nv > 0 && with_vals <= smem_budget(target)) ? 1 : 0;
+  pl.smem = Smem(pl.dp, m, sizeof(T), pl.vals_smem ? nv : 0).total;
+  pl.smem_fallback = FallbackSmem(pl.mp, m, sizeof(T)).total;
+  int ctas_per_sm = pl.smem <= smem_budget(2) ? 2 : 1;
   if (sizeof(T) == 8) ctas_per_sm = 1;
   long grid = (long)num_sms * ctas_per_sm;
   if (grid > n) grid = n;
@@ -770,9 +1122,9 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
   // as a launch error that the engine reports)
   if (pl.smem > 48 * 1024)
     cudaFuncSetAttribute(k_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
-  k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta, n, ep,
-                                             sp, theta, scratch, logdet, draw_flags, x, lambda,
-                                             key, refine, y, rows);
+  k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
+                                             pl.vals_smem, n, ep, sp, theta, scratch, logdet,
+                                             draw_flags, x, lambda, key, refine, y, rows);
 }
 
 template <typename T>
