@@ -114,10 +114,14 @@ struct Smem {
   }
 };
 
-// Shared memory of the pivoting redo: the right-hand side and correction, the
-// permutation, one diagonal block and the FP64 forecast vectors.
+// Shared memory of the pivoting redo: the 32-column panel (column-major, stride
+// mp), one 128-column chunk of the row panel U12, the right-hand side and
+// correction, the row permutation, one diagonal block and the FP64 forecast
+// vectors.
+constexpr int kFbChunk = 128;
 struct FallbackSmem {
-  size_t off_D, off_z, off_d, off_perm, off_nu, off_res, off_red, total;
+  size_t off_pan, off_U, off_piv, off_pivabs, off_cand, off_D, off_z, off_d, off_perm, off_nu,
+      off_res, off_red, total;
   __host__ __device__ FallbackSmem(int mp, int m, size_t tsz) {
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -125,6 +129,11 @@ struct FallbackSmem {
       o += (bytes + 15) & ~(size_t)15;
       return at;
     };
+    off_pan = take((size_t)kB * mp * tsz);
+    off_U = take((size_t)kFbChunk * kUs * tsz);
+    off_piv = take((size_t)kB * sizeof(int));
+    off_pivabs = take((size_t)mp * tsz);
+    off_cand = take((size_t)2 * kWarps * (tsz > 4 ? tsz : 4));
     off_D = take((size_t)kB * (kB + 1) * tsz);
     off_z = take((size_t)mp * tsz);
     off_d = take((size_t)mp * tsz);
@@ -218,8 +227,9 @@ template <> struct Pair<double> {
   }
 };
 
-// Register-tiled trailing update A[r0:, r0:] -= Lp B over an R x R region, B
-// (32 x R) read from Up[t * kUs + c].  16 x 16 threads; thread (tr, tc) owns rows
+// Register-tiled trailing update A[r0:, r0:] -= Lp B over the rows r0 .. r0+R and
+// the C columns r0+c_off .. (a chunk of the R x R trailing matrix), B (32 x C)
+// read from Up[t * kUs + c] with t relative to the chunk.  16 x 16 threads; thread (tr, tc) owns rows
 // {tr*W + a, 16W + tr*W + a} and columns {tc*4 + b, 64 + tc*4 + b} of a
 // (32W) x 128 tile.  Lp reads are 16-byte vectors, the 8 threads of each access
 // phase reading one contiguous 128-byte line; B is read two k at a time (two
@@ -227,7 +237,7 @@ template <> struct Pair<double> {
 // vectors, 16 threads covering 256 contiguous bytes of a column.
 template <typename T>
 __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r0, int R,
-                                                const T *__restrict__ Lp,
+                                                int c_off, int C, const T *__restrict__ Lp,
                                                 const T *__restrict__ Up, int Rmax) {
   using V = Vec<T>;
   constexpr int W = V::W;
@@ -235,11 +245,11 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
   constexpr int tileM = 32 * W, tileN = 128;
   const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
   for (int tile_r = 0; tile_r < R; tile_r += tileM) {
-    for (int tile_c = 0; tile_c < R; tile_c += tileN) {
+    for (int tile_c = 0; tile_c < C; tile_c += tileN) {
       const int ra = tile_r + tr * W, rb = ra + 16 * W;
       const int ca = tile_c + tc * 4, cb = ca + 64;
-      if (ra >= R || ca >= R) continue;  // chunk b lies beyond chunk a
-      const bool vb = rb < R, wb = cb < R;
+      if (ra >= R || ca >= C) continue;  // chunk b lies beyond chunk a
+      const bool vb = rb < R, wb = cb < C;
       T acc[TM][TN];
 #pragma unroll
       for (int b = 0; b < TN; ++b) {
@@ -247,7 +257,7 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
         const bool cv = (b < 4) || wb;
         T tmp[W];
         if (cv) {
-          const T *colp = A + (size_t)mp * (r0 + col) + r0;
+          const T *colp = A + (size_t)mp * (r0 + c_off + col) + r0;
           V::ld(colp + ra, tmp);
 #pragma unroll
           for (int a = 0; a < W; ++a) acc[a][b] = tmp[a];
@@ -299,7 +309,7 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
         const bool cv = (b < 4) || wb;
         if (!cv) continue;
         const int col = (b < 4) ? (ca + b) : (cb + b - 4);
-        T *colp = A + (size_t)mp * (r0 + col) + r0;
+        T *colp = A + (size_t)mp * (r0 + c_off + col) + r0;
         T tmp[W];
 #pragma unroll
         for (int a = 0; a < W; ++a) tmp[a] = acc[a][b];
@@ -889,7 +899,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
           }
         }
         // (c) trailing update E -= (C D^-1) B
-        trailing_update<T>(A, dp, r0, R, Lp, Up, Rmax);
+        trailing_update<T>(A, dp, r0, R, 0, R, Lp, Up, Rmax);
       }
       __syncthreads();
     }
@@ -933,8 +943,16 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
 }
 
 // Partial-pivoting LU of the full matrix for the draws the fast pass flagged
-// (getrf semantics).  Unblocked; it runs only on draws whose (I - Gamma) is not
-// diagonally dominant enough for the no-pivot pass.
+// (getrf semantics: at each column the row with the largest |entry| becomes the
+// pivot row).  Blocked right-looking LU with 32-column panels:
+//  (a) the panel (rows k0.., columns k0..k0+31) is factored with partial pivoting
+//      in shared memory, three barriers per column (pivot search, row swap,
+//      elimination);
+//  (b) the panel's row swaps are applied to the other columns and the right-hand
+//      side, and the factors are written back;
+//  (c) U12 = L11^-1 A12 by forward substitution, one column per thread, in
+//      128-column chunks, each followed by the register-tiled trailing update
+//      A22 -= L21 U12 of those columns.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_lu_fallback(int m, int P, int mp, long n, const unsigned *__restrict__ sp,
@@ -942,8 +960,16 @@ __global__ void __launch_bounds__(kThreads)
                   double *__restrict__ logdet, int *__restrict__ draw_flags,
                   const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
                   double *__restrict__ y, GammaRows rows) {
+  using V = Vec<T>;
+  constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const FallbackSmem L(mp, m, sizeof(T));
+  T *pan = reinterpret_cast<T *>(smem_raw + L.off_pan);            // pan[c * mp + r]
+  T *Uc = reinterpret_cast<T *>(smem_raw + L.off_U);               // U12 chunk [t][kUs]
+  int *piv = reinterpret_cast<int *>(smem_raw + L.off_piv);        // block's pivot rows
+  T *pivabs = reinterpret_cast<T *>(smem_raw + L.off_pivabs);      // |u_jj|, all columns
+  T *cand_v = reinterpret_cast<T *>(smem_raw + L.off_cand);        // per-warp pivot candidates
+  int *cand_i = reinterpret_cast<int *>(cand_v + kWarps);
   T *z = reinterpret_cast<T *>(smem_raw + L.off_z);
   double *nu = reinterpret_cast<double *>(smem_raw + L.off_nu);
   double *res = reinterpret_cast<double *>(smem_raw + L.off_res);
@@ -955,7 +981,6 @@ __global__ void __launch_bounds__(kThreads)
   const int nwarps = blockDim.x >> 5;
   T *A = scratch + (size_t)blockIdx.x * mp * mp;
   const bool solve = (x != nullptr);
-  __shared__ int s_piv;
   __shared__ bool s_singular;
 
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
@@ -969,76 +994,136 @@ __global__ void __launch_bounds__(kThreads)
     for (int r = tid; r < mp; r += blockDim.x) perm[r] = r;
     if (tid == 0) s_singular = false;
     __syncthreads();
-    double ld = 0.0;
-    for (int k = 0; k < mp; ++k) {
-      // pivot search over rows k.. of column k
-      double best = -1.0;
-      int bidx = k;
-      for (int r = k + tid; r < mp; r += blockDim.x) {
-        const double v = fabs((double)A[(size_t)r + (size_t)mp * k]);
-        if (v > best) {
-          best = v;
-          bidx = r;
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const double ov = __shfl_xor_sync(kFull, best, o);
-        const int oi = __shfl_xor_sync(kFull, bidx, o);
-        if (ov > best || (ov == best && oi < bidx)) {
-          best = ov;
-          bidx = oi;
-        }
-      }
-      if (lane == 0) {
-        red[warp] = best;
-        red[32 + warp] = (double)bidx;
+    for (int k0 = 0; k0 < mp && !s_singular; k0 += kB) {
+      const int Rp = mp - k0, r0 = k0 + kB, R = mp - r0;
+      // (a) panel -> shared memory, factored with partial pivoting
+      for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
+        const int c = u / (Rp / W), rw = u - c * (Rp / W);
+        T v[W];
+        V::ld(A + (size_t)(k0 + rw * W) + (size_t)mp * (k0 + c), v);
+        V::st(pan + c * mp + rw * W, v);
       }
       __syncthreads();
-      if (tid == 0) {
-        double b = red[0];
-        int bi = (int)red[32];
-        for (int w = 1; w < nwarps; ++w) {
-          if (red[w] > b || (red[w] == b && (int)red[32 + w] < bi)) {
-            b = red[w];
-            bi = (int)red[32 + w];
+      for (int j = 0; j < kB; ++j) {
+        // pivot search in the working precision (ties -> lowest row)
+        T best = T(-1);
+        int bidx = j;
+        for (int r = j + tid; r < Rp; r += blockDim.x) {
+          const T v = dabs(pan[j * mp + r]);
+          if (v > best) {
+            best = v;
+            bidx = r;
           }
         }
-        s_piv = bi;
-        if (!(b > 0.0) || !(b <= 3.0e38)) s_singular = true;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const T ov = __shfl_xor_sync(kFull, best, o);
+          const int oi = __shfl_xor_sync(kFull, bidx, o);
+          if (ov > best || (ov == best && oi < bidx)) {
+            best = ov;
+            bidx = oi;
+          }
+        }
+        if (lane == 0) {
+          cand_v[warp] = best;
+          cand_i[warp] = bidx;
+        }
+        __syncthreads();
+        T b = cand_v[0];
+        int p = cand_i[0];
+        for (int w = 1; w < nwarps; ++w)
+          if (cand_v[w] > b || (cand_v[w] == b && cand_i[w] < p)) {
+            b = cand_v[w];
+            p = cand_i[w];
+          }
+        if (!(b > T(0)) || !(b <= (T)3.0e38)) {
+          if (tid == 0) s_singular = true;
+          break;  // uniform: every thread computed the same b
+        }
+        if (p != j && tid < kB) {
+          const T t0 = pan[tid * mp + j];
+          pan[tid * mp + j] = pan[tid * mp + p];
+          pan[tid * mp + p] = t0;
+        }
+        if (tid == 0) piv[j] = p;
+        __syncthreads();
+        const T pv = pan[j * mp + j];
+        if (tid == 0) pivabs[k0 + j] = dabs(pv);
+        for (int r = j + 1 + tid; r < Rp; r += blockDim.x) {
+          const T l = pan[j * mp + r] / pv;
+          pan[j * mp + r] = l;
+          for (int c = j + 1; c < kB; ++c) pan[c * mp + r] -= l * pan[c * mp + j];
+        }
+        __syncthreads();
       }
       __syncthreads();
       if (s_singular) break;
-      const int pr = s_piv;
-      if (pr != k) {
-        for (int c = tid; c < mp; c += blockDim.x) {
-          const T t0 = A[(size_t)k + (size_t)mp * c];
-          A[(size_t)k + (size_t)mp * c] = A[(size_t)pr + (size_t)mp * c];
-          A[(size_t)pr + (size_t)mp * c] = t0;
+      // (b) factors back to global; the block's swaps on the other columns,
+      // the permutation and the right-hand side
+      for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
+        const int c = u / (Rp / W), rw = u - c * (Rp / W);
+        T v[W];
+        V::ld(pan + c * mp + rw * W, v);
+        V::st(A + (size_t)(k0 + rw * W) + (size_t)mp * (k0 + c), v);
+      }
+      for (int c = tid; c < mp - kB; c += blockDim.x) {
+        const int col = c < k0 ? c : c + kB;
+        T *cp = A + (size_t)mp * col;
+        for (int j = 0; j < kB; ++j) {
+          const int p = piv[j];
+          if (p != j) {
+            const T t0 = cp[k0 + j];
+            cp[k0 + j] = cp[k0 + p];
+            cp[k0 + p] = t0;
+          }
         }
-        if (tid == 0) {
-          const int tp = perm[k];
-          perm[k] = perm[pr];
-          perm[pr] = tp;
-          const T tz = z[k];
-          z[k] = z[pr];
-          z[pr] = tz;
+      }
+      if (tid == 0) {
+        for (int j = 0; j < kB; ++j) {
+          const int p = piv[j];
+          if (p != j) {
+            const int tp = perm[k0 + j];
+            perm[k0 + j] = perm[k0 + p];
+            perm[k0 + p] = tp;
+            if (solve) {
+              const T tz = z[k0 + j];
+              z[k0 + j] = z[k0 + p];
+              z[k0 + p] = tz;
+            }
+          }
         }
       }
       __syncthreads();
-      const T piv = A[(size_t)k + (size_t)mp * k];
-      ld += log(fabs((double)piv));
-      for (int r = k + 1 + tid; r < mp; r += blockDim.x) A[(size_t)r + (size_t)mp * k] /= piv;
-      __syncthreads();
-      const int rem = mp - k - 1;
-      for (long e = tid; e < (long)rem * rem; e += blockDim.x) {
-        const int r = k + 1 + (int)(e % rem), c = k + 1 + (int)(e / rem);
-        A[(size_t)r + (size_t)mp * c] -= A[(size_t)r + (size_t)mp * k] * A[(size_t)k + (size_t)mp * c];
+      // (c) U12 chunk by chunk, each followed by its trailing update
+      for (int c_off = 0; c_off < R; c_off += kFbChunk) {
+        const int C = min(kFbChunk, R - c_off);
+        for (int t = tid; t < C; t += blockDim.x) {
+          T *cp = A + (size_t)k0 + (size_t)mp * (r0 + c_off + t);
+          T xv[kB];
+#pragma unroll
+          for (int q = 0; q < kB; q += W) V::ld(cp + q, xv + q);
+#pragma unroll
+          for (int q = 1; q < kB; ++q) {
+            T acc = xv[q];
+#pragma unroll
+            for (int qq = 0; qq < q; ++qq) acc -= pan[qq * mp + q] * xv[qq];
+            xv[q] = acc;
+          }
+#pragma unroll
+          for (int q = 0; q < kB; q += W) {
+            V::st(cp + q, xv + q);
+            V::st(Uc + t * kUs + q, xv + q);
+          }
+        }
+        __syncthreads();
+        if (R > 0) trailing_update<T>(A, mp, r0, R, c_off, C, pan + kB, Uc, mp);
+        __syncthreads();
       }
-      if (solve) {
-        for (int r = k + 1 + tid; r < mp; r += blockDim.x) z[r] -= A[(size_t)r + (size_t)mp * k] * z[k];
-      }
-      __syncthreads();
     }
+    double ld = 0.0;
+    if (!s_singular)
+      for (int r = tid; r < mp; r += blockDim.x) ld += log_abs(pivabs[r]);
+    ld = block_sum_det(ld, red);  // contains __syncthreads
     if (tid == 0) {
       if (s_singular) {
         logdet[i] = -INFINITY;
@@ -1053,6 +1138,7 @@ __global__ void __launch_bounds__(kThreads)
       if (s_singular) {
         for (int r = tid; r < m; r += blockDim.x) y[(size_t)i * m + r] = NAN;
       } else {
+        block_forward_solve<T>(A, mp, z, D);
         block_back_solve<T>(A, mp, z, D);
         residual<T>(m, P, n, i, rows, theta, nu, z, res);
         for (int r = tid; r < mp; r += blockDim.x) d[r] = (perm[r] < m) ? (T)res[perm[r]] : T(0);

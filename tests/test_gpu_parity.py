@@ -347,6 +347,32 @@ def test_pivoting_fallback(built_lib, precision, levels):
     assert np.isfinite(vb["n"]).all()
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_pivoting_fallback_forecast(built_lib, precision):
+    """Forecast draws through the partial-pivoting redo (levels = 0 and a
+    multiplier of 20 below the diagonal): the permuted solve plus one FP64
+    refinement gives y = (I - Gamma)^-1 nu of the oracle."""
+    m, P = 3, 1
+    sp = np.array([[0 + 3 * 1, 1 + 3 * 0, 2 + 3 * 0]], dtype=np.float64)
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents([1, 1, 1], sp)
+    s.setEliminationLevels(0)
+    s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
+    s.setPriorParameters(np.array([[0.3, 20.0, -15.0]]), np.full((1, 1, m), 1e-4),
+                         np.full(m, 20.0), np.full(m, 1.0))
+    s.setRngState(8, 0)
+    x = np.zeros((P, m), order="F")
+    out = s.computeForecastDebug(256, 256, x)
+    assert s.getStats()["draws_pivoted"] == 256
+    lam = np.asfortranarray(out["lambdas"].T)
+    th = np.asfortranarray(out["thetas"].transpose(0, 2, 1))
+    y, _ = oracle.forecast(sp.astype(np.uint32), lam, th, x, 8, 0)
+    # y_1 = nu_1 + 20 y_0 cancels terms of size ~6 down to ~1e-2: FP32 factors plus
+    # one FP64-residual refinement leave absolute errors of a few 1e-6 there
+    tol = dict(rtol=1e-5, atol=1e-5) if precision == "mixed" else dict(rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(out["y"], y, **tol)
+
+
 def test_fused_device_step_matches_api_sequence(built_lib):
     torch = pytest.importorskip("torch")
     d = readme_inputs(100)
