@@ -49,7 +49,8 @@ constexpr int kWarps = kThreads / 32;
 constexpr double kPivotThreshold = 8.0;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kDs = 36;  // row stride of D^-1 in shared memory (16-byte rows, 4-way store conflicts)
-constexpr int kUs = 36;  // stride of the row panel B, stored column by column: B[c][t] at t*kUs + c
+constexpr int kUs = 36;
+constexpr int kGjRows = 224;  // rows of C the panel Gauss-Jordan holds (warps 1..7)  // stride of the row panel B, stored column by column: B[c][t] at t*kUs + c
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -81,11 +82,11 @@ __device__ double block_sum_det(double v, double *red) {
 // panel buffers Lp (C, column-major, 32 x Rmax) / Up (B, Rmax columns of kUs)
 // and the value slots of the sparse levels (nv_smem of them, 0 when they live in
 // global memory) share one region: the slots are dead while the panels are in
-// use.  pcol / prow receive the pivot columns / rows of the Gauss-Jordan steps.
+// use.  prow passes the pivot rows of the panel Gauss-Jordan's super-steps.
 struct Smem {
   int Rmax;
-  size_t off_D, off_pcol, off_prow, off_Lp, off_Up, off_vals, off_z, off_nu, off_res, off_zf,
-      off_yf, off_yd, off_red, off_bsum, total;
+  size_t off_D, off_prow, off_Lp, off_Up, off_vals, off_z, off_nu, off_res, off_zf, off_yf,
+      off_yd, off_red, off_bsum, total;
   __host__ __device__ Smem(int dp, int m, size_t tsz, int nv_smem) {
     Rmax = dp - kB > 0 ? dp - kB : kB;
     size_t o = 0;
@@ -95,8 +96,7 @@ struct Smem {
       return at;
     };
     off_D = take((size_t)kB * kDs * tsz);
-    off_pcol = take((size_t)kB * kB * tsz);
-    off_prow = take((size_t)kB * kB * tsz);
+    off_prow = take((size_t)2 * kB * 4 * tsz);
     const size_t panels = ((size_t)kB * Rmax + (size_t)Rmax * kUs) * tsz;
     const size_t vals = (((size_t)nv_smem + 3) / 4) * 4 * tsz;
     off_Lp = take(panels > vals ? panels : vals);
@@ -228,13 +228,14 @@ template <> struct Pair<double> {
 };
 
 // Register-tiled trailing update A[r0:, r0:] -= Lp B over the rows r0 .. r0+R and
-// the C columns r0+c_off .. (a chunk of the R x R trailing matrix), B (32 x C)
-// read from Up[t * kUs + c] with t relative to the chunk.  16 x 16 threads; thread (tr, tc) owns rows
-// {tr*W + a, 16W + tr*W + a} and columns {tc*4 + b, 64 + tc*4 + b} of a
-// (32W) x 128 tile.  Lp reads are 16-byte vectors, the 8 threads of each access
-// phase reading one contiguous 128-byte line; B is read two k at a time (two
-// distinct addresses per warp).  Global loads are 16-byte
-// vectors, 16 threads covering 256 contiguous bytes of a column.
+// the C columns r0+c_off .. (a chunk of the R x R trailing matrix; R and C are
+// multiples of 32), B (32 x C) read from Up[t * kUs + c] with t relative to the
+// chunk.  The region is cut exactly into units of 2W rows x 8 columns: rows
+// {ra .. ra+W-1, ra+R/2 .. ra+R/2+W-1} and columns {ca .. ca+3, ca+C/2 .. ca+C/2+3},
+// handed to the threads round-robin (no padded tiles).  Consecutive threads take
+// consecutive row groups, so Lp reads are conflict-free 16-byte vectors over one
+// contiguous line, B reads see at most two addresses per warp, and the global
+// loads and stores of the accumulators are coalesced 16-byte vectors.
 template <typename T>
 __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r0, int R,
                                                 int c_off, int C, const T *__restrict__ Lp,
@@ -242,84 +243,57 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
   using V = Vec<T>;
   constexpr int W = V::W;
   constexpr int TM = 2 * W, TN = 8;
-  constexpr int tileM = 32 * W, tileN = 128;
-  const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
-  for (int tile_r = 0; tile_r < R; tile_r += tileM) {
-    for (int tile_c = 0; tile_c < C; tile_c += tileN) {
-      const int ra = tile_r + tr * W, rb = ra + 16 * W;
-      const int ca = tile_c + tc * 4, cb = ca + 64;
-      if (ra >= R || ca >= C) continue;  // chunk b lies beyond chunk a
-      const bool vb = rb < R, wb = cb < C;
-      T acc[TM][TN];
+  const int nrg = R / (2 * W), hr = R / 2, hc = C / 2;
+  const int nu = nrg * (C / 8);
+  T *Abase = A + (size_t)mp * (r0 + c_off) + r0;
+  for (int u = threadIdx.x; u < nu; u += blockDim.x) {
+    const int cg = u / nrg, rg = u - cg * nrg;
+    const int ra = rg * W, rb = ra + hr;
+    const int ca = cg * 4, cb = ca + hc;
+    T acc[TM][TN];
 #pragma unroll
-      for (int b = 0; b < TN; ++b) {
-        const int col = (b < 4) ? (ca + b) : (cb + b - 4);
-        const bool cv = (b < 4) || wb;
-        T tmp[W];
-        if (cv) {
-          const T *colp = A + (size_t)mp * (r0 + c_off + col) + r0;
-          V::ld(colp + ra, tmp);
+    for (int b = 0; b < TN; ++b) {
+      const int col = (b < 4) ? (ca + b) : (cb + b - 4);
+      const T *colp = Abase + mp * col;
+      T tmp[W];
+      V::ld(colp + ra, tmp);
 #pragma unroll
-          for (int a = 0; a < W; ++a) acc[a][b] = tmp[a];
-          if (vb) {
-            V::ld(colp + rb, tmp);
+      for (int a = 0; a < W; ++a) acc[a][b] = tmp[a];
+      V::ld(colp + rb, tmp);
 #pragma unroll
-            for (int a = 0; a < W; ++a) acc[W + a][b] = tmp[a];
-          } else {
-#pragma unroll
-            for (int a = 0; a < W; ++a) acc[W + a][b] = T(0);
-          }
-        } else {
-#pragma unroll
-          for (int a = 0; a < TM; ++a) acc[a][b] = T(0);
-        }
-      }
+      for (int a = 0; a < W; ++a) acc[W + a][b] = tmp[a];
+    }
 #pragma unroll 1
-      for (int k2 = 0; k2 < kB; k2 += 2) {
-        T u2[TN][2];
-#pragma unroll
-        for (int b = 0; b < TN; ++b) {
-          const int col = (b < 4) ? (ca + b) : (cb + b - 4);
-          if ((b < 4) || wb) {
-            Pair<T>::ld(Up + col * kUs + k2, u2[b]);
-          } else {
-            u2[b][0] = T(0);
-            u2[b][1] = T(0);
-          }
-        }
-#pragma unroll
-        for (int kk = 0; kk < 2; ++kk) {
-          T lv[TM];
-          const T *lrow = Lp + (k2 + kk) * Rmax;
-          V::ld(lrow + ra, lv);
-          if (vb) {
-            V::ld(lrow + rb, lv + W);
-          } else {
-#pragma unroll
-            for (int a = 0; a < W; ++a) lv[W + a] = T(0);
-          }
-#pragma unroll
-          for (int a = 0; a < TM; ++a)
-#pragma unroll
-            for (int b = 0; b < TN; ++b) acc[a][b] -= lv[a] * u2[b][kk];
-        }
-      }
+    for (int k2 = 0; k2 < kB; k2 += 2) {
+      T u2[TN][2];
 #pragma unroll
       for (int b = 0; b < TN; ++b) {
-        const bool cv = (b < 4) || wb;
-        if (!cv) continue;
         const int col = (b < 4) ? (ca + b) : (cb + b - 4);
-        T *colp = A + (size_t)mp * (r0 + c_off + col) + r0;
-        T tmp[W];
-#pragma unroll
-        for (int a = 0; a < W; ++a) tmp[a] = acc[a][b];
-        V::st(colp + ra, tmp);
-        if (vb) {
-#pragma unroll
-          for (int a = 0; a < W; ++a) tmp[a] = acc[W + a][b];
-          V::st(colp + rb, tmp);
-        }
+        Pair<T>::ld(Up + col * kUs + k2, u2[b]);
       }
+#pragma unroll
+      for (int kk = 0; kk < 2; ++kk) {
+        T lv[TM];
+        const T *lrow = Lp + (k2 + kk) * Rmax;
+        V::ld(lrow + ra, lv);
+        V::ld(lrow + rb, lv + W);
+#pragma unroll
+        for (int a = 0; a < TM; ++a)
+#pragma unroll
+          for (int b = 0; b < TN; ++b) acc[a][b] -= lv[a] * u2[b][kk];
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < TN; ++b) {
+      const int col = (b < 4) ? (ca + b) : (cb + b - 4);
+      T *colp = Abase + mp * col;
+      T tmp[W];
+#pragma unroll
+      for (int a = 0; a < W; ++a) tmp[a] = acc[a][b];
+      V::st(colp + ra, tmp);
+#pragma unroll
+      for (int a = 0; a < W; ++a) tmp[a] = acc[W + a][b];
+      V::st(colp + rb, tmp);
     }
   }
 }
@@ -334,17 +308,18 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
-// Issues the copies of the column panel C (rows r0.., columns k0..k0+31) into
-// Lp[c * Rmax + t] and of the row panel B (rows k0..k0+31, columns r0..) into
-// Up[t * kUs + c]; both are 16-byte pieces of contiguous global columns.
+// Issues the copies of rows t_begin.. of the column panel C (rows r0.., columns
+// k0..k0+31) into Lp[c * Rmax + t] and of the row panel B (rows k0..k0+31,
+// columns r0..) into Up[t * kUs + c]; both are 16-byte pieces of contiguous
+// global columns.
 template <typename T>
 __device__ __forceinline__ void stage_panels_async(const T *__restrict__ A, int dp, int k0, int r0,
-                                                   int R, T *Lp, T *Up, int Rmax) {
+                                                   int R, int t_begin, T *Lp, T *Up, int Rmax) {
   constexpr int W = Vec<T>::W;
-  const int RW = R / W, nc = kB * RW;
+  const int RW = (R - t_begin) / W, nc = kB * RW;
   for (int u = threadIdx.x; u < nc; u += blockDim.x) {
-    const int c = u / RW, tw = u - c * RW;
-    cp_async16(Lp + c * Rmax + tw * W, A + (size_t)(r0 + tw * W) + (size_t)dp * (k0 + c));
+    const int c = u / RW, t = t_begin + (u - c * RW) * W;
+    cp_async16(Lp + c * Rmax + t, A + (size_t)(r0 + t) + (size_t)dp * (k0 + c));
   }
   constexpr int QW = kB / W;
   for (int u = threadIdx.x; u < R * QW; u += blockDim.x) {
@@ -363,147 +338,94 @@ __device__ __forceinline__ float rcp_fast(float x) {
 }
 __device__ __forceinline__ double rcp_fast(double x) { return 1.0 / x; }
 
-// In-register inverse of a 4 x 4 block by Gauss-Jordan elimination without
-// pivoting (m[q][q'] = row q, column q').
+// Panel Gauss-Jordan: column elimination of the stacked block column [D; C]
+// (D the 32 x 32 diagonal block, C the rows below it) with 4 x 4 pivot blocks,
+// in place, giving [D^-1; C D^-1] -- the block inverse and the block multipliers
+// of the elimination in one pass.  Warp 0 holds the rows of D, warps 1..7 up to
+// 224 rows of C; every thread keeps its row in registers (a[p], column position
+// p).  Super-step K (pivot rows c0 = 4K .. 4K+3 of D, pivot columns at positions
+// 0..3) right-multiplies by [[P^-1, -P^-1 B], [0, I]]:
+//   rows outside the pivot rows:  a[pivot] <- g = a[0..3] P^-1,
+//                                 a[p]     <- a[p] - g . M[K][p]
+//   pivot row qi:                 a[pivot] <- (P^-1)[qi][*],
+//                                 a[p]     <- -(P^-1 M[K][p])[qi]
+// and rotates the columns by four positions (a[p-4] <- new a[p], a[28..31] <- the
+// new pivot columns), so that every register index is a constant and after
+// eight super-steps the columns are back in place.  The pivot rows travel
+// through shared memory (prowT, two alternating buffers of 32 positions x 4, so
+// one barrier per super-step suffices); each warp inverts P in 16 lanes by
+// Gauss-Jordan with shuffles.  The pivots of P are the LU pivots of D.
+// No-pivot check: zero / non-finite pivots, LU multipliers inside P above tau,
+// and block multipliers g of the rows still to be eliminated (rows of D below the
+// pivot rows, all rows of C) above tau.  Thread 0 returns sum log|det P|.
 template <typename T>
-__device__ __forceinline__ void invert4(T (&m)[4][4]) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const T rp = rcp_fast(m[k][k]);
-    T rk[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) rk[j] = (j == k) ? rp : m[k][j] * rp;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      if (i == k) continue;
-      const T f = m[i][k];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) m[i][j] = (j == k) ? -f * rp : m[i][j] - f * rk[j];
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) m[k][j] = rk[j];
-  }
-}
-
-// Gauss-Jordan inversion (no pivoting) of the 32 x 32 block D by all eight warps,
-// with 4 x 4 pivot blocks: thread (lane i, warp w) holds a[s] = D[i][w + 8s].
-// Super-step K (pivot rows / columns c0 = 4K .. 4K+3) publishes the pivot
-// columns in pcol[c][*] (from warps 4(K%2) .. +3) and the pivot rows in
-// prowT[c][c0 ..] (from lanes c0 .. c0+3), then every thread inverts the pivot
-// block P itself and updates its four entries:
-//   i, c outside the block:  a -= M[i][K] P^-1 M[K][c]
-//   i in the block:          row (P^-1 M[K][*]) of the scaled pivot rows
-//   c in the block:          -(M[i][K] P^-1), resp. P^-1 itself.
-// Each super-step writes its own pcol / prowT entries, so one barrier per
-// super-step suffices; eight in all.  pcol keeps the pivot columns as published
-// (the Schur complement's columns, for the LU check).  On return
-// a[s] = (D^-1)[i][w + 8s].
-template <typename T>
-__device__ __forceinline__ void gauss_jordan_invert(T (&a)[4], T *pcol, T *prowT) {
+__device__ __forceinline__ double panel_gauss_jordan(T (&a)[kB], bool active, T *prowT, T tau,
+                                                     bool &bad) {
   using V = Vec<T>;
-  const int i = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int l16 = lane & 15, pq = l16 >> 2, pc = l16 & 3;
+  double ld = 0.0;
 #pragma unroll 1
   for (int K = 0; K < kB / 4; ++K) {
-    const int c0 = 4 * K, sK = K >> 1, w0 = (K & 1) * 4;
-    const bool inK = (i >= c0 && i < c0 + 4);
-    if (w >= w0 && w < w0 + 4)
-      pcol[(c0 + w - w0) * kB + i] = sK == 0 ? a[0] : sK == 1 ? a[1] : sK == 2 ? a[2] : a[3];
+    const int c0 = 4 * K;
+    T *buf = prowT + (K & 1) * (kB * 4);
+    const bool inK = (warp == 0) && lane >= c0 && lane < c0 + 4;
     if (inK) {
 #pragma unroll
-      for (int s = 0; s < 4; ++s) prowT[(w + 8 * s) * kB + i] = a[s];
+      for (int p = 0; p < kB; ++p) buf[p * 4 + (lane - c0)] = a[p];
     }
     __syncthreads();
-    T Pm[4][4];
+    // P^-1 in 16 lanes: lane (pq, pc) holds entry (pq, pc)
+    T mv = buf[pc * 4 + pq];
+    T det = T(1);
 #pragma unroll
-    for (int qc = 0; qc < 4; ++qc) {
-      T col[4];
-#pragma unroll
-      for (int q = 0; q < 4; q += V::W) V::ld(prowT + (c0 + qc) * kB + c0 + q, col + q);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) Pm[q][qc] = col[q];
+    for (int k = 0; k < 4; ++k) {
+      const T pk = __shfl_sync(kFull, mv, 5 * k);
+      if (!(finite_t(pk) && pk != T(0))) bad = true;
+      det *= pk;
+      const T rp = rcp_fast(pk);
+      const T prk = __shfl_sync(kFull, mv, 4 * k + pc);
+      const T fik = __shfl_sync(kFull, mv, 4 * pq + k);
+      if (pq > k && pc == k && !(dabs(fik * rp) <= tau)) bad = true;
+      mv = (pq == k) ? ((pc == k) ? rp : prk * rp) : ((pc == k) ? -fik * rp : mv - fik * (prk * rp));
     }
-    invert4<T>(Pm);
-    // g = f P^-1 with f = M[i][K] (rows outside the block) or the unit vector e_qi
-    const int qi = i - c0;
+    if (threadIdx.x == 0) ld += log_abs(det);
+    // g = f P^-1, f = this row's pivot-column entries (unit vector for pivot rows)
     T f[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) f[q] = inK ? (q == qi ? T(1) : T(0)) : pcol[(c0 + q) * kB + i];
+    for (int q = 0; q < 4; ++q) f[q] = inK ? (q == lane - c0 ? T(1) : T(0)) : a[q];
     T g[4];
 #pragma unroll
-    for (int qc = 0; qc < 4; ++qc) {
+    for (int c = 0; c < 4; ++c) {
       T acc = T(0);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc += f[q] * Pm[q][qc];
-      g[qc] = acc;
+      for (int q = 0; q < 4; ++q) acc += f[q] * __shfl_sync(kFull, mv, 4 * q + c);
+      g[c] = acc;
     }
-    const T sgn = inK ? T(1) : T(-1);
+    if (active && (warp > 0 || lane >= c0 + 4)) {
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      const int c = w + 8 * s;
-      if (s == sK && w >= w0 && w < w0 + 4) {
-        const int qc = w - w0;
-        const T gq = qc == 0 ? g[0] : qc == 1 ? g[1] : qc == 2 ? g[2] : g[3];
-        a[s] = sgn * gq;
-      } else {
+      for (int c = 0; c < 4; ++c)
+        if (!(dabs(g[c]) <= tau)) bad = true;
+    }
+    if (warp == 0) {
+#pragma unroll
+      for (int p = 4; p < kB; ++p) {
         T r[4];
 #pragma unroll
-        for (int q = 0; q < 4; q += V::W) V::ld(prowT + c * kB + c0 + q, r + q);
-        const T dot = g[0] * r[0] + g[1] * r[1] + g[2] * r[2] + g[3] * r[3];
-        a[s] = (inK ? T(0) : a[s]) + sgn * dot;
+        for (int q = 0; q < 4; q += V::W) V::ld(buf + p * 4 + q, r + q);
+        a[p - 4] = (inK ? T(0) : a[p]) - (g[0] * r[0] + g[1] * r[1] + g[2] * r[2] + g[3] * r[3]);
+      }
+    } else {
+#pragma unroll
+      for (int p = 4; p < kB; ++p) {
+        T r[4];
+#pragma unroll
+        for (int q = 0; q < 4; q += V::W) V::ld(buf + p * 4 + q, r + q);
+        a[p - 4] = a[p] - (g[0] * r[0] + g[1] * r[1] + g[2] * r[2] + g[3] * r[3]);
       }
     }
-  }
-}
-
-// No-pivot check and log|det| share of the block from the published pivot data:
-// thread (row r = lane, super-step K = warp) redoes the 4 x 4 LU of that
-// super-step's pivot block P and flags a zero / non-finite pivot or a scalar LU
-// multiplier above tau (below the diagonal inside P, or M[r][K] U_P^-1 for rows
-// r below the block).  Lane 0 of each warp returns sum log|u_qq| of its block.
-template <typename T>
-__device__ __forceinline__ double pivot_blocks_check(const T *pcol, const T *prowT, T tau,
-                                                     bool &bad) {
-  const int r = threadIdx.x & 31, K = threadIdx.x >> 5, c0 = 4 * K;
-  T U[4][4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q)
-#pragma unroll
-    for (int qc = 0; qc < 4; ++qc) U[q][qc] = prowT[(c0 + qc) * kB + c0 + q];
-  T Lq[4][4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (!(finite_t(U[k][k]) && U[k][k] != T(0))) bad = true;
-    const T rp = rcp_fast(U[k][k]);
-#pragma unroll
-    for (int q = k + 1; q < 4; ++q) {
-      const T l = U[q][k] * rp;
-      Lq[q][k] = l;
-#pragma unroll
-      for (int qc = k + 1; qc < 4; ++qc) U[q][qc] -= l * U[k][qc];
-    }
-  }
-  if (r >= c0 && r < c0 + 4) {
-    const int qr = r - c0;
-#pragma unroll
-    for (int q = 1; q < 4; ++q)
-#pragma unroll
-      for (int k = 0; k < q; ++k)
-        if (q == qr && !(dabs(Lq[q][k]) <= tau)) bad = true;
-  } else if (r >= c0 + 4) {
-    T l[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      T x = pcol[(c0 + q) * kB + r];
-#pragma unroll
-      for (int k = 0; k < q; ++k) x -= l[k] * U[k][q];
-      l[q] = x / U[q][q];
-      if (!(dabs(l[q]) <= tau)) bad = true;
-    }
-  }
-  double ld = 0.0;
-  if (r == 0) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) ld += log_abs(U[q][q]);
+    for (int c = 0; c < 4; ++c) a[kB - 4 + c] = g[c];
   }
   return ld;
 }
@@ -698,7 +620,6 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0);
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);  // D^-1, row-major, stride kB
-  T *pcol = reinterpret_cast<T *>(smem_raw + L.off_pcol);
   T *prow = reinterpret_cast<T *>(smem_raw + L.off_prow);
   T *Lp = reinterpret_cast<T *>(smem_raw + L.off_Lp);
   T *Up = reinterpret_cast<T *>(smem_raw + L.off_Up);
@@ -832,30 +753,49 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     __syncthreads();
     for (int kb = 0; kb < nbk; ++kb) {
       const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
-      // (a) panels C and B in flight while all warps invert D by Gauss-Jordan
-      if (R > 0) stage_panels_async<T>(A, dp, k0, r0, R, Lp, Up, Rmax);
+      const int Rg = R < kGjRows ? R : kGjRows;  // rows of C inside the panel Gauss-Jordan
+      // (a) the row panel B (and rows of C beyond Rg) in flight while the panel
+      // Gauss-Jordan turns [D; C] into [D^-1; C D^-1]
+      if (R > 0) stage_panels_async<T>(A, dp, k0, r0, R, Rg, Lp, Up, Rmax);
       {
-        T a[4];
-        const T *dcol = A + (size_t)(k0 + lane) + (size_t)dp * k0;
+        const int t = (warp - 1) * 32 + lane;  // row of C (warps 1..7)
+        const bool active = (warp == 0) || t < Rg;
+        T *rowp = A + (size_t)(warp == 0 ? k0 + lane : r0 + t) + (size_t)dp * k0;
+        T a[kB];
 #pragma unroll
-        for (int s = 0; s < 4; ++s) a[s] = dcol[(size_t)dp * (warp + 8 * s)];
-        gauss_jordan_invert<T>(a, pcol, prow);
-        ld_part += pivot_blocks_check<T>(pcol, prow, tau, bad);
+        for (int q = 0; q < kB; ++q) a[q] = active ? rowp[(size_t)dp * q] : T(0);
+        if (warp == 0 || (warp - 1) * 32 < Rg) {
+          ld_part += panel_gauss_jordan<T>(a, active, prow, tau, bad);
+        } else {
+          for (int K = 0; K < kB / 4; ++K) __syncthreads();  // the same barriers, no rows
+        }
+        if (warp == 0) {
 #pragma unroll
-        for (int s = 0; s < 4; ++s) D[lane * kDs + warp + 8 * s] = a[s];
-        if (solve) {
-          T *dc = A + (size_t)(k0 + lane) + (size_t)dp * k0;
+          for (int q = 0; q < kB; q += W) V::st(D + lane * kDs + q, a + q);
+        } else if (active) {
 #pragma unroll
-          for (int s = 0; s < 4; ++s) dc[(size_t)dp * (warp + 8 * s)] = a[s];
+          for (int q = 0; q < kB; ++q) Lp[q * Rmax + t] = a[q];
+        }
+        if (solve && active) {
+          // keep D^-1 and C D^-1 for the solves; the right-hand side rides along
+#pragma unroll
+          for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = a[q];
+          if (warp > 0) {
+            T acc = T(0);
+#pragma unroll
+            for (int q = 0; q < kB; ++q) acc += a[q] * z[k0 + q];
+            z[r0 + t] -= acc;
+          }
         }
       }
       cp_async_wait_all();
       __syncthreads();
-      if (R > 0) {
-        // (b) Lp <- C D^-1 in place: warp (half, quarter) owns 32 rows x 8 columns
-        // of each 64-row round; a round reads its rows completely before writing.
+      if (R > Rg) {
+        // (b) rows of C beyond Rg: Lp <- C D^-1 in place; warp (half, quarter) owns
+        // 32 rows x 8 columns of each 64-row round, a round reads its rows before
+        // writing them.
         const int qc = (warp >> 1) * 8;
-        for (int t0 = 0; t0 < R; t0 += 64) {
+        for (int t0 = Rg; t0 < R; t0 += 64) {
           const int t = t0 + (warp & 1) * 32 + lane;
           const bool act = t < R;
           T o[8];
@@ -883,21 +823,22 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         }
         __syncthreads();
         if (solve) {
-          // keep C D^-1 for the solves; the right-hand side rides along
-          const int RW = R / W;
+          const int RW = (R - Rg) / W;
           for (int u = tid; u < kB * RW; u += blockDim.x) {
-            const int c = u / RW, tw = u - c * RW;
+            const int c = u / RW, tt = Rg + (u - c * RW) * W;
             T v[W];
-            V::ld(Lp + c * Rmax + tw * W, v);
-            V::st(A + (size_t)(r0 + tw * W) + (size_t)dp * (k0 + c), v);
+            V::ld(Lp + c * Rmax + tt, v);
+            V::st(A + (size_t)(r0 + tt) + (size_t)dp * (k0 + c), v);
           }
-          for (int t = tid; t < R; t += blockDim.x) {
+          for (int tt = Rg + tid; tt < R; tt += blockDim.x) {
             T acc = T(0);
 #pragma unroll 8
-            for (int c = 0; c < kB; ++c) acc += Lp[c * Rmax + t] * z[k0 + c];
-            z[r0 + t] -= acc;
+            for (int c = 0; c < kB; ++c) acc += Lp[c * Rmax + tt] * z[k0 + c];
+            z[r0 + tt] -= acc;
           }
         }
+      }
+      if (R > 0) {
         // (c) trailing update E -= (C D^-1) B
         trailing_update<T>(A, dp, r0, R, 0, R, Lp, Up, Rmax);
       }
