@@ -178,6 +178,41 @@ EliminationPlanHost plan_elimination(int m, int P, const std::vector<unsigned> &
     }
   pl.core_n = (int)pl.core_node.size();
   pl.dp = std::max(32, (pl.core_n + 31) / 32 * 32);
+  // renumber the slots: the constants, then the values the solve programs read,
+  // then the rest (so that a solve needs only a prefix of the slot array)
+  std::vector<int> remap(nv, -1);
+  int next = 0;
+  remap[kSlotZero] = next++;
+  remap[kSlotOne] = next++;
+  auto take = [&](int slot) {
+    if (remap[slot] < 0) remap[slot] = next++;
+  };
+  for (unsigned f : pl.fwd) take((int)(f & 0xFFFFu));
+  for (unsigned b : pl.bwd) take((int)(b & 0xFFFFu));
+  for (int d : pl.bwd_diag) take(d);
+  pl.n_solve = next;
+  for (int v = 0; v < nv; ++v) take(v);
+  auto lo_map = [&](unsigned w) { return pack16((unsigned)remap[w & 0xFFFFu], w >> 16); };
+  auto both_map = [&](unsigned w) {
+    return pack16((unsigned)remap[w & 0xFFFFu], (unsigned)remap[w >> 16]);
+  };
+  pl.diag_slot.resize(m);
+  for (int r = 0; r < m; ++r) pl.diag_slot[r] = remap[(int)kSlotDiag0 + r];
+  pl.l0_slot.resize(pl.l0_e.size());
+  for (size_t k = 0; k < pl.l0_e.size(); ++k) pl.l0_slot[k] = remap[(int)kSlotDiag0 + m + (int)k];
+  for (int &v : pl.piv) v = remap[v];
+  for (unsigned &w : pl.scale) w = both_map(w);
+  for (unsigned &w : pl.ent) {
+    const unsigned out = w & 0xFFFFu;
+    w = pack16(out == kSlotNone ? kSlotNone : (unsigned)remap[out], (unsigned)remap[w >> 16]);
+  }
+  for (unsigned &w : pl.terms) w = both_map(w);
+  for (unsigned &w : pl.fwd) w = lo_map(w);
+  for (unsigned &w : pl.bwd) w = lo_map(w);
+  for (int &v : pl.bwd_diag) v = remap[v];
+  for (int &v : diag) v = remap[v];
+  for (int r = 0; r < m; ++r)
+    for (auto &kv : rows[r]) kv.second = remap[kv.second];
   if (pl.nlev > 0) {
     const size_t dp = (size_t)pl.dp;
     pl.core_map.assign(dp * dp, (uint16_t)kSlotZero);

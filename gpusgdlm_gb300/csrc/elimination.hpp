@@ -19,9 +19,10 @@
 // multiplier L[r][t] replaces M[r][t] in its slot.  Slot indices fit 16 bits.
 //   slot 0             constant 0 (padding terms read it; never written)
 //   slot 1             constant 1 (identity padding of the dense core)
-//   slots 2 .. 2+m     diagonal of (I - Gamma) = 1 (then updated in place)
-//   slots 2+m ..       level-0 off-diagonals -theta[e] (e = j*max_p + k)
-//   then the fill-in each level creates.
+//   slots 2 .. n_solve the values the forward / backward solve programs read
+//                      (rows, columns and pivots of the eliminated nodes)
+//   then everything else.
+// Initial values: vals[diag_slot[r]] = 1, vals[l0_slot[k]] = -theta[l0_e[k]].
 // A level runs as: pivots and multipliers (scale), barrier, new entries,
 // barrier.  Entries are grouped in chunks of 32 (one per warp lane), sorted by
 // term count so that a chunk's lanes do the same number of terms; a chunk's
@@ -45,7 +46,10 @@ struct EliminationPlanHost {
   int m = 0, P = 0;
   int nlev = 0;
   int nv = 0;                        // slots per draw
-  std::vector<int> l0_e;             // theta index e of slot kSlotDiag0 + m + k
+  int n_solve = 2;                   // slots [0, n_solve) hold what the solves read
+  std::vector<int> diag_slot;        // m initial diagonal slots (value 1)
+  std::vector<int> l0_e;             // theta index e (j*max_p + k) of level-0 entry
+  std::vector<int> l0_slot;          // its slot (value -theta[e])
   // per level (nlev + 1 offsets each)
   std::vector<int> lev_piv;          // -> piv
   std::vector<int> piv;              // slot of M[t][t] of the eliminated nodes
@@ -79,8 +83,8 @@ struct EliminationPlanHost {
 // Device copy of the plan (pointers into one allocation owned by the engine).
 // core_map == nullptr means "no plan": the whole matrix is the dense core.
 struct EliminationPlan {
-  int m, P, nlev, nv, nnz0, core_n;
-  const int *l0_e;
+  int m, P, nlev, nv, n_solve, nnz0, core_n;
+  const int *diag_slot, *l0_e, *l0_slot;
   const int *lev_piv, *piv;
   const int *lev_scale;
   const unsigned *scale;

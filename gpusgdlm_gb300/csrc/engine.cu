@@ -86,6 +86,7 @@ struct sgdlm_engine {
   DevBuf<unsigned> p, sp;
   DevBuf<int> g_rowptr;
   DevBuf<int2> g_ent;
+  DevBuf<int> g_extptr, g_extk;
   // sparse pre-elimination plan of (I - Gamma) (elimination.hpp)
   int elim_levels = 4;
   EliminationPlanHost eplan;
@@ -206,6 +207,17 @@ int upload_gamma_rows(sgdlm_engine *h) {
   CK(h->g_ent.alloc(ent.size()));
   CK(cudaMemcpy(h->g_rowptr.ptr, rowptr.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->g_ent.ptr, ent.data(), ent.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  std::vector<int> extptr(m + 1, 0), extk;
+  for (size_t j = 0; j < m; ++j) {
+    for (size_t k = 0; k < P; ++k)
+      if ((size_t)h->h_sp[j * P + k] >= mm) extk.push_back((int)k);
+    extptr[j + 1] = (int)extk.size();
+  }
+  if (extk.empty()) extk.push_back(0);
+  CK(h->g_extptr.alloc(m + 1));
+  CK(h->g_extk.alloc(extk.size()));
+  CK(cudaMemcpy(h->g_extptr.ptr, extptr.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->g_extk.ptr, extk.data(), extk.size() * sizeof(int), cudaMemcpyHostToDevice));
   return SGDLM_OK;
 }
 
@@ -223,7 +235,9 @@ int upload_elimination(sgdlm_engine *h) {
     const int *p = static_cast<const int *>(data);
     buf.insert(buf.end(), p, p + n_ints);
   };
+  put(pl.diag_slot.data(), pl.diag_slot.size());
   put(pl.l0_e.data(), pl.l0_e.size());
+  put(pl.l0_slot.data(), pl.l0_slot.size());
   put(pl.lev_piv.data(), pl.lev_piv.size());
   put(pl.piv.data(), pl.piv.size());
   put(pl.lev_scale.data(), pl.lev_scale.size());
@@ -254,10 +268,13 @@ int upload_elimination(sgdlm_engine *h) {
   d.P = P;
   d.nlev = pl.nlev;
   d.nv = pl.nlev > 0 ? pl.nv : 0;
+  d.n_solve = pl.nlev > 0 ? pl.n_solve : 0;
   d.nnz0 = (int)pl.l0_e.size();
   d.core_n = pl.nlev > 0 ? pl.core_n : m;
   size_t k = 0;
+  d.diag_slot = b + offs[k++];
   d.l0_e = b + offs[k++];
+  d.l0_slot = b + offs[k++];
   d.lev_piv = b + offs[k++];
   d.piv = b + offs[k++];
   d.lev_scale = b + offs[k++];
@@ -348,6 +365,8 @@ void release_all(sgdlm_engine *h) {
   h->sp.release();
   h->g_rowptr.release();
   h->g_ent.release();
+  h->g_extptr.release();
+  h->g_extk.release();
   h->elim_buf.release();
   h->elim_dev = EliminationPlan{};
   h->series_flags.release();
@@ -452,7 +471,7 @@ template <typename T>
 void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   const long n = (long)h->nsim;
   const bool refine = (h->precision != SGDLM_PRECISION_FP64);
-  const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr};
+  const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr, h->g_extptr.ptr, h->g_extk.ptr};
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
                as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
                refine, y, rows);

@@ -86,8 +86,12 @@ template <typename T> LuPlan plan_lu(int m, int P, long n, int num_sms, int core
 // rowptr[r] .. rowptr[r+1]-1 are (e = j*P + k, column).  Built on the host from
 // the parental sets; gives the forecast residual a fixed summation order.
 struct GammaRows {
-  const int *rowptr;  // m + 1
-  const int2 *ent;    // nnz
+  const int *rowptr;   // m + 1
+  const int2 *ent;     // nnz
+  // external predictors: for series j, the k with sp[j*P + k] >= m*m are
+  // ext_k[ext_ptr[j] .. ext_ptr[j+1]-1] (the terms of nu's mean)
+  const int *ext_ptr;  // m + 1
+  const int *ext_k;
 };
 struct EliminationPlan;
 template <typename T>

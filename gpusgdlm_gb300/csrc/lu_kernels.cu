@@ -148,11 +148,10 @@ struct FallbackSmem {
 // nu_j = z/sqrt(lambda) + sum over external predictors x_jk theta_jk for draw i
 // (batchedComputeNuPlusMu, kernel_functions.cuh:1156-1178), into nu (double).
 template <typename T>
-__device__ void forecast_rhs(int m, int P, long n, long i, const unsigned *__restrict__ sp,
+__device__ void forecast_rhs(int m, int P, long n, long i, GammaRows rows,
                              const T *__restrict__ theta, const double *__restrict__ x,
                              const T *__restrict__ lambda, RngKey key, double *nu) {
   const uint32_t ep = key_epoch(key);
-  const size_t mm = (size_t)m * m;
   for (int j = threadIdx.x; j < m; j += blockDim.x) {
     const U4 g = philox((uint32_t)i, (uint32_t)j, tag_sub(TAG_NU, 0), ep, key.k0, key.k1);
     T z0, z1;
@@ -160,8 +159,10 @@ __device__ void forecast_rhs(int m, int P, long n, long i, const unsigned *__res
     const T lam = lambda[(size_t)j * n + i];
     double v = (double)(z0 / dev_sqrt(lam));
     const T *th = theta + ((size_t)j * n + i) * P;
-    for (int k = 0; k < P; ++k)
-      if ((size_t)sp[(size_t)j * P + k] >= mm) v += x[(size_t)j * P + k] * (double)th[k];
+    for (int q = rows.ext_ptr[j]; q < rows.ext_ptr[j + 1]; ++q) {
+      const int k = rows.ext_k[q];
+      v += x[(size_t)j * P + k] * (double)th[k];
+    }
     nu[j] = v;
   }
 }
@@ -431,27 +432,36 @@ __device__ __forceinline__ double panel_gauss_jordan(T (&a)[kB], bool active, T 
 }
 
 // Back solve of the block elimination, in place on v (length dp, shared):
-// for k = last .. 0:  x_k = D_k^-1 (v_k - B_k x_{>k}), with D_k^-1 stored in the
+// x_k = D_k^-1 (v_k - B_k x_{>k}) for k = last .. 0, with D_k^-1 stored in the
 // diagonal block and B_k (rows of block k, columns beyond it) untouched in A.
+// Column-oriented: as soon as x_k is known, every row above block k subtracts
+// A[r][block k] x_k (thread per row, 32 independent loads), so each block costs
+// two barriers and one round of loads instead of a dependent chain.
 template <typename T>
 __device__ void be_back_solve(const T *__restrict__ A, int dp, T *v, T *bsum) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31;
   for (int kb = dp / kB - 1; kb >= 0; --kb) {
-    const int k0 = kb * kB, r0 = k0 + kB;
-    T acc = T(0);
-    for (int col = r0 + warp; col < dp; col += kWarps)
-      acc += A[(size_t)(k0 + lane) + (size_t)dp * col] * v[col];
-    bsum[warp * kB + lane] = acc;
-    __syncthreads();
-    if (warp == 0) {
-      T w = v[k0 + lane];
+    const int k0 = kb * kB;
+    if (tid < 32) {
+      T dinv[kB];
 #pragma unroll
-      for (int s = 0; s < kWarps; ++s) w -= bsum[s * kB + lane];
+      for (int c = 0; c < kB; ++c) dinv[c] = A[(size_t)(k0 + lane) + (size_t)dp * (k0 + c)];
+      const T w = v[k0 + lane];
       T xk = T(0);
-#pragma unroll 8
-      for (int c = 0; c < kB; ++c)
-        xk += A[(size_t)(k0 + lane) + (size_t)dp * (k0 + c)] * __shfl_sync(kFull, w, c);
-      v[k0 + lane] = xk;
+#pragma unroll
+      for (int c = 0; c < kB; ++c) xk += dinv[c] * __shfl_sync(kFull, w, c);
+      bsum[lane] = xk;
+    }
+    __syncthreads();
+    if (tid < 32) v[k0 + tid] = bsum[tid];
+    for (int r = tid; r < k0; r += blockDim.x) {
+      T b[kB];
+#pragma unroll
+      for (int c = 0; c < kB; ++c) b[c] = A[(size_t)r + (size_t)dp * (k0 + c)];
+      T acc = T(0);
+#pragma unroll
+      for (int c = 0; c < kB; ++c) acc += b[c] * bsum[c];
+      v[r] -= acc;
     }
     __syncthreads();
   }
@@ -463,9 +473,12 @@ __device__ void be_forward(const T *__restrict__ A, int dp, T *v) {
   for (int kb = 0; kb < dp / kB - 1; ++kb) {
     const int k0 = kb * kB, r0 = k0 + kB;
     for (int t = threadIdx.x; t < dp - r0; t += blockDim.x) {
+      T b[kB];
+#pragma unroll
+      for (int c = 0; c < kB; ++c) b[c] = A[(size_t)(r0 + t) + (size_t)dp * (k0 + c)];
       T acc = T(0);
-#pragma unroll 8
-      for (int c = 0; c < kB; ++c) acc += A[(size_t)(r0 + t) + (size_t)dp * (k0 + c)] * v[k0 + c];
+#pragma unroll
+      for (int c = 0; c < kB; ++c) acc += b[c] * v[k0 + c];
       v[r0 + t] -= acc;
     }
     __syncthreads();
@@ -579,16 +592,25 @@ __device__ void levels_backward(const EliminationPlan &ep, const T *vals, const 
 }
 
 // res = nu - (I - Gamma) y in FP64, one thread per row summing that row's Gamma
-// entries in a fixed order (deterministic).
+// entries in a fixed order (deterministic); the entries' indices and theta values
+// are gathered eight at a time so that their loads overlap.
 template <typename T>
 __device__ void residual(int m, int P, long n, long i, GammaRows rows,
                          const T *__restrict__ theta, const double *nu, const T *y, double *res) {
   for (int r = threadIdx.x; r < m; r += blockDim.x) {
     double v = nu[r] - (double)y[r];
-    for (int q = rows.rowptr[r]; q < rows.rowptr[r + 1]; ++q) {
-      const int2 ec = rows.ent[q];
-      const int j = ec.x / P, k = ec.x % P;
-      v += (double)theta[((size_t)j * n + i) * P + k] * (double)y[ec.y];
+    const int q1 = rows.rowptr[r + 1];
+    for (int q0 = rows.rowptr[r]; q0 < q1; q0 += 8) {
+      int2 ec[8];
+#pragma unroll
+      for (int h = 0; h < 8; ++h) ec[h] = (q0 + h < q1) ? rows.ent[q0 + h] : make_int2(-1, 0);
+      T th[8];
+#pragma unroll
+      for (int h = 0; h < 8; ++h)
+        th[h] = ec[h].x >= 0 ? theta[((size_t)(ec[h].x / P) * n + i) * P + ec[h].x % P] : T(0);
+#pragma unroll
+      for (int h = 0; h < 8; ++h)
+        if (ec[h].x >= 0) v += (double)th[h] * (double)y[ec[h].y];
     }
     res[r] = v;
   }
@@ -648,11 +670,19 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     double ld_part = 0.0;  // this thread's share of sum log|pivot| (levels and core)
     // ---- build: value slots of level 0, forecast right-hand side
     if (planned) {
-      for (int s = tid; s < (int)kSlotDiag0 + m; s += blockDim.x) vals[s] = (s == 0) ? T(0) : T(1);
+      if (tid == 0) {
+        vals[kSlotZero] = T(0);
+        vals[kSlotOne] = T(1);
+      }
+      for (int r = tid; r < m; r += blockDim.x) vals[ep.diag_slot[r]] = T(1);
       for (int k0 = tid; k0 < ep.nnz0; k0 += 4 * kThreads) {
-        int e[4];
+        int e[4], sl[4];
 #pragma unroll
-        for (int h = 0; h < 4; ++h) e[h] = (k0 + h * kThreads < ep.nnz0) ? ep.l0_e[k0 + h * kThreads] : -1;
+        for (int h = 0; h < 4; ++h) {
+          const bool ok = k0 + h * kThreads < ep.nnz0;
+          e[h] = ok ? ep.l0_e[k0 + h * kThreads] : -1;
+          sl[h] = ok ? ep.l0_slot[k0 + h * kThreads] : 0;
+        }
         T th[4];
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
@@ -661,14 +691,14 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         }
 #pragma unroll
         for (int h = 0; h < 4; ++h)
-          if (e[h] >= 0) vals[kSlotDiag0 + m + k0 + h * kThreads] = -th[h];
+          if (e[h] >= 0) vals[sl[h]] = -th[h];
       }
     } else {
       // no plan: the whole matrix is the core, scattered from the parental sets
       build_full<T>(m, P, dp, n, i, sp, theta, A);
     }
     if (solve) {
-      forecast_rhs<T>(m, P, n, i, sp, theta, x, lambda, key, nu);
+      forecast_rhs<T>(m, P, n, i, rows, theta, x, lambda, key, nu);
       for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)nu[r];
     }
     __syncthreads();
@@ -745,7 +775,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
           }
         }
       }
-      if (solve && vals_smem) copy_vals<T>(vals_g, vals, ep.nv);  // the solves need them later
+      if (solve && vals_smem) copy_vals<T>(vals_g, vals, ep.n_solve);  // what the solves read
     }
     if (solve)
       for (int r = tid; r < dp; r += blockDim.x)
@@ -853,7 +883,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     }
     if (solve && !flagged) {
       if (planned && vals_smem) {
-        copy_vals<T>(vals, vals_g, ep.nv);
+        copy_vals<T>(vals, vals_g, ep.n_solve);
         __syncthreads();
       }
       be_back_solve<T>(A, dp, z, bsum);  // core part of y0
@@ -928,7 +958,7 @@ __global__ void __launch_bounds__(kThreads)
     if (!(draw_flags[i] & DRAW_FLAG_PIVOT)) continue;
     build_full<T>(m, P, mp, n, i, sp, theta, A);
     if (solve) {
-      forecast_rhs<T>(m, P, n, i, sp, theta, x, lambda, key, nu);
+      forecast_rhs<T>(m, P, n, i, rows, theta, x, lambda, key, nu);
       __syncthreads();
       for (int r = tid; r < mp; r += blockDim.x) z[r] = (r < m) ? (T)nu[r] : T(0);
     }

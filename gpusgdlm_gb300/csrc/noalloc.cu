@@ -96,7 +96,7 @@ extern "C" int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const flo
   if (cudaMemsetAsync(d_flags, 0, n * sizeof(int), s) != cudaSuccess)
     return reject(SGDLM_ERR_DEVICE, "cannot clear the flag array");
   const RngKey no_key{0, 0, 0, nullptr};
-  const GammaRows no_rows{nullptr, nullptr};
+  const GammaRows no_rows{nullptr, nullptr, nullptr, nullptr};
   EliminationPlan no_plan{};
   no_plan.m = (int)m;
   no_plan.P = (int)max_p;

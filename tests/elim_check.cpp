@@ -12,8 +12,8 @@ extern "C" int elim_check(int m, int P, const unsigned *sp, const double *theta_
   const sgdlm::EliminationPlanHost pl = sgdlm::plan_elimination(m, P, spv, max_levels);
   std::vector<double> v(pl.nv, 0.0);
   v[sgdlm::kSlotOne] = 1.0;
-  for (int r = 0; r < m; ++r) v[sgdlm::kSlotDiag0 + r] = 1.0;
-  for (size_t k = 0; k < pl.l0_e.size(); ++k) v[sgdlm::kSlotDiag0 + m + k] = -theta_e[pl.l0_e[k]];
+  for (int r = 0; r < m; ++r) v[pl.diag_slot[r]] = 1.0;
+  for (size_t k = 0; k < pl.l0_e.size(); ++k) v[pl.l0_slot[k]] = -theta_e[pl.l0_e[k]];
   auto lo = [](unsigned w) { return (int)(w & 0xFFFFu); };
   auto hi = [](unsigned w) { return (int)(w >> 16); };
   double ld = 0.0;
@@ -84,8 +84,14 @@ extern "C" int elim_check(int m, int P, const unsigned *sp, const double *theta_
       y[pl.bwd_node[g]] = acc / v[pl.bwd_diag[g]];
     }
   for (int r = 0; r < m; ++r) sol[r] = y[r];
+  // the solve programs read only the prefix [0, n_solve) of the slots
+  bool prefix_ok = true;
+  for (unsigned f : pl.fwd) prefix_ok &= (int)lo(f) < pl.n_solve;
+  for (unsigned b : pl.bwd) prefix_ok &= (int)lo(b) < pl.n_solve;
+  for (int d : pl.bwd_diag) prefix_ok &= d < pl.n_solve;
+  if (!prefix_ok) info[1] = -1;
   info[0] = ld;
-  info[1] = n;
+  if (info[1] != -1) info[1] = n;
   info[2] = pl.nlev;
   info[3] = (double)pl.n_terms;
   return 0;

@@ -63,6 +63,7 @@ def test_plan_reproduces_dense_logdet_and_solve(elim, m, kmax, seed, levels):
     info, sol = run(elim, sp, theta, levels, rhs)
     A = full_matrix(sp, theta)
     sign, ld = np.linalg.slogdet(A)
+    assert info[1] >= 1  # -1: a solve program reads a slot outside the solve prefix
     np.testing.assert_allclose(info[0], ld, rtol=1e-10, atol=1e-11)
     np.testing.assert_allclose(sol, np.linalg.solve(A, rhs), rtol=1e-9, atol=1e-11)
     if levels == 0:
