@@ -98,7 +98,7 @@ struct sgdlm_engine {
   DevBuf<float> U32;
   std::vector<unsigned> h_p, h_sp;
   // simulation
-  DevBuf<unsigned char> lambda, theta, lu_scratch;
+  DevBuf<unsigned char> lambda, theta, theta_dm, lu_scratch;
   DevBuf<double> logdet, w, y_fc, stats6, part_a, part_b;
   DevBuf<int> draw_flags, series_flags;
   DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
@@ -341,6 +341,7 @@ int alloc_state(sgdlm_engine *h) {
 void release_sim(sgdlm_engine *h) {
   h->lambda.release();
   h->theta.release();
+  h->theta_dm.release();
   h->lu_scratch.release();
   h->logdet.release();
   h->w.release();
@@ -402,6 +403,7 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   h->chunks = (int)vb_chunks((long)nsim);
   CK(h->lambda.alloc(m * nsim * ts));
   CK(h->theta.alloc(m * nsim * P * ts));
+  CK(h->theta_dm.alloc(m * nsim * P * ts));
   CK(h->lu_scratch.alloc(pl.scratch_elems_total * ts));
   CK(h->logdet.alloc(nsim));
   CK(h->w.alloc(nsim));
@@ -463,7 +465,7 @@ void sample_draws(sgdlm_engine *h, const double *m_t, const double *C_t, const d
   const T *U = std::is_same<T, float>::value ? reinterpret_cast<const T *>(h->U32.ptr)
                                               : reinterpret_cast<const T *>(h->U64.ptr);
   launch_sample<T>(h->stream, m, P, n, m_t, n_t, s_t, U, key, as<T>(h->lambda), as<T>(h->theta),
-                   h->draw_flags.ptr);
+                   as<T>(h->theta_dm), h->draw_flags.ptr);
   h->launches += 2;
 }
 
@@ -473,10 +475,10 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   const bool refine = (h->precision != SGDLM_PRECISION_FP64);
   const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr, h->g_extptr.ptr, h->g_extk.ptr};
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
-               as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
+               as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
                refine, y, rows);
   launch_lu_fallback<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta),
-                        as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
+                        as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
                         as<T>(h->lambda), key, y, rows);
   h->launches += 2;
 }
@@ -614,7 +616,7 @@ template <typename T> int evolve(sgdlm_engine *h) {
   launch_evolve<T>(h->stream, m, P, n, h->p.ptr, h->fn_t.ptr, h->fs_t.ptr, h->beta.ptr, UW,
                    key, (h->compat & SGDLM_COMPAT_UNSCALED_EVOLUTION) != 0,
                    (h->compat & SGDLM_COMPAT_BETA_NO_BOOST) != 0, as<T>(h->lambda),
-                   as<T>(h->theta), h->draw_flags.ptr);
+                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr);
   h->launches += 2;
   return sync(h);
 }

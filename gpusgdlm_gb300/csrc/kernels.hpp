@@ -58,14 +58,15 @@ void launch_cholesky(cudaStream_t s, int m, int P, const unsigned *p, const doub
 template <typename T>
 void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                    const double *n_t, const double *s_t, const T *U, RngKey key,
-                   T *lambda, T *theta, int *draw_flags);
+                   T *lambda, T *theta, T *theta_dm, int *draw_flags);
 
 // (a9) multi-step evolution of forecast draws.  rSGDLM/src/SGDLM/SGDLM.cu:679-762
 template <typename T>
 void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
                    const double *r_t, const double *c_t, const double *beta,
                    const T *UW, RngKey key, bool compat_unscaled_omega,
-                   bool compat_beta_no_boost, T *lambda, T *theta, int *draw_flags);
+                   bool compat_beta_no_boost, T *lambda, T *theta, T *theta_dm,
+                   int *draw_flags);
 
 // (a4)/(a8) batched LU of (I - Gamma_i): log|det| per draw, and optionally the
 // forecast solve y_i = (I - Gamma_i)^-1 nu_i with one refinement step.
@@ -95,14 +96,16 @@ struct GammaRows {
 };
 struct EliminationPlan;
 template <typename T>
+// theta: the draws series-major; theta_dm: their draw-major copy, or nullptr.
 void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan &ep,
-               const unsigned *sp, const T *theta, T *scratch, double *logdet, int *draw_flags,
+               const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
+               double *logdet, int *draw_flags,
                // forecast solve (x == nullptr: log|det| only)
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
                GammaRows rows);
 template <typename T>
 void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n,
-                        const unsigned *sp, const T *theta, T *scratch,
+                        const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
                         double *logdet, int *draw_flags, const double *x,
                         const T *lambda, RngKey key, double *y, GammaRows rows);
 

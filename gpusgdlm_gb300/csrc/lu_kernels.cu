@@ -145,11 +145,26 @@ struct FallbackSmem {
   }
 };
 
+// The draws' theta, series-major (theta[(j*n + i)*P + k], the sampler's layout)
+// and, when present, the draw-major copy theta_dm[(i*m + j)*P + k] in which one
+// draw's values are one contiguous row; the LU kernels read the latter.
+template <typename T> struct Theta {
+  const T *sm, *dm;
+  int m, P;
+  long n;
+  __device__ __forceinline__ T at(long i, int e) const {  // e = j*P + k
+    return dm ? dm[(size_t)i * m * P + e] : sm[((size_t)(e / P) * n + i) * P + e % P];
+  }
+  __device__ __forceinline__ const T *row(long i, int j) const {
+    return dm ? dm + ((size_t)i * m + j) * P : sm + ((size_t)j * n + i) * P;
+  }
+};
+
 // nu_j = z/sqrt(lambda) + sum over external predictors x_jk theta_jk for draw i
 // (batchedComputeNuPlusMu, kernel_functions.cuh:1156-1178), into nu (double).
 template <typename T>
-__device__ void forecast_rhs(int m, int P, long n, long i, GammaRows rows,
-                             const T *__restrict__ theta, const double *__restrict__ x,
+__device__ void forecast_rhs(int m, int P, long n, long i, GammaRows rows, Theta<T> theta,
+                             const double *__restrict__ x,
                              const T *__restrict__ lambda, RngKey key, double *nu) {
   const uint32_t ep = key_epoch(key);
   for (int j = threadIdx.x; j < m; j += blockDim.x) {
@@ -158,7 +173,7 @@ __device__ void forecast_rhs(int m, int P, long n, long i, GammaRows rows,
     box_muller<T>(g.x, g.y, z0, z1);
     const T lam = lambda[(size_t)j * n + i];
     double v = (double)(z0 / dev_sqrt(lam));
-    const T *th = theta + ((size_t)j * n + i) * P;
+    const T *th = theta.row(i, j);
     for (int q = rows.ext_ptr[j]; q < rows.ext_ptr[j + 1]; ++q) {
       const int k = rows.ext_k[q];
       v += x[(size_t)j * P + k] * (double)th[k];
@@ -171,7 +186,7 @@ __device__ void forecast_rhs(int m, int P, long n, long i, GammaRows rows,
 // mp x mp matrix A (fillGammas, kernel_functions.cuh:822-842).
 template <typename T>
 __device__ void build_full(int m, int P, int mp, long n, long i, const unsigned *__restrict__ sp,
-                           const T *__restrict__ theta, T *__restrict__ A) {
+                           Theta<T> theta, T *__restrict__ A) {
   const int tid = threadIdx.x;
   const size_t n16 = (size_t)mp * mp * sizeof(T) / 16;
   uint4 *A16 = reinterpret_cast<uint4 *>(A);
@@ -182,9 +197,8 @@ __device__ void build_full(int m, int P, int mp, long n, long i, const unsigned 
   for (int e = tid; e < m * P; e += blockDim.x) {
     const unsigned pos = sp[e];
     if ((size_t)pos < mm) {
-      const int j = e / P, k = e % P;
       const int row = (int)(pos % (unsigned)m), col = (int)(pos / (unsigned)m);
-      A[row + (size_t)mp * col] = -theta[((size_t)j * n + i) * P + k];
+      A[row + (size_t)mp * col] = -theta.at(i, e);
     }
   }
   __syncthreads();
@@ -595,8 +609,8 @@ __device__ void levels_backward(const EliminationPlan &ep, const T *vals, const 
 // entries in a fixed order (deterministic); the entries' indices and theta values
 // are gathered eight at a time so that their loads overlap.
 template <typename T>
-__device__ void residual(int m, int P, long n, long i, GammaRows rows,
-                         const T *__restrict__ theta, const double *nu, const T *y, double *res) {
+__device__ void residual(int m, int P, long n, long i, GammaRows rows, Theta<T> theta,
+                         const double *nu, const T *y, double *res) {
   for (int r = threadIdx.x; r < m; r += blockDim.x) {
     double v = nu[r] - (double)y[r];
     const int q1 = rows.rowptr[r + 1];
@@ -607,7 +621,7 @@ __device__ void residual(int m, int P, long n, long i, GammaRows rows,
       T th[8];
 #pragma unroll
       for (int h = 0; h < 8; ++h)
-        th[h] = ec[h].x >= 0 ? theta[((size_t)(ec[h].x / P) * n + i) * P + ec[h].x % P] : T(0);
+        th[h] = ec[h].x >= 0 ? theta.at(i, ec[h].x) : T(0);
 #pragma unroll
       for (int h = 0; h < 8; ++h)
         if (ec[h].x >= 0) v += (double)th[h] * (double)y[ec[h].y];
@@ -633,13 +647,15 @@ __device__ __forceinline__ void copy_vals(T *__restrict__ dst, const T *__restri
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, long n, EliminationPlan ep,
-         const unsigned *__restrict__ sp, const T *__restrict__ theta, T *__restrict__ scratch,
+         const unsigned *__restrict__ sp, const T *__restrict__ theta_sm,
+         const T *__restrict__ theta_dm, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
          const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
          double *__restrict__ y, GammaRows rows) {
   using V = Vec<T>;
   constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Theta<T> theta{theta_sm, theta_dm, m, P, n};
   const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0);
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);  // D^-1, row-major, stride kB
   T *prow = reinterpret_cast<T *>(smem_raw + L.off_prow);
@@ -687,7 +703,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
           th[h] = T(0);
-          if (e[h] >= 0) th[h] = theta[((size_t)(e[h] / P) * n + i) * P + e[h] % P];
+          if (e[h] >= 0) th[h] = theta.at(i, e[h]);
         }
 #pragma unroll
         for (int h = 0; h < 4; ++h)
@@ -927,13 +943,15 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_lu_fallback(int m, int P, int mp, long n, const unsigned *__restrict__ sp,
-                  const T *__restrict__ theta, T *__restrict__ scratch,
+                  const T *__restrict__ theta_sm, const T *__restrict__ theta_dm,
+                  T *__restrict__ scratch,
                   double *__restrict__ logdet, int *__restrict__ draw_flags,
                   const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
                   double *__restrict__ y, GammaRows rows) {
   using V = Vec<T>;
   constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const Theta<T> theta{theta_sm, theta_dm, m, P, n};
   const FallbackSmem L(mp, m, sizeof(T));
   T *pan = reinterpret_cast<T *>(smem_raw + L.off_pan);            // pan[c * mp + r]
   T *Uc = reinterpret_cast<T *>(smem_raw + L.off_U);               // U12 chunk [t][kUs]
@@ -1172,7 +1190,8 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv) {
 
 template <typename T>
 void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &ep,
-               const unsigned *sp, const T *theta, T *scratch, double *logdet, int *draw_flags,
+               const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
+               double *logdet, int *draw_flags,
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
                GammaRows rows) {
   // opt in to exactly the shared memory this plan needs (a failure here shows up
@@ -1180,36 +1199,43 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
   if (pl.smem > 48 * 1024)
     cudaFuncSetAttribute(k_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
   k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
-                                             pl.vals_smem, n, ep, sp, theta, scratch, logdet,
+                                             pl.vals_smem, n, ep, sp, theta, theta_dm, scratch,
+                                             logdet,
                                              draw_flags, x, lambda, key, refine, y, rows);
 }
 
 template <typename T>
 void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const unsigned *sp,
-                        const T *theta, T *scratch, double *logdet, int *draw_flags,
+                        const T *theta, const T *theta_dm, T *scratch, double *logdet,
+                        int *draw_flags,
                         const double *x, const T *lambda, RngKey key, double *y,
                         GammaRows rows) {
   if (pl.smem_fallback > 48 * 1024)
     cudaFuncSetAttribute(k_lu_fallback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)pl.smem_fallback);
   k_lu_fallback<T><<<pl.fb_grid, pl.block, pl.smem_fallback, s>>>(
-      pl.m, pl.P, pl.mp, n, sp, theta, scratch, logdet, draw_flags, x, lambda, key, y, rows);
+      pl.m, pl.P, pl.mp, n, sp, theta, theta_dm, scratch, logdet, draw_flags, x, lambda, key, y,
+      rows);
 }
 
 template LuPlan plan_lu<float>(int, int, long, int, int, int);
 template LuPlan plan_lu<double>(int, int, long, int, int, int);
 template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
-                               const unsigned *, const float *, float *, double *, int *,
+                               const unsigned *, const float *, const float *, float *,
+                               double *, int *,
                                const double *, const float *, RngKey, bool, double *, GammaRows);
 template void launch_lu<double>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
-                                const unsigned *, const double *, double *, double *, int *,
+                                const unsigned *, const double *, const double *, double *,
+                                double *, int *,
                                 const double *, const double *, RngKey, bool, double *,
                                 GammaRows);
 template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long, const unsigned *,
-                                        const float *, float *, double *, int *, const double *,
+                                        const float *, const float *, float *, double *, int *,
+                                        const double *,
                                         const float *, RngKey, double *, GammaRows);
 template void launch_lu_fallback<double>(cudaStream_t, const LuPlan &, long, const unsigned *,
-                                         const double *, double *, double *, int *,
+                                         const double *, const double *, double *, double *,
+                                         int *,
                                          const double *, const double *, RngKey, double *,
                                          GammaRows);
 

@@ -17,12 +17,32 @@ namespace {
 
 constexpr int kSampleThreads = 128;
 
+// Writes draw i's row of series j (P values) into the draw-major copy
+// theta_dm[(i*m + j)*P + k] used by the LU kernels (one contiguous row per draw),
+// with 16-byte stores when the rows are 16-byte aligned.
+template <typename T>
+__device__ __forceinline__ void write_draw_major(T *__restrict__ theta_dm, int m, int P, long i,
+                                                 int j, const T *row) {
+  T *dst = theta_dm + ((size_t)i * m + j) * P;
+  if ((P * sizeof(T)) % 16 == 0) {
+    for (int k = 0; k < P; k += (int)(16 / sizeof(T))) {
+      if (sizeof(T) == 4)
+        *reinterpret_cast<float4 *>(dst + k) =
+            make_float4((float)row[k], (float)row[k + 1], (float)row[k + 2], (float)row[k + 3]);
+      else
+        *reinterpret_cast<double2 *>(dst + k) = make_double2((double)row[k], (double)row[k + 1]);
+    }
+  } else {
+    for (int k = 0; k < P; ++k) dst[k] = row[k];
+  }
+}
+
 template <typename T, int PMAX>
 __global__ void __launch_bounds__(kSampleThreads)
     k_sample(int m, int P, long n, const double *__restrict__ m_t,
              const double *__restrict__ n_t, const double *__restrict__ s_t,
              const T *__restrict__ U, RngKey key, T *__restrict__ lambda,
-             T *__restrict__ theta, int *__restrict__ draw_flags) {
+             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Us = reinterpret_cast<T *>(smem_raw);  // P*P, U[row + P*col]
   T *ms = Us + P * P;                       // P
@@ -65,6 +85,7 @@ __global__ void __launch_bounds__(kSampleThreads)
       }
     }
     lambda[(size_t)j * n + i] = lam;
+    if (theta_dm) write_draw_major<T>(theta_dm, m, P, i, j, row);
     if (fail) atomicOr(&draw_flags[i], DRAW_FLAG_GAMMA_CAP);
   }
   __syncthreads();
@@ -83,7 +104,7 @@ __global__ void __launch_bounds__(kSampleThreads)
              const double *__restrict__ r_t, const double *__restrict__ c_t,
              const double *__restrict__ beta, const T *__restrict__ UW, RngKey key,
              bool compat_unscaled, bool compat_no_boost, T *__restrict__ lambda,
-             T *__restrict__ theta, int *__restrict__ draw_flags) {
+             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Us = reinterpret_cast<T *>(smem_raw);
   T *stage = Us + P * P;
@@ -141,6 +162,7 @@ __global__ void __launch_bounds__(kSampleThreads)
         row[k] = acc + row[k];
       }
     }
+    if (theta_dm) write_draw_major<T>(theta_dm, m, P, i, j, row);
     if (fail) atomicOr(&draw_flags[i], DRAW_FLAG_GAMMA_CAP);
   }
   __syncthreads();
@@ -156,7 +178,7 @@ template <typename T> size_t sample_smem(int P) {
 template <typename T>
 void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                    const double *n_t, const double *s_t, const T *U, RngKey key,
-                   T *lambda, T *theta, int *draw_flags) {
+                   T *lambda, T *theta, T *theta_dm, int *draw_flags) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
   const size_t smem = sample_smem<T>(P);
   if (smem > 48 * 1024) {
@@ -167,23 +189,24 @@ void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
   }
   if (P <= 8)
     k_sample<T, 8><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                      lambda, theta, draw_flags);
+                                                      lambda, theta, theta_dm, draw_flags);
   else if (P <= 16)
     k_sample<T, 16><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, draw_flags);
+                                                       lambda, theta, theta_dm, draw_flags);
   else if (P <= 32)
     k_sample<T, 32><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, draw_flags);
+                                                       lambda, theta, theta_dm, draw_flags);
   else
     k_sample<T, 64><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, draw_flags);
+                                                       lambda, theta, theta_dm, draw_flags);
 }
 
 template <typename T>
 void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
                    const double *r_t, const double *c_t, const double *beta,
                    const T *UW, RngKey key, bool compat_unscaled_omega,
-                   bool compat_beta_no_boost, T *lambda, T *theta, int *draw_flags) {
+                   bool compat_beta_no_boost, T *lambda, T *theta, T *theta_dm,
+                   int *draw_flags) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
   const size_t smem = ((size_t)P * P + (size_t)kSampleThreads * P) * sizeof(T);
   if (smem > 48 * 1024) {
@@ -196,7 +219,7 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
   k_evolve<T, PM><<<grid, kSampleThreads, smem, s>>>(m, P, n, p, r_t, c_t, beta, UW, \
                                                      key, compat_unscaled_omega,      \
                                                      compat_beta_no_boost, lambda,    \
-                                                     theta, draw_flags)
+                                                     theta, theta_dm, draw_flags)
   if (P <= 8)
     SGDLM_EVOLVE(8);
   else if (P <= 16)
@@ -210,17 +233,17 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
 
 template void launch_sample<float>(cudaStream_t, int, int, long, const double *,
                                    const double *, const double *, const float *, RngKey,
-                                   float *, float *, int *);
+                                   float *, float *, float *, int *);
 template void launch_sample<double>(cudaStream_t, int, int, long, const double *,
                                     const double *, const double *, const double *,
-                                    RngKey, double *, double *, int *);
+                                    RngKey, double *, double *, double *, int *);
 template void launch_evolve<float>(cudaStream_t, int, int, long, const unsigned *,
                                    const double *, const double *, const double *,
                                    const float *, RngKey, bool, bool, float *, float *,
-                                   int *);
+                                   float *, int *);
 template void launch_evolve<double>(cudaStream_t, int, int, long, const unsigned *,
                                     const double *, const double *, const double *,
                                     const double *, RngKey, bool, bool, double *,
-                                    double *, int *);
+                                    double *, double *, int *);
 
 }  // namespace sgdlm
