@@ -85,6 +85,8 @@ SIGNATURES = {
     "sgdlm_compute_prior": [_H, _i],
     "sgdlm_init_forecast_priors": [_H],
     "sgdlm_evolve_forecast_samples": [_H],
+    "sgdlm_compute_evo_prior": [_H, _Pd, _i],
+    "sgdlm_evolve_forecast_samples_evo": [_H, _Pd],
     "sgdlm_compute_forecast": [_H, _Pd, _Pd, _Pd, _Pd, _i],
     "sgdlm_get_draws": [_H, _Pd, _Pd, _Pd],
     "sgdlm_set_precision": [_H, _i],

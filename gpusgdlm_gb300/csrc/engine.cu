@@ -87,6 +87,9 @@ struct sgdlm_engine {
   DevBuf<int> g_rowptr;
   DevBuf<int2> g_ent;
   DevBuf<int> g_extptr, g_extk;
+  // evolution matrices G (P x P x m, FP64 and the FP32 copy the draws use)
+  DevBuf<double> G_t;
+  DevBuf<float> G32;
   // sparse pre-elimination plan of (I - Gamma) (elimination.hpp)
   int elim_levels = 4;
   EliminationPlanHost eplan;
@@ -368,6 +371,8 @@ void release_all(sgdlm_engine *h) {
   h->g_ent.release();
   h->g_extptr.release();
   h->g_extk.release();
+  h->G_t.release();
+  h->G32.release();
   h->elim_buf.release();
   h->elim_dev = EliminationPlan{};
   h->series_flags.release();
@@ -603,7 +608,21 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
   return collect_flags(h, false);
 }
 
-template <typename T> int evolve(sgdlm_engine *h) {
+// Copies the evolution matrices (P x P x m, column-major per series) to the device
+// (setEvolutionMatrix, HostWrapperImpl.cu:737-754), with an FP32 copy.
+int upload_evolution_matrix(sgdlm_engine *h, const double *G) {
+  const size_t n = h->P * h->P * h->m;
+  if (h->G_t.count != n) {
+    CK(h->G_t.alloc(n));
+    CK(h->G32.alloc(n));
+  }
+  CK(cudaMemcpyAsync(h->G_t.ptr, G, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  launch_to_float(h->stream, n, h->G_t.ptr, h->G32.ptr);
+  h->launches += 1;
+  return SGDLM_OK;
+}
+
+template <typename T> int evolve(sgdlm_engine *h, bool with_G = false) {
   const int m = (int)h->m, P = (int)h->P;
   const long n = (long)h->nsim;
   const RngKey key = h->key((uint32_t)h->epoch);
@@ -616,7 +635,11 @@ template <typename T> int evolve(sgdlm_engine *h) {
   launch_evolve<T>(h->stream, m, P, n, h->p.ptr, h->fn_t.ptr, h->fs_t.ptr, h->beta.ptr, UW,
                    key, (h->compat & SGDLM_COMPAT_UNSCALED_EVOLUTION) != 0,
                    (h->compat & SGDLM_COMPAT_BETA_NO_BOOST) != 0, as<T>(h->lambda),
-                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr);
+                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr,
+                   with_G ? (std::is_same<T, float>::value
+                                 ? reinterpret_cast<const T *>(h->G32.ptr)
+                                 : reinterpret_cast<const T *>(h->G_t.ptr))
+                          : nullptr);
   h->launches += 2;
   return sync(h);
 }
@@ -969,6 +992,36 @@ int sgdlm_compute_prior(sgdlm_handle h, int evolve_forecast_variables) {
   if (st) return st;
   h->is_prior = true;
   return SGDLM_OK;
+}
+
+int sgdlm_compute_evo_prior(sgdlm_handle h, const double *G_tp1, int evolve_forecast_variables) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!G_tp1) return h->fail(SGDLM_ERR_BAD_ARG, "null evolution matrix");
+  if (!evolve_forecast_variables && !h->check_prior(false)) return SGDLM_ERR_WRONG_STATE;
+  int st = upload_evolution_matrix(h, G_tp1);
+  if (st) return st;
+  const int m = (int)h->m, P = (int)h->P;
+  double *m_t = evolve_forecast_variables ? h->fm_t.ptr : h->m_t.ptr;
+  double *C_t = evolve_forecast_variables ? h->fC_t.ptr : h->C_t.ptr;
+  double *n_t = evolve_forecast_variables ? h->fn_t.ptr : h->n_t.ptr;
+  double *W_t = evolve_forecast_variables ? h->fW_t.ptr : h->W_t.ptr;
+  launch_prior(h->stream, m, P, h->p.ptr, C_t, n_t, W_t, h->beta.ptr, h->delta.ptr);
+  launch_evo_prior(h->stream, m, P, h->p.ptr, m_t, C_t, h->G_t.ptr);
+  h->launches += 2;
+  if ((st = sync(h))) return st;
+  if (!evolve_forecast_variables) h->is_prior = true;
+  return SGDLM_OK;
+}
+
+int sgdlm_evolve_forecast_samples_evo(sgdlm_handle h, const double *G_tp1) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+  if (!G_tp1) return h->fail(SGDLM_ERR_BAD_ARG, "null evolution matrix");
+  int st = upload_evolution_matrix(h, G_tp1);
+  if (st) return st;
+  return h->precision == SGDLM_PRECISION_FP64 ? evolve<double>(h, true) : evolve<float>(h, true);
 }
 
 int sgdlm_init_forecast_priors(sgdlm_handle h) {

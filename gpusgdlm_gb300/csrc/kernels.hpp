@@ -50,6 +50,11 @@ void launch_prior(cudaStream_t s, int m, int P, const unsigned *p, double *C_t,
 
 // Upper Cholesky factor U (U'U = C) of the leading p x p block, zero elsewhere,
 // in double and in the sampling precision.  rSGDLM/src/kernel_functions.cuh:845-902
+// Evolution-matrix step of the prior: a = G m, R = G R G' with the reference's
+// cut-offs (rSGDLM/src/SGDLM/SGDLM.cu:151-178).
+void launch_evo_prior(cudaStream_t s, int m, int P, const unsigned *p, double *m_t,
+                      double *C_t, const double *G);
+void launch_to_float(cudaStream_t s, size_t n, const double *src, float *dst);
 void launch_cholesky(cudaStream_t s, int m, int P, const unsigned *p, const double *C,
                      double *U64, float *U32);
 
@@ -66,7 +71,7 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
                    const double *r_t, const double *c_t, const double *beta,
                    const T *UW, RngKey key, bool compat_unscaled_omega,
                    bool compat_beta_no_boost, T *lambda, T *theta, T *theta_dm,
-                   int *draw_flags);
+                   int *draw_flags, const T *G = nullptr);
 
 // (a4)/(a8) batched LU of (I - Gamma_i): log|det| per draw, and optionally the
 // forecast solve y_i = (I - Gamma_i)^-1 nu_i with one refinement step.

@@ -104,15 +104,19 @@ __global__ void __launch_bounds__(kSampleThreads)
              const double *__restrict__ r_t, const double *__restrict__ c_t,
              const double *__restrict__ beta, const T *__restrict__ UW, RngKey key,
              bool compat_unscaled, bool compat_no_boost, T *__restrict__ lambda,
-             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags) {
+             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags,
+             const T *__restrict__ G) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Us = reinterpret_cast<T *>(smem_raw);
-  T *stage = Us + P * P;
+  T *Gs = Us + P * P;  // G_j when an evolution matrix is given
+  T *stage = Gs + (G ? P * P : 0);
   const int j = blockIdx.y;
   const long i0 = (long)blockIdx.x * blockDim.x;
   const long cnt = (long)min((long)blockDim.x, n - i0) * P;
   T *src = theta + ((size_t)j * n + i0) * P;
   for (int e = threadIdx.x; e < P * P; e += blockDim.x) Us[e] = UW[(size_t)j * P * P + e];
+  if (G)
+    for (int e = threadIdx.x; e < P * P; e += blockDim.x) Gs[e] = G[(size_t)j * P * P + e];
   for (long e = threadIdx.x; e < cnt; e += blockDim.x) stage[e] = src[e];
   __syncthreads();
   const long i = i0 + threadIdx.x;
@@ -153,6 +157,20 @@ __global__ void __launch_bounds__(kSampleThreads)
       for (int k = 0; k < PMAX; ++k) w[k] = ((unsigned)k < pj) ? w[k] / den : T(0);
     }
     T *row = stage + (size_t)threadIdx.x * P;
+    if (G) {
+      // theta = G theta over the full max_p x max_p product (SGDLM.cu:729-740)
+      T g[PMAX];
+#pragma unroll
+      for (int k = 0; k < PMAX; ++k) {
+        T acc = T(0);
+        if (k < P)
+          for (int l = 0; l < P; ++l) acc += Gs[k + P * l] * row[l];
+        g[k] = acc;
+      }
+#pragma unroll
+      for (int k = 0; k < PMAX; ++k)
+        if (k < P) row[k] = g[k];
+    }
 #pragma unroll
     for (int k = 0; k < PMAX; ++k) {
       if (k < P) {
@@ -206,9 +224,10 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
                    const double *r_t, const double *c_t, const double *beta,
                    const T *UW, RngKey key, bool compat_unscaled_omega,
                    bool compat_beta_no_boost, T *lambda, T *theta, T *theta_dm,
-                   int *draw_flags) {
+                   int *draw_flags, const T *G) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
-  const size_t smem = ((size_t)P * P + (size_t)kSampleThreads * P) * sizeof(T);
+  const size_t smem =
+      ((size_t)P * P * (G ? 2 : 1) + (size_t)kSampleThreads * P) * sizeof(T);
   if (smem > 48 * 1024) {
     cudaFuncSetAttribute(k_evolve<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_evolve<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -219,7 +238,7 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
   k_evolve<T, PM><<<grid, kSampleThreads, smem, s>>>(m, P, n, p, r_t, c_t, beta, UW, \
                                                      key, compat_unscaled_omega,      \
                                                      compat_beta_no_boost, lambda,    \
-                                                     theta, theta_dm, draw_flags)
+                                                     theta, theta_dm, draw_flags, G)
   if (P <= 8)
     SGDLM_EVOLVE(8);
   else if (P <= 16)
@@ -240,10 +259,10 @@ template void launch_sample<double>(cudaStream_t, int, int, long, const double *
 template void launch_evolve<float>(cudaStream_t, int, int, long, const unsigned *,
                                    const double *, const double *, const double *,
                                    const float *, RngKey, bool, bool, float *, float *,
-                                   float *, int *);
+                                   float *, int *, const float *);
 template void launch_evolve<double>(cudaStream_t, int, int, long, const unsigned *,
                                     const double *, const double *, const double *,
                                     const double *, RngKey, bool, bool, double *,
-                                    double *, double *, int *);
+                                    double *, double *, int *, const double *);
 
 }  // namespace sgdlm

@@ -171,6 +171,53 @@ __global__ void k_gate(int m, int P, const double *__restrict__ stats, double th
 
 __global__ void k_advance_epoch(uint32_t *dev_epoch, uint32_t delta) { *dev_epoch += delta; }
 
+// Evolution-matrix step of the prior (compute_one_step_ahead_prior with G_t,
+// SGDLM.cu:151-178): a = G m with the entries >= p zeroed, then R = (G R) G' with
+// the entries whose row AND column are >= p zeroed (the cut-offs of
+// kernel_functions.cuh:86-110).  One block per series; G, R and G R in shared
+// memory; FP64.
+__global__ void k_evo_prior(int m, int P, const unsigned *__restrict__ p,
+                            double *__restrict__ m_t, double *__restrict__ C_t,
+                            const double *__restrict__ G) {
+  extern __shared__ double sh[];
+  const size_t PP = (size_t)P * P;
+  const int j = blockIdx.x;
+  double *Gs = sh, *Rs = Gs + PP, *Ts = Rs + PP, *ms = Ts + PP;
+  const double *Gj = G + (size_t)j * PP;
+  double *Cj = C_t + (size_t)j * PP;
+  for (int e = threadIdx.x; e < (int)PP; e += blockDim.x) {
+    Gs[e] = Gj[e];
+    Rs[e] = Cj[e];
+  }
+  for (int e = threadIdx.x; e < P; e += blockDim.x) ms[e] = m_t[(size_t)j * P + e];
+  __syncthreads();
+  const unsigned pj = p[j];
+  for (int e = threadIdx.x; e < (int)PP; e += blockDim.x) {  // T = G R
+    const int r = e % P, c = e / P;
+    double acc = 0.0;
+    for (int l = 0; l < P; ++l) acc += Gs[r + P * l] * Rs[l + P * c];
+    Ts[e] = acc;
+  }
+  for (int r = threadIdx.x; r < P; r += blockDim.x) {  // a = G m
+    double acc = 0.0;
+    for (int l = 0; l < P; ++l) acc += Gs[r + P * l] * ms[l];
+    m_t[(size_t)j * P + r] = ((unsigned)r < pj) ? acc : 0.0;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < (int)PP; e += blockDim.x) {  // R = T G'
+    const int r = e % P, c = e / P;
+    double acc = 0.0;
+    for (int l = 0; l < P; ++l) acc += Ts[r + P * l] * Gs[c + P * l];
+    Cj[e] = ((unsigned)r >= pj && (unsigned)c >= pj) ? 0.0 : acc;
+  }
+}
+
+// Converts a double array to the working precision of the draws.
+__global__ void k_to_float(size_t n, const double *__restrict__ src, float *__restrict__ dst) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) dst[e] = (float)src[e];
+}
+
 }  // namespace
 
 void launch_advance_epoch(cudaStream_t s, uint32_t *dev_epoch, uint32_t delta) {
@@ -192,6 +239,18 @@ void launch_prior(cudaStream_t s, int m, int P, const unsigned *p, double *C_t,
   const int bs = 256;
   k_prior<<<(unsigned)((total + bs - 1) / bs), bs, 0, s>>>(m, P, p, C_t, n_t, W_t, beta,
                                                             delta);
+}
+
+void launch_evo_prior(cudaStream_t s, int m, int P, const unsigned *p, double *m_t,
+                      double *C_t, const double *G) {
+  const size_t smem = (3 * (size_t)P * P + P) * sizeof(double);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(k_evo_prior, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_evo_prior<<<m, 128, smem, s>>>(m, P, p, m_t, C_t, G);
+}
+
+void launch_to_float(cudaStream_t s, size_t n, const double *src, float *dst) {
+  k_to_float<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, src, dst);
 }
 
 void launch_cholesky(cudaStream_t s, int m, int P, const unsigned *p, const double *C,

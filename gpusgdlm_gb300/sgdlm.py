@@ -251,8 +251,44 @@ class SGDLM:
         self._check(self._lib.sgdlm_compute_prior(self._h, 0))
         return None
 
-    def _forecast(self, nsim, nsim_batch, F_tp1, debug: bool):
-        """RcppWrapper.cpp:411-479 (and :481-574 for the debug variant)."""
+    def computeEvoPrior(self, G_tp1):
+        """RcppWrapper.cpp:377-409: the prior step with an evolution matrix G_tp1
+        (max_p x max_p x m): a = G m and R = G R G' after the discount."""
+        m, P = self.m, self.max_p
+        G = np.asarray(G_tp1, dtype=np.float64)
+        if G.ndim != 3:
+            return self._bad_dim("Incorrect dimension of the input arguments")
+        if G.shape != (P, P, m):
+            return self._bad_dim("Dimensions of input arguments are incompatible")
+        G = np.asfortranarray(G)
+        self._check(self._lib.sgdlm_compute_evo_prior(self._h, _pd(G), 0))
+        return None
+
+    def computeEvoForecast(self, nsim: int, nsim_batch: int, F_tp1, G_tp1):
+        """RcppWrapper.cpp:576-688: multi-step forecast whose draws evolve with the
+        evolution matrices G_tp1 (max_p x max_p x m, or x K with one matrix per
+        step; a single matrix serves every step)."""
+        m, P = self.m, self.max_p
+        F = np.asarray(F_tp1, dtype=np.float64)
+        if F.ndim not in (2, 3):
+            return self._bad_dim("Incorrect dimension of the input arguments")
+        if F.shape[0] != P or F.shape[1] != m:
+            return self._bad_dim("Dimensions of input arguments are incompatible")
+        K = 1 if F.ndim == 2 else F.shape[2]
+        G = np.asarray(G_tp1, dtype=np.float64)
+        if G.ndim not in (3, 4):
+            return self._bad_dim("Incorrect dimension of the input arguments")
+        KG = 1 if G.ndim == 3 else G.shape[3]
+        if KG > 1 and KG != K:
+            return self._bad_dim("Dimensions of input arguments are incompatible")
+        if G.shape[0] != P or G.shape[1] != P or G.shape[2] != m:
+            return self._bad_dim("Dimensions of input arguments are incompatible")
+        G4 = np.asfortranarray(G.reshape(P, P, m, KG, order="F"))
+        return self._forecast(nsim, nsim_batch, F_tp1, debug=False, G4=G4)
+
+    def _forecast(self, nsim, nsim_batch, F_tp1, debug: bool, G4=None):
+        """RcppWrapper.cpp:411-479 (and :481-574 for the debug variant; :576-688 with
+        evolution matrices G4, max_p x max_p x m x KG)."""
         m, P = self.m, self.max_p
         F = np.asarray(F_tp1, dtype=np.float64)
         if F.ndim not in (2, 3):
@@ -270,7 +306,11 @@ class SGDLM:
         if not self._check(self._lib.sgdlm_init_forecast_priors(self._h)):
             return None
         for k in range(K):
-            if k > 0 and not self._check(self._lib.sgdlm_evolve_forecast_samples(self._h)):
+            if k > 0 and G4 is not None:
+                Gk = np.asfortranarray(G4[:, :, :, k if G4.shape[3] > 1 else 0])
+                if not self._check(self._lib.sgdlm_evolve_forecast_samples_evo(self._h, _pd(Gk))):
+                    return None
+            elif k > 0 and not self._check(self._lib.sgdlm_evolve_forecast_samples(self._h)):
                 return None
             xk = np.asfortranarray(F3[:, :, k])
             yk = np.zeros((m, n), order="F")

@@ -108,6 +108,14 @@ int sgdlm_compute_vb_posterior(sgdlm_handle h, double *mean_m_t, double *mean_C_
 int sgdlm_compute_prior(sgdlm_handle h, int evolve_forecast_variables);            /* :800 */
 int sgdlm_init_forecast_priors(sgdlm_handle h);                                    /* :540 */
 int sgdlm_evolve_forecast_samples(sgdlm_handle h);                                 /* :880 */
+/* Evolution-matrix variants (state evolution theta_t = G_t theta_{t-1} + omega_t):
+ * computePrior(const DOUBLE *G, bool) (HostWrapperImpl.cu:837-877) -- the prior
+ * step, then a = G m and R = G R G' with the reference's cut-offs; G_tp1 is
+ * max_p x max_p x m, column-major per series (R's array(…, c(max_p, max_p, m))).
+ * evolveForecastSamples(const DOUBLE *G) (HostWrapperImpl.cu:904-946) -- the
+ * evolution of forecast draws with theta = G theta before adding chol(W)' omega. */
+int sgdlm_compute_evo_prior(sgdlm_handle h, const double *G_tp1, int evolve_forecast_variables);
+int sgdlm_evolve_forecast_samples_evo(sgdlm_handle h, const double *G_tp1);
 int sgdlm_compute_forecast(sgdlm_handle h, double *y_tp1, const double *x_tp1,
                            double *lambdas, double *thetas,
                            int use_existing_lambdas_and_thetas);                   /* :949 */

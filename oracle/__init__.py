@@ -57,7 +57,9 @@ def lib():
         L.orc_weights.argtypes = [l, P_d, P_d]; L.orc_weights.restype = d
         L.orc_vb.argtypes = [i, i, P_u, P_d, P_d, l, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d]
         L.orc_forecast.argtypes = [i, i, P_u, l, P_d, P_d, P_d, u64, u64, P_d, P_d, i]
-        L.orc_evolve.argtypes = [i, i, P_u, P_d, P_d, P_d, P_d, l, u64, u64, C.c_uint, P_d, P_d, i]
+        L.orc_evolve.argtypes = [i, i, P_u, P_d, P_d, P_d, P_d, P_d, l, u64, u64, C.c_uint, P_d,
+                                 P_d, i]
+        L.orc_evo_prior.argtypes = [i, i, P_u, P_d, P_d, P_d, P_d, P_d, P_d, P_d]
         L.orc_evolve.restype = l
         _lib = L
     return _lib
@@ -164,10 +166,23 @@ def forecast(sp, lam, theta, x, seed, epoch, nthreads=0):
     return y, ld
 
 
-def evolve(p, W_t, r_t, c_t, beta, lam, theta, seed, epoch, compat, nthreads=0):
+def evolve(p, W_t, r_t, c_t, beta, lam, theta, seed, epoch, compat, nthreads=0, G=None):
     P, n, m = theta.shape
     p, W_t, r_t, c_t, beta = u32(p), f64(W_t), f64(r_t), f64(c_t), f64(beta)
     lam, theta = f64(lam), f64(theta)
-    capped = lib().orc_evolve(m, P, _u(p), _d(W_t), _d(r_t), _d(c_t), _d(beta), n, seed, epoch,
-                              compat, _d(lam), _d(theta), nthreads)
+    Gp = None if G is None else f64(G)
+    capped = lib().orc_evolve(m, P, _u(p), _d(W_t), _d(r_t), _d(c_t), _d(beta),
+                              None if Gp is None else _d(Gp), n, seed, epoch, compat, _d(lam),
+                              _d(theta), nthreads)
     return lam, theta, capped
+
+
+def evo_prior(p, m_t, C_t, n_t, beta, delta, G):
+    """compute_one_step_ahead_prior with an evolution matrix: (a, R, r, W)."""
+    P, _, m = C_t.shape
+    p, m_t, C_t, n_t = u32(p), f64(m_t), f64(C_t), f64(n_t)
+    beta, delta, G = f64(beta), f64(delta), f64(G)
+    W_t = f64(np.zeros_like(C_t))
+    lib().orc_evo_prior(m, P, _u(p), _d(m_t), _d(C_t), _d(n_t), _d(W_t), _d(beta), _d(delta),
+                        _d(G))
+    return m_t, C_t, n_t, W_t

@@ -426,4 +426,62 @@ void ref_evolve_theta(int m, int P, const unsigned *p, const double *W_t, const 
       }
 }
 
+// compute_one_step_ahead_prior with an evolution matrix, SGDLM.cu:116-178: r = beta n,
+// R = C / Delta and W = R - C inside p x p (batchedMatrixScaleWithDiff), then
+// a = G m (gemmBatched, as loops) cut at p (batchedCutOffVector), C_buffer = G R,
+// R = C_buffer G' (gemmBatched, as loops), batchedCutOffMatrix with the launch
+// shape of SGDLM.cu:170-175.
+void ref_evo_prior(int m, int P, const unsigned *p, double *m_t, double *C_t, double *n_t,
+                   double *W_t, const double *beta, const double *delta, const double *G) {
+  ref_prior(m, P, p, C_t, n_t, W_t, beta, delta);
+  const size_t PP = (size_t)P * P;
+  std::vector<double> mbuf(m_t, m_t + (size_t)m * P), Cbuf(PP * m);
+  for (int j = 0; j < m; ++j)
+    for (int r = 0; r < P; ++r) {
+      double acc = 0.0;
+      for (int l = 0; l < P; ++l) acc += G[j * PP + r + (size_t)P * l] * mbuf[(size_t)j * P + l];
+      m_t[(size_t)j * P + r] = acc;
+    }
+  auto mp = ptrs(m_t, m, P);
+  launch(dim3(cdiv(m, TPB / P), 1), dim3(TPB / P, P), false,
+         [&] { batchedCutOffVector<double>(m, P, p, mp.data()); });
+  for (int j = 0; j < m; ++j)
+    for (int c = 0; c < P; ++c)
+      for (int r = 0; r < P; ++r) {
+        double acc = 0.0;
+        for (int l = 0; l < P; ++l) acc += G[j * PP + r + (size_t)P * l] * C_t[j * PP + l + (size_t)P * c];
+        Cbuf[j * PP + r + (size_t)P * c] = acc;
+      }
+  for (int j = 0; j < m; ++j)
+    for (int c = 0; c < P; ++c)
+      for (int r = 0; r < P; ++r) {
+        double acc = 0.0;
+        for (int l = 0; l < P; ++l) acc += Cbuf[j * PP + r + (size_t)P * l] * G[j * PP + c + (size_t)P * l];
+        C_t[j * PP + r + (size_t)P * c] = acc;
+      }
+  auto Cp = ptrs(C_t, m, PP);
+  launch(dim3(cdiv(m, TPB / P), P), dim3(TPB / P, P), false,
+         [&] { batchedCutOffMatrix<double>(m, P, P, p, p, Cp.data()); });
+}
+
+// evolve_lambdas_and_thetas with an evolution matrix (SGDLM.cu:729-740): theta = G theta
+// (gemmBatched over all n*m draws, as loops) before theta += chol(W)' omega.
+void ref_evolve_theta_g(int m, int P, const unsigned *p, const double *W_t, const double *c_t,
+                        long n, const double *lambdas, const double *omegas_in, const double *G,
+                        double *thetas) {
+  const size_t PP = (size_t)P * P;
+  std::vector<double> buf(P);
+  for (long i = 0; i < n; ++i)
+    for (int j = 0; j < m; ++j) {
+      double *th = thetas + ((size_t)i * m + j) * P;
+      for (int l = 0; l < P; ++l) buf[l] = th[l];
+      for (int r = 0; r < P; ++r) {
+        double acc = 0.0;
+        for (int l = 0; l < P; ++l) acc += G[j * PP + r + (size_t)P * l] * buf[l];
+        th[r] = acc;
+      }
+    }
+  ref_evolve_theta(m, P, p, W_t, c_t, n, lambdas, omegas_in, thetas);
+}
+
 }  // extern "C"

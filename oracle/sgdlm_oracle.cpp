@@ -281,6 +281,42 @@ void orc_prior(int m, int P, const unsigned *p, double *C_t, double *n_t, double
   }
 }
 
+// compute_one_step_ahead_prior with an evolution matrix G (SGDLM.cu:116-178): the
+// prior above, then a = G m with entries >= p zeroed (batchedCutOffVector,
+// kernel_functions.cuh:86-95) and R = G R G' with the entries whose row AND column
+// are >= p zeroed (batchedCutOffMatrix :98-110).  W keeps the untransformed
+// R - C.
+void orc_evo_prior(int m, int P, const unsigned *p, double *m_t, double *C_t, double *n_t,
+                   double *W_t, const double *beta, const double *delta, const double *G) {
+  orc_prior(m, P, p, C_t, n_t, W_t, beta, delta);
+  const size_t PP = (size_t)P * P;
+  std::vector<double> mv(P), T(PP);
+  for (int j = 0; j < m; ++j) {
+    const double *Gj = G + j * PP;
+    double *mj = m_t + (size_t)j * P;
+    double *Cj = C_t + j * PP;
+    for (int l = 0; l < P; ++l) mv[l] = mj[l];
+    for (int r = 0; r < P; ++r) {
+      double acc = 0.0;
+      for (int l = 0; l < P; ++l) acc += Gj[r + (size_t)P * l] * mv[l];
+      mj[r] = ((unsigned)r < p[j]) ? acc : 0.0;
+    }
+    for (int c = 0; c < P; ++c)
+      for (int r = 0; r < P; ++r) {
+        double acc = 0.0;
+        for (int l = 0; l < P; ++l) acc += Gj[r + (size_t)P * l] * Cj[l + (size_t)P * c];
+        T[r + (size_t)P * c] = acc;
+      }
+    for (int c = 0; c < P; ++c)
+      for (int r = 0; r < P; ++r) {
+        double acc = 0.0;
+        for (int l = 0; l < P; ++l) acc += T[r + (size_t)P * l] * Gj[c + (size_t)P * l];
+        const bool cut = (unsigned)r >= p[j] && (unsigned)c >= p[j];
+        Cj[r + (size_t)P * c] = cut ? 0.0 : acc;
+      }
+  }
+}
+
 // cholesky, kernel_functions.cuh:845-902 (upper U, U'U = C; element (row, col) at
 // row + P*col).
 void orc_cholesky(int m, int P, const unsigned *p, const double *C, double *U) {
@@ -504,9 +540,11 @@ void orc_forecast(int m, int P, const unsigned *sp, long n, const double *lambda
 // lambda *= eta, omega ~ N(0,1) scaled (see compat flags), theta += chol(W)' omega.
 // compat bit 1: only draw 0 of series 0 is scaled (reference launch geometry);
 // compat bit 2: Marsaglia-Tsang without the boost for shapes below one.
+// G (P x P x m, or nullptr): theta = G theta first (SGDLM.cu:729-740, the full
+// max_p x max_p product).
 long orc_evolve(int m, int P, const unsigned *p, const double *W_t, const double *r_t,
-                const double *c_t, const double *beta, long n, uint64_t seed, uint64_t epoch,
-                unsigned compat, double *lambda, double *theta, int nthreads) {
+                const double *c_t, const double *beta, const double *G, long n, uint64_t seed,
+                uint64_t epoch, unsigned compat, double *lambda, double *theta, int nthreads) {
   const Key key = make_key(seed, epoch);
   std::vector<double> UW((size_t)P * P * m);
   orc_cholesky(m, P, p, W_t, UW.data());
@@ -533,11 +571,21 @@ long orc_evolve(int m, int P, const unsigned *p, const double *W_t, const double
         const double den = std::sqrt(c_t[j] * lam);
         for (int k = 0; k < P; ++k) om[k] = ((unsigned)k < p[j]) ? om[k] / den : 0.0;
       }
+      double *th = theta + ((size_t)j * n + i) * P;
+      if (G) {
+        const double *Gj = G + (size_t)j * P * P;
+        std::vector<double> old(th, th + P);
+        for (int k = 0; k < P; ++k) {
+          double acc = 0.0;
+          for (int l = 0; l < P; ++l) acc += Gj[k + (size_t)P * l] * old[l];
+          th[k] = acc;
+        }
+      }
       const double *U = UW.data() + (size_t)j * P * P;
       for (int k = 0; k < P; ++k) {
         double acc = 0.0;
         for (int l = 0; l <= k; ++l) acc += U[l + P * k] * om[l];
-        theta[((size_t)j * n + i) * P + k] += acc;
+        th[k] += acc;
       }
     }
   }

@@ -44,6 +44,8 @@ def ref_lib():
     L.ref_vb.argtypes = [i, i, Pu, Pu, Pd, Pd, l, Pd, Pd, Pd, Pd, Pd, Pd, Pd, Pd, Pd]
     L.ref_forecast.argtypes = [i, i, Pu, l, Pd, Pd, Pd, Pd, Pd]
     L.ref_evolve_theta.argtypes = [i, i, Pu, Pd, Pd, l, Pd, Pd, Pd]
+    L.ref_evo_prior.argtypes = [i, i, Pu, Pd, Pd, Pd, Pd, Pd, Pd, Pd]
+    L.ref_evolve_theta_g.argtypes = [i, i, Pu, Pd, Pd, l, Pd, Pd, Pd, Pd]
     return L
 
 
@@ -197,6 +199,44 @@ def case_sampling_vb_forecast(L, rng, name, p, sp, n, seed, epoch):
              thetas_ev_ref=th_ev_ref)
 
 
+def case_evolution_matrix(L, rng, name, p, sp, n, seed, epoch):
+    """computeEvoPrior (a = G m, R = G R G' with the reference's cut-offs) and the
+    evolution of forecast draws with G (theta = G theta + chol(W)' omega)."""
+    P, m = sp.shape
+    m_t, C_t, n_t, s_t = random_state(rng, m, P, p, off_block=True)
+    beta = f64(rng.uniform(0.9, 0.99, m))
+    delta = np.asfortranarray(rng.uniform(0.9, 0.999, (P, P, m)))
+    G = np.asfortranarray(np.repeat(np.eye(P)[:, :, None], m, axis=2) + rng.normal(0, 0.1, (P, P, m)))
+    a, R, r = m_t.copy(order="F"), C_t.copy(order="F"), n_t.copy()
+    W = np.zeros((P, P, m), order="F")
+    L.ref_evo_prior(m, P, U(p), D(a), D(R), D(r), D(W), D(beta), D(delta), D(G))
+    # draws of a valid posterior, evolved with G
+    m2, C2, n2, s2 = random_state(rng, m, P, p, off_block=False)
+    for j in range(m):
+        m2[p[j]:, j] = 0.0
+    lam_o, th_o, capped = oracle.sample(p, m2, C2, n2, s2, n, seed, epoch)
+    assert capped == 0
+    th_dm = np.ascontiguousarray(th_o.transpose(1, 2, 0))
+    W2 = np.zeros((P, P, m), order="F")
+    for j in range(m):
+        A = rng.normal(0, 0.05, (p[j], p[j]))
+        W2[: p[j], : p[j], j] = A @ A.T + 1e-4 * np.eye(p[j])
+    c_t = f64(rng.uniform(0.002, 0.02, m))
+    r_t = f64(rng.uniform(8, 20, m))
+    beta2 = f64(np.full(m, 0.95)); beta2[0] = 1.0
+    ev_epoch = epoch + 1
+    lam_ev, _, capped = oracle.evolve(p, W2, r_t, c_t, beta2, lam_o, th_o, seed, ev_epoch, compat=3,
+                                      G=G)
+    om = philox_normals(seed, ev_epoch, TAG_OMEGA, n, m, P)
+    th_ev_ref = th_dm.copy()
+    L.ref_evolve_theta_g(m, P, U(p), D(W2), D(c_t), n, D(np.ascontiguousarray(lam_ev)),
+                         D(np.ascontiguousarray(om)), D(G), D(th_ev_ref))
+    np.savez(OUT / f"{name}_evo.npz", p=p, sp=sp, m_t=m_t, C_t=C_t, n_t=n_t, beta=beta, delta=delta,
+             G=G, evo_a=a, evo_R=R, evo_r=r, evo_W=W, m2=m2, C2=C2, n2=n2, s2=s2, n=n, seed=seed,
+             epoch=epoch, W2=W2, c_t=c_t, r_t=r_t, beta2=beta2, ev_epoch=ev_epoch,
+             lambdas_ev=np.ascontiguousarray(lam_ev), thetas_ev_ref=th_ev_ref)
+
+
 def case_samplers(L, rng):
     """make_gamma2 and make_beta on supplied uniforms/normals (n_loops = 2)."""
     m, n, loops = 3, 1000, 2
@@ -230,6 +270,7 @@ def main():
     case_sampling_vb_forecast(L, rng, "m20", p2, sp2, n=300, seed=0xDEADBEEF12345, epoch=3)
     case_samplers(L, rng)
     case_psi(L)
+    case_evolution_matrix(L, rng, "m20", p2, sp2, n=200, seed=77, epoch=5)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

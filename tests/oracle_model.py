@@ -46,8 +46,13 @@ class OracleSGDLM:
         self.C_t, self.n_t, self.W = oracle.prior(self.p, self.C_t, self.n_t, self.beta, self.delta,
                                                   self.W)
 
-    def forecast(self, n, x):
-        """computeForecast for a P x m (one step) or P x m x K array (RcppWrapper.cpp:455-472)."""
+    def evo_prior(self, G):
+        self.m_t, self.C_t, self.n_t, self.W = oracle.evo_prior(self.p, self.m_t, self.C_t, self.n_t,
+                                                              self.beta, self.delta, G)
+
+    def forecast(self, n, x, G4=None):
+        """computeForecast for a P x m (one step) or P x m x K array (RcppWrapper.cpp:455-472);
+        with evolution matrices G4 (P x P x m x KG) computeEvoForecast (:576-688)."""
         x = np.asarray(x, dtype=np.float64)
         K = 1 if x.ndim == 2 else x.shape[2]
         x3 = x.reshape(self.P, self.m, K, order="F")
@@ -59,8 +64,9 @@ class OracleSGDLM:
                 lam, th, _ = oracle.sample(self.p, fm, fC, fn, fs, n, self.seed, self.epoch,
                                            self.nthreads)
             else:
+                G = None if G4 is None else G4[:, :, :, k if G4.shape[3] > 1 else 0]
                 lam, th, _ = oracle.evolve(self.p, fW, fn, fs, self.beta, lam, th, self.seed,
-                                           self.epoch, self.compat, self.nthreads)
+                                           self.epoch, self.compat, self.nthreads, G=G)
                 self.epoch += 1
             y, _ = oracle.forecast(self.sp, lam, th, np.asfortranarray(x3[:, :, k]), self.seed,
                                    self.epoch, self.nthreads)

@@ -157,6 +157,49 @@ def test_multistep_forecast_matches_oracle(built_lib, golden, precision, compat)
     assert s.getRngState()[1] == epoch + 5
 
 
+def test_evo_prior_matches_reference(built_lib, golden):
+    """computeEvoPrior against the reference's kernels (fixture m20_evo): a = G m and
+    R = G R G' with the reference's cut-offs, FP64."""
+    g = golden("m20_evo.npz")
+    P, m = g["sp"].shape
+    s = model_from(g, "fp64", beta=g["beta"], delta=g["delta"])
+    s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], np.ones(m))
+    s.computeEvoPrior(g["G"])
+    assert s.isPrior()
+    prm = s.getParameters()
+    np.testing.assert_array_equal(prm["n"], g["evo_r"])
+    np.testing.assert_allclose(prm["m"], g["evo_a"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(prm["C"], g["evo_R"], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_evo_forecast_matches_oracle(built_lib, golden, precision):
+    """computeEvoForecast, K = 3 steps with one evolution matrix per step: the draws
+    evolve as theta = G theta + chol(W)' omega between steps."""
+    g = golden("m20_vb_forecast.npz")
+    ge = golden("m20_evo.npz")
+    P, m = g["sp"].shape
+    n, seed, epoch = 256, 41, 2
+    x3 = np.asfortranarray(np.stack([g["x"] * (1 + 0.1 * k) for k in range(3)], axis=2))
+    G4 = np.asfortranarray(np.stack([ge["G"] * (1 - 0.05 * k) for k in range(3)], axis=3))
+    s = model_from(g, precision, seed=seed, epoch=epoch)
+    s.setCompat(0)
+    s.setPosteriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    s.computePrior()
+    y = s.computeEvoForecast(n, n, x3, G4)
+    o = OracleSGDLM(g["p"], g["sp"], np.full(m, 0.95), np.full((P, P, m), 0.97), seed=seed,
+                    epoch=epoch, compat=0)
+    o.set_parameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    o.prior()
+    yo = o.forecast(n, x3, G4)
+    assert y.shape == (m, n, 3)
+    assert np.isfinite(y).all() and np.isfinite(yo).all()
+    rtol, atol = (1e-8, 1e-10) if precision == "fp64" else (2e-3, 2e-4)
+    np.testing.assert_allclose(y, yo, rtol=rtol, atol=atol)
+    # the evolution matrix matters: without it the later steps differ
+    assert not np.allclose(y[:, :, 2], s.computeForecast(n, n, x3)[:, :, 2], rtol=1e-3)
+
+
 def readme_inputs(T, seed=20261203):
     """The README scenario (README.md:48-154) as arrays."""
     m = 6

@@ -166,3 +166,32 @@ def test_psi_series(golden):
     g = golden("psi.npz")
     np.testing.assert_allclose([oracle.psi(x) for x in g["x"]], g["psi"], rtol=1e-14)
     np.testing.assert_allclose([oracle.psi1(x) for x in g["x"]], g["psi1"], rtol=1e-14)
+
+
+def test_evo_prior_matches_reference(golden):
+    """computeEvoPrior: a = G m cut at p, R = G R G' with the reference's cut-off of
+    the entries whose row AND column are >= p (kernel_functions.cuh:98-110)."""
+    g = golden("m20_evo.npz")
+    a, R, r, W = oracle.evo_prior(g["p"], g["m_t"], g["C_t"], g["n_t"], g["beta"], g["delta"],
+                                  g["G"])
+    np.testing.assert_array_equal(r, g["evo_r"])
+    np.testing.assert_allclose(W, g["evo_W"], rtol=1e-15, atol=0)
+    np.testing.assert_allclose(a, g["evo_a"], rtol=1e-13, atol=1e-16)
+    np.testing.assert_allclose(R, g["evo_R"], rtol=1e-12, atol=1e-16)
+    p, P = g["p"], R.shape[0]
+    mixed = [R[r_, c, j] for j in range(R.shape[2]) for r_ in range(p[j]) for c in range(p[j], P)]
+    assert np.count_nonzero(mixed) > 0  # the row-and-column cut keeps these
+
+
+def test_evolve_with_G_matches_reference(golden):
+    """Forecast draws evolved with an evolution matrix: theta = G theta (full max_p
+    product) before theta += chol(W)' omega (SGDLM.cu:729-758)."""
+    g = golden("m20_evo.npz")
+    n, seed, epoch = int(g["n"]), int(g["seed"]), int(g["epoch"])
+    lam, th, _ = oracle.sample(g["p"], g["m2"], g["C2"], g["n2"], g["s2"], n, seed, epoch)
+    lam2, th2, _ = oracle.evolve(g["p"], g["W2"], g["r_t"], g["c_t"], g["beta2"], lam, th, seed,
+                                 int(g["ev_epoch"]), compat=3, G=g["G"])
+    np.testing.assert_array_equal(lam2, g["lambdas_ev"])
+    got, want = th2.transpose(1, 2, 0).copy(), g["thetas_ev_ref"].copy()
+    got[0, 0, :] = want[0, 0, :] = 0.0  # the reference's scale_omegas race (see above)
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-13)
