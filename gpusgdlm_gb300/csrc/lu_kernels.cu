@@ -247,21 +247,24 @@ template <> struct Pair<double> {
 // multiples of 32), B (32 x C) read from Up[t * kUs + c] with t relative to the
 // chunk.  The region is cut exactly into units of 2W rows x 8 columns: rows
 // {ra .. ra+W-1, ra+R/2 .. ra+R/2+W-1} and columns {ca .. ca+3, ca+C/2 .. ca+C/2+3},
-// handed to the threads round-robin (no padded tiles).  Consecutive threads take
+// handed round-robin to the nthr threads tid = 0 .. nthr-1 (no padded tiles).  Consecutive threads take
 // consecutive row groups, so Lp reads are conflict-free 16-byte vectors over one
 // contiguous line, B reads see at most two addresses per warp, and the global
 // loads and stores of the accumulators are coalesced 16-byte vectors.
 template <typename T>
 __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r0, int R,
                                                 int c_off, int C, const T *__restrict__ Lp,
-                                                const T *__restrict__ Up, int Rmax) {
+                                                const T *__restrict__ Up, int Rmax,
+                                                int tid = threadIdx.x, int nthr = blockDim.x) {
   using V = Vec<T>;
   constexpr int W = V::W;
   constexpr int TM = 2 * W, TN = 8;
   const int nrg = R / (2 * W), hr = R / 2, hc = C / 2;
   const int nu = nrg * (C / 8);
   T *Abase = A + (size_t)mp * (r0 + c_off) + r0;
-  for (int u = threadIdx.x; u < nu; u += blockDim.x) {
+  // whole units in full rounds of the block; the rest as quarter units below
+  const int full = (nu / nthr) * nthr;
+  for (int u = tid; u < full; u += nthr) {
     const int cg = u / nrg, rg = u - cg * nrg;
     const int ra = rg * W, rb = ra + hr;
     const int ca = cg * 4, cb = ca + hc;
@@ -309,6 +312,46 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
 #pragma unroll
       for (int a = 0; a < W; ++a) tmp[a] = acc[W + a][b];
       V::st(colp + rb, tmp);
+    }
+  }
+  // the last, partial round: quarter units (W rows x 4 columns) so that every
+  // thread gets nearly the same share; consecutive threads take consecutive row
+  // groups of the same quarter
+  const int nrem = nu - full, nq = 4 * nrem;
+  for (int v = tid; v < nq; v += nthr) {
+    const int qd = v / nrem, u = full + (v - qd * nrem);
+    const int cg = u / nrg, rg = u - cg * nrg;
+    const int ra = rg * W + ((qd & 1) ? hr : 0);
+    const int ca = cg * 4 + ((qd & 2) ? hc : 0);
+    T acc[W][4];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      T tmp[W];
+      V::ld(Abase + mp * (ca + b) + ra, tmp);
+#pragma unroll
+      for (int a = 0; a < W; ++a) acc[a][b] = tmp[a];
+    }
+#pragma unroll 1
+    for (int k2 = 0; k2 < kB; k2 += 2) {
+      T u2[4][2];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) Pair<T>::ld(Up + (ca + b) * kUs + k2, u2[b]);
+#pragma unroll
+      for (int kk = 0; kk < 2; ++kk) {
+        T lv[W];
+        V::ld(Lp + (k2 + kk) * Rmax + ra, lv);
+#pragma unroll
+        for (int a = 0; a < W; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[a][b] -= lv[a] * u2[b][kk];
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      T tmp[W];
+#pragma unroll
+      for (int a = 0; a < W; ++a) tmp[a] = acc[a][b];
+      V::st(Abase + mp * (ca + b) + ra, tmp);
     }
   }
 }
@@ -691,22 +734,20 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         vals[kSlotOne] = T(1);
       }
       for (int r = tid; r < m; r += blockDim.x) vals[ep.diag_slot[r]] = T(1);
-      for (int k0 = tid; k0 < ep.nnz0; k0 += 4 * kThreads) {
-        int e[4], sl[4];
+      // level-0 values: all of this thread's gathers in flight at once
+      for (int k0 = tid; k0 < ep.nnz0; k0 += 16 * kThreads) {
+        int e[16], sl[16];
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
+        for (int h = 0; h < 16; ++h) {
           const bool ok = k0 + h * kThreads < ep.nnz0;
           e[h] = ok ? ep.l0_e[k0 + h * kThreads] : -1;
           sl[h] = ok ? ep.l0_slot[k0 + h * kThreads] : 0;
         }
-        T th[4];
+        T th[16];
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          th[h] = T(0);
-          if (e[h] >= 0) th[h] = theta.at(i, e[h]);
-        }
+        for (int h = 0; h < 16; ++h) th[h] = e[h] >= 0 ? theta.at(i, e[h]) : T(0);
 #pragma unroll
-        for (int h = 0; h < 4; ++h)
+        for (int h = 0; h < 16; ++h)
           if (e[h] >= 0) vals[sl[h]] = -th[h];
       }
     } else {
@@ -732,40 +773,50 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         vals[lo16(w)] = l;
       }
       __syncthreads();
-      // new entries: each warp runs four chunks at a time (independent loads in flight)
-      const int c_end = ep.lev_chunk[lev + 1];
-      for (int c = ep.lev_chunk[lev] + warp; c < c_end; c += 4 * kWarps) {
-        unsigned e[4];
-        const unsigned *tp[4];
-        int K[4];
+      // new entries: warp w takes chunks c_begin + w + 8i; lane l prefetches the term
+      // offsets of its warp's chunk i = base + l, so that the term loads do not wait
+      // on a dependent load; four chunks are in flight at a time
+      const int c_begin = ep.lev_chunk[lev], c_end = ep.lev_chunk[lev + 1];
+      const int n_w = (c_begin + warp < c_end) ? (c_end - c_begin - warp + kWarps - 1) / kWarps : 0;
+      for (int base = 0; base < n_w; base += 32) {
+        int my_t0 = 0, my_t1 = 0;
+        if (base + lane < n_w) {
+          const int ci = c_begin + warp + (base + lane) * kWarps;
+          my_t0 = ep.chunk_tofs[ci];
+          my_t1 = ep.chunk_tofs[ci + 1];
+        }
+        const int n_here = min(32, n_w - base);
+        for (int i0 = 0; i0 < n_here; i0 += 4) {
+          unsigned e[4];
+          const unsigned *tp[4];
+          int K[4];
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const int ch = c + h * kWarps;
-          e[h] = kSlotNone;  // no store, base = constant 0
-          K[h] = 0;
-          tp[h] = ep.terms;
-          if (ch < c_end) {
-            e[h] = ep.ent[(size_t)ch * 32 + lane];
-            const int t0 = ep.chunk_tofs[ch];
-            K[h] = (ep.chunk_tofs[ch + 1] - t0) >> 5;
+          for (int h = 0; h < 4; ++h) {
+            const int ii = i0 + h;
+            const int t0 = __shfl_sync(kFull, my_t0, ii & 31);
+            const int t1 = __shfl_sync(kFull, my_t1, ii & 31);
+            const bool ok = ii < n_here;
+            const int ch = c_begin + warp + (base + ii) * kWarps;
+            e[h] = ok ? ep.ent[(size_t)ch * 32 + lane] : kSlotNone;  // none: no store, base 0
+            K[h] = ok ? (t1 - t0) >> 5 : 0;
             tp[h] = ep.terms + t0 + lane;
           }
-        }
-        T v[4];
+          T v[4];
 #pragma unroll
-        for (int h = 0; h < 4; ++h) v[h] = vals[hi16(e[h])];
-        const int Kmax = max(max(K[0], K[1]), max(K[2], K[3]));
+          for (int h = 0; h < 4; ++h) v[h] = vals[hi16(e[h])];
+          const int Kmax = max(max(K[0], K[1]), max(K[2], K[3]));
 #pragma unroll 2
-        for (int k = 0; k < Kmax; ++k) {
-          unsigned w[4];
+          for (int k = 0; k < Kmax; ++k) {
+            unsigned w[4];
 #pragma unroll
-          for (int h = 0; h < 4; ++h) w[h] = (k < K[h]) ? tp[h][32 * k] : 0u;
+            for (int h = 0; h < 4; ++h) w[h] = (k < K[h]) ? tp[h][32 * k] : 0u;
 #pragma unroll
-          for (int h = 0; h < 4; ++h) v[h] -= vals[lo16(w[h])] * vals[hi16(w[h])];
+            for (int h = 0; h < 4; ++h) v[h] -= vals[lo16(w[h])] * vals[hi16(w[h])];
+          }
+#pragma unroll
+          for (int h = 0; h < 4; ++h)
+            if ((unsigned)lo16(e[h]) != kSlotNone) vals[lo16(e[h])] = v[h];
         }
-#pragma unroll
-        for (int h = 0; h < 4; ++h)
-          if ((unsigned)lo16(e[h]) != kSlotNone) vals[lo16(e[h])] = v[h];
       }
       if (solve) level_forward<T>(ep, lev, vals, zf);
       __syncthreads();
@@ -774,15 +825,15 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     if (planned) {
       const uint2 *map4 = reinterpret_cast<const uint2 *>(ep.core_map);
       const int nq = dp * dp / 4;
-      for (int q0 = tid; q0 < nq; q0 += 4 * kThreads) {
-        uint2 w[4];
+      for (int q0 = tid; q0 < nq; q0 += 8 * kThreads) {
+        uint2 w[8];
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
+        for (int h = 0; h < 8; ++h) {
           const int q = q0 + h * kThreads;
           w[h] = q < nq ? map4[q] : make_uint2(0u, 0u);
         }
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
+        for (int h = 0; h < 8; ++h) {
           const int q = q0 + h * kThreads;
           if (q < nq) {
             T v4[4] = {vals[lo16(w[h].x)], vals[hi16(w[h].x)], vals[lo16(w[h].y)], vals[hi16(w[h].y)]};
