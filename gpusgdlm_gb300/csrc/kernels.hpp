@@ -83,6 +83,7 @@ struct LuPlan {
   int fb_grid;         // grid of the pivoting redo
   size_t smem, smem_fallback;
   int vals_smem;       // the sparse levels' value slots live in shared memory
+  int tc;              // trailing updates on the tensor cores (tcgen05)
   size_t scratch_elems_per_cta;  // dense core + per-draw values of the sparse levels
   size_t scratch_elems_total;    // covers both passes
 };

@@ -36,6 +36,8 @@
 //     solve with the same factors.
 #include <algorithm>
 
+#include <cuda_bf16.h>
+
 #include "elimination.hpp"
 #include "kernels.hpp"
 #include "rng.cuh"
@@ -84,11 +86,12 @@ __device__ double block_sum_det(double v, double *red) {
 // global memory) share one region: the slots are dead while the panels are in
 // use.  prow passes the pivot rows of the panel Gauss-Jordan's super-steps.
 struct Smem {
-  int Rmax;
-  size_t off_D, off_prow, off_Lp, off_Up, off_vals, off_z, off_nu, off_res, off_zf, off_yf,
-      off_yd, off_red, off_bsum, total;
-  __host__ __device__ Smem(int dp, int m, size_t tsz, int nv_smem) {
+  int Rmax, Mpad;
+  size_t off_D, off_prow, off_Lp, off_Up, off_vals, off_Lt, off_Ut, part_L, part_U, off_z, off_nu,
+      off_res, off_zf, off_yf, off_yd, off_red, off_bsum, total;
+  __host__ __device__ Smem(int dp, int m, size_t tsz, int nv_smem, bool tc = false) {
     Rmax = dp - kB > 0 ? dp - kB : kB;
+    Mpad = (Rmax + 127) / 128 * 128;
     size_t o = 0;
     auto take = [&](size_t bytes) {
       const size_t at = o;
@@ -97,10 +100,17 @@ struct Smem {
     };
     off_D = take((size_t)kB * kDs * tsz);
     off_prow = take((size_t)2 * kB * 4 * tsz);
-    const size_t panels = ((size_t)kB * Rmax + (size_t)Rmax * kUs) * tsz;
+    // tensor-core path: three bf16 parts of C D^-1 (Mpad rows) and of B (Rmax
+    // columns), each a K-major 32-wide UMMA tile of 64-byte rows
+    part_L = (size_t)Mpad * 64;
+    part_U = (size_t)Rmax * 64;
+    const size_t panels = tc ? 3 * (part_L + part_U) : ((size_t)kB * Rmax + (size_t)Rmax * kUs) * tsz;
     const size_t vals = (((size_t)nv_smem + 3) / 4) * 4 * tsz;
+    o = (o + 127) & ~(size_t)127;
     off_Lp = take(panels > vals ? panels : vals);
     off_Up = off_Lp + (size_t)kB * Rmax * tsz;
+    off_Lt = off_Lp;
+    off_Ut = off_Lp + 3 * part_L;
     off_vals = off_Lp;
     off_z = take((size_t)dp * tsz);
     off_nu = take((size_t)m * sizeof(double));
@@ -396,6 +406,147 @@ __device__ __forceinline__ float rcp_fast(float x) {
 }
 __device__ __forceinline__ double rcp_fast(double x) { return 1.0 / x; }
 
+// ---- tensor-core (tcgen05) trailing update for the mixed precision ------------
+// E -= L U with L = C D^-1 (R x 32) and U = B (32 x R) split three ways into
+// bf16, x = h + m + l (h = bf16(x), m = bf16(x - h), l = bf16(x - h - m)); the six
+// products h.h + h.m + m.h + h.l + m.m + l.h accumulate in FP32 into E held in
+// tensor memory, which leaves an FP32-level error.  Operands are K-major UMMA
+// tiles without swizzle: core matrices of 8 rows x 16 bytes, the four K-chunks of
+// a row group 128 bytes apart (LBO) and row groups 512 bytes apart (SBO).
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)(128 >> 4) << 16;  // leading byte offset: next K-chunk
+  d |= (uint64_t)(512 >> 4) << 32;  // stride byte offset: next 8-row group
+  d |= (uint64_t)1 << 46;           // descriptor version of tcgen05
+  return d;                         // base offset 0, no swizzle
+}
+// kind::f16 instruction descriptor: D f32, A and B bf16, A negated, K-major,
+// M = 128, N columns.
+__device__ __forceinline__ uint32_t umma_idesc(int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 13) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(128 >> 4) << 24);
+}
+// byte offset of (row n, k) in a K-major 32-wide bf16 tile
+__device__ __forceinline__ int umma_off(int n, int k) {
+  return (n >> 3) * 512 + (k >> 3) * 128 + (n & 7) * 16 + (k & 7) * 2;
+}
+__device__ __forceinline__ uint32_t bf16_pair(__nv_bfloat16 a, __nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+// Writes row n (32 values) of a split operand: three parts, part_bytes apart.
+__device__ __forceinline__ void write_split_row(unsigned char *tile, size_t part_bytes, int n,
+                                                const float (&x)[kB]) {
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    uint32_t h[4], mm[4], l[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      __nv_bfloat16 hv[2], mv[2], lv[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const float v = x[8 * c + 2 * e + u];
+        hv[u] = __float2bfloat16_rn(v);
+        const float r1 = v - __bfloat162float(hv[u]);
+        mv[u] = __float2bfloat16_rn(r1);
+        lv[u] = __float2bfloat16_rn(r1 - __bfloat162float(mv[u]));
+      }
+      h[e] = bf16_pair(hv[0], hv[1]);
+      mm[e] = bf16_pair(mv[0], mv[1]);
+      l[e] = bf16_pair(lv[0], lv[1]);
+    }
+    unsigned char *d = tile + umma_off(n, 8 * c);
+    *reinterpret_cast<uint4 *>(d) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(d + part_bytes) = make_uint4(mm[0], mm[1], mm[2], mm[3]);
+    *reinterpret_cast<uint4 *>(d + 2 * part_bytes) = make_uint4(l[0], l[1], l[2], l[3]);
+  }
+}
+
+// E[r0:, r0:] (R x R, leading dimension dp) -= L U on the tensor cores, 128-row
+// tiles (rows beyond R are padding: loaded as 0, never stored).  E goes through
+// tensor memory (tmem: 128 lanes x up to 256 columns of this CTA); thread 0
+// issues the 12 MMAs of a tile and commits them to mbar; every thread waits with
+// a bounded spin (a timeout sets bad, and the draw is redone by the pivoting
+// pass).  All 8 warps load and store: warp w handles lanes 32 (w % 4) .. and the
+// column half w / 4.
+__device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
+                                   const unsigned char *Lt, const unsigned char *Ut,
+                                   size_t part_L, size_t part_U, uint32_t tmem, uint64_t *mbar,
+                                   uint32_t &mphase, bool &bad) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, half = warp >> 2, hc = R / 2;
+  float *E = A + (size_t)r0 + (size_t)dp * r0;
+  const uint32_t idesc = umma_idesc(R);
+  for (int mt = 0; mt < R; mt += 128) {
+    const int row = mt + quarter * 32 + lane;
+    const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
+    for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 16) {
+      uint32_t v[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        v[j] = __float_as_uint(row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f);
+      asm volatile(
+          "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+          "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(tlane + (uint32_t)c0),
+          "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+          "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+          "r"(v[15]));
+    }
+    asm volatile("tcgen05.wait::st.sync.aligned;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const uint32_t la = smem_u32(Lt) + (uint32_t)(mt / 8) * 512, ua = smem_u32(Ut);
+      const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          const uint64_t ad = umma_desc(la + (uint32_t)(pa[q] * part_L) + ks * 256);
+          const uint64_t bd = umma_desc(ua + (uint32_t)(pb[q] * part_U) + ks * 256);
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(1));
+        }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(mbar)));
+    }
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22) && !done; ++it)
+      asm volatile(
+          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+          "selp.u32 %0, 1, 0, p;\n}"
+          : "=r"(done)
+          : "r"(smem_u32(mbar)), "r"(mphase));
+    if (!done) bad = true;
+    mphase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 16) {
+      uint32_t v[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(tlane + (uint32_t)c0));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (row < R) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) E[(size_t)row + (size_t)dp * (c0 + j)] = __uint_as_float(v[j]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+  }
+}
+
 // Panel Gauss-Jordan: column elimination of the stacked block column [D; C]
 // (D the 32 x 32 diagonal block, C the rows below it) with 4 x 4 pivot blocks,
 // in place, giving [D^-1; C D^-1] -- the block inverse and the block multipliers
@@ -689,7 +840,7 @@ __device__ __forceinline__ void copy_vals(T *__restrict__ dst, const T *__restri
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
-    k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, long n, EliminationPlan ep,
+    k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, int tc, long n, EliminationPlan ep,
          const unsigned *__restrict__ sp, const T *__restrict__ theta_sm,
          const T *__restrict__ theta_dm, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
@@ -699,7 +850,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Theta<T> theta{theta_sm, theta_dm, m, P, n};
-  const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0);
+  const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0, tc != 0);
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);  // D^-1, row-major, stride kB
   T *prow = reinterpret_cast<T *>(smem_raw + L.off_prow);
   T *Lp = reinterpret_cast<T *>(smem_raw + L.off_Lp);
@@ -722,6 +873,25 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   const bool solve = (x != nullptr);
   const T tau = (T)kPivotThreshold;
   __shared__ int sflag;
+  // tensor-core trailing updates (FP32 draws, d_p <= 256): 256 columns of tensor
+  // memory for this CTA and the MMA completion barrier
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_mbar;
+  uint32_t mphase = 0;
+  if constexpr (sizeof(T) == 4) {
+    if (tc) {
+      if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+            smem_u32(&s_tmem)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+      }
+      if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_mbar)));
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+  }
+  const uint32_t tmem = (sizeof(T) == 4 && tc) ? s_tmem : 0u;
 
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
     if (tid == 0) sflag = 0;
@@ -848,7 +1018,65 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       for (int r = tid; r < dp; r += blockDim.x)
         z[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
     __syncthreads();
-    for (int kb = 0; kb < nbk; ++kb) {
+    if constexpr (sizeof(T) == 4) {
+      if (tc) {
+        // d_p <= 256: the panel Gauss-Jordan holds every row of C; the trailing
+        // update runs on the tensor cores
+        unsigned char *Lt = smem_raw + L.off_Lt, *Ut = smem_raw + L.off_Ut;
+        for (int kb = 0; kb < nbk; ++kb) {
+          const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
+          {
+            const int t = (warp - 1) * 32 + lane;  // row of C (warps 1..7)
+            const bool active = (warp == 0) || t < R;
+            T *rowp = A + (size_t)(warp == 0 ? k0 + lane : r0 + t) + (size_t)dp * k0;
+            T a[kB];
+#pragma unroll
+            for (int q = 0; q < kB; ++q) a[q] = active ? rowp[(size_t)dp * q] : T(0);
+            if (warp == 0 || (warp - 1) * 32 < R) {
+              ld_part += panel_gauss_jordan<T>(a, active, prow, tau, bad);
+            } else {
+              for (int K = 0; K < kB / 4; ++K) __syncthreads();  // the same barriers, no rows
+            }
+            if (warp > 0 && active) {
+              write_split_row(Lt, L.part_L, t, reinterpret_cast<const float(&)[kB]>(a));
+              if (solve) {
+                T acc = T(0);
+#pragma unroll
+                for (int q = 0; q < kB; ++q) acc += a[q] * z[k0 + q];
+                z[r0 + t] -= acc;
+              }
+            }
+            if (solve && active) {
+              // keep D^-1 and C D^-1 for the solves
+#pragma unroll
+              for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = a[q];
+            }
+          }
+          if (R > 0) {
+            // the row panel B (rows k0.., columns r0..), split, one column per thread
+            for (int t = tid; t < R; t += blockDim.x) {
+              const float *colp = reinterpret_cast<const float *>(A) + (size_t)k0 + (size_t)dp * (r0 + t);
+              float b[kB];
+#pragma unroll
+              for (int q = 0; q < kB; q += 4) {
+                const float4 v = *reinterpret_cast<const float4 *>(colp + q);
+                b[q] = v.x; b[q + 1] = v.y; b[q + 2] = v.z; b[q + 3] = v.w;
+              }
+              write_split_row(Ut, L.part_U, t, b);
+            }
+            asm volatile("fence.proxy.async.shared::cta;");
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            tc_trailing_update(reinterpret_cast<float *>(A), dp, r0, R, Lt, Ut, L.part_L,
+                               L.part_U, tmem, &s_mbar, mphase, bad);
+          } else {
+            __syncthreads();
+          }
+        }
+      }
+    }
+    if (!(sizeof(T) == 4 && tc)) for (int kb = 0; kb < nbk; ++kb) {
       const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
       const int Rg = R < kGjRows ? R : kGjRows;  // rows of C inside the panel Gauss-Jordan
       // (a) the row panel B (and rows of C beyond Rg) in flight while the panel
@@ -977,6 +1205,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       }
     }
     __syncthreads();
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (tc && warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
   }
 }
 
@@ -1213,9 +1444,12 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv) {
   pl.block = kThreads;
   // value slots in shared memory when that keeps the target occupancy
   const int target = sizeof(T) == 4 ? 2 : 1;
-  const size_t with_vals = Smem(pl.dp, m, sizeof(T), nv).total;
+  // tensor-core trailing updates for FP32 draws while the 32-wide panel holds every
+  // row of the core (d_p <= 256: N <= 224 columns in 256 columns of tensor memory)
+  pl.tc = (sizeof(T) == 4 && pl.dp <= 256) ? 1 : 0;
+  const size_t with_vals = Smem(pl.dp, m, sizeof(T), nv, pl.tc != 0).total;
   pl.vals_smem = (nv > 0 && with_vals <= smem_budget(target)) ? 1 : 0;
-  pl.smem = Smem(pl.dp, m, sizeof(T), pl.vals_smem ? nv : 0).total;
+  pl.smem = Smem(pl.dp, m, sizeof(T), pl.vals_smem ? nv : 0, pl.tc != 0).total;
   pl.smem_fallback = FallbackSmem(pl.mp, m, sizeof(T)).total;
   int ctas_per_sm = pl.smem <= smem_budget(2) ? 2 : 1;
   if (sizeof(T) == 8) ctas_per_sm = 1;
@@ -1250,7 +1484,7 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
   if (pl.smem > 48 * 1024)
     cudaFuncSetAttribute(k_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
   k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
-                                             pl.vals_smem, n, ep, sp, theta, theta_dm, scratch,
+                                             pl.vals_smem, pl.tc, n, ep, sp, theta, theta_dm, scratch,
                                              logdet,
                                              draw_flags, x, lambda, key, refine, y, rows);
 }
