@@ -51,8 +51,11 @@ constexpr int kWarps = kThreads / 32;
 constexpr double kPivotThreshold = 8.0;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kDs = 36;  // row stride of D^-1 in shared memory (16-byte rows, 4-way store conflicts)
-constexpr int kUs = 36;
-constexpr int kGjRows = 224;  // rows of C the panel Gauss-Jordan holds (warps 1..7)  // stride of the row panel B, stored column by column: B[c][t] at t*kUs + c
+constexpr int kUs = 36;  // stride of the row panel B, stored column by column: B[c][t] at t*kUs + c
+constexpr int kGjRows = 224;  // rows of C the panel Gauss-Jordan holds (warps 1..7)
+// one super-step of the panel Gauss-Jordan in shared memory: the pivot rows
+// (row q, position p at 32q + p), then P^-1 (entry (q, c) at 128 + 4q + c)
+constexpr int kGjSlot = kB * 4 + 16;
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -84,7 +87,7 @@ __device__ double block_sum_det(double v, double *red) {
 // panel buffers Lp (C, column-major, 32 x Rmax) / Up (B, Rmax columns of kUs)
 // and the value slots of the sparse levels (nv_smem of them, 0 when they live in
 // global memory) share one region: the slots are dead while the panels are in
-// use.  prow passes the pivot rows of the panel Gauss-Jordan's super-steps.
+// use.  prow holds the eight super-steps of the panel Gauss-Jordan.
 struct Smem {
   int Rmax, Mpad;
   size_t off_D, off_prow, off_Lp, off_Up, off_vals, off_Lt, off_Ut, part_L, part_U, off_z, off_nu,
@@ -99,7 +102,7 @@ struct Smem {
       return at;
     };
     off_D = take((size_t)kB * kDs * tsz);
-    off_prow = take((size_t)2 * kB * 4 * tsz);
+    off_prow = take((size_t)(kB / 4) * kGjSlot * tsz);
     // tensor-core path: three bf16 parts of C D^-1 (Mpad rows) and of B (Rmax
     // columns), each a K-major 32-wide UMMA tile of 64-byte rows
     part_L = (size_t)Mpad * 64;
@@ -560,32 +563,92 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
 //                                 a[p]     <- -(P^-1 M[K][p])[qi]
 // and rotates the columns by four positions (a[p-4] <- new a[p], a[28..31] <- the
 // new pivot columns), so that every register index is a constant and after
-// eight super-steps the columns are back in place.  The pivot rows travel
-// through shared memory (prowT, two alternating buffers of 32 positions x 4, so
-// one barrier per super-step suffices); each warp inverts P in 16 lanes by
-// Gauss-Jordan with shuffles.  The pivots of P are the LU pivots of D.
+// eight super-steps the columns are back in place.  The pivots of P are the LU
+// pivots of D.
+//
+// Only the rows of D feed the next super-step, so warp 0 runs the eight of them
+// alone (gj_diag, warp-synchronous) and publishes super-step K in its own slot
+// of shared memory -- the pivot rows M[K][*] at the start of the super-step and
+// P^-1 -- with bar.arrive on named barrier 1 + K; the rows of C (gj_rows) wait
+// on that barrier only, so they trail warp 0 without a CTA-wide barrier between
+// super-steps, and warps 1..7 can do other work (the row panel B) first.  All 256
+// threads take part in the eight named barriers of every panel.
 // No-pivot check: zero / non-finite pivots, LU multipliers inside P above tau,
 // and block multipliers g of the rows still to be eliminated (rows of D below the
-// pivot rows, all rows of C) above tau.  Thread 0 returns sum log|det P|.
+// pivot rows, all rows of C) above tau.
+constexpr int kGjBar0 = 1;            // named barriers 1 .. 8; barrier 0 is __syncthreads
+
+__device__ __forceinline__ void named_arrive(int id) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(kThreads) : "memory");
+}
+__device__ __forceinline__ void named_sync(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(kThreads) : "memory");
+}
+
+// The update of one super-step, with the rotation: a[p - 4] <- base[p] - g . M[K][p]
+// for p = 4..31 (base = a, or 0 for the pivot rows), M[K] the pivot rows in the
+// slot buf.  FP32: packed f32x2 FMAs over pairs of positions.
 template <typename T>
-__device__ __forceinline__ double panel_gauss_jordan(T (&a)[kB], bool active, T *prowT, T tau,
-                                                     bool &bad) {
+__device__ __forceinline__ void gj_update(T (&a)[kB], const T (&g)[4], const T *buf, bool zero) {
+  if constexpr (sizeof(T) == 4) {
+    float2 ng[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) ng[q] = make_float2(-g[q], -g[q]);
+#pragma unroll
+    for (int p = 4; p < kB; p += 4) {
+      float4 r[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) r[q] = *reinterpret_cast<const float4 *>(buf + q * kB + p);
+      float2 lo = zero ? make_float2(0.f, 0.f) : make_float2(a[p], a[p + 1]);
+      float2 hi = zero ? make_float2(0.f, 0.f) : make_float2(a[p + 2], a[p + 3]);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        lo = __ffma2_rn(ng[q], make_float2(r[q].x, r[q].y), lo);
+        hi = __ffma2_rn(ng[q], make_float2(r[q].z, r[q].w), hi);
+      }
+      a[p - 4] = lo.x;
+      a[p - 3] = lo.y;
+      a[p - 2] = hi.x;
+      a[p - 1] = hi.y;
+    }
+  } else {
+#pragma unroll
+    for (int p = 4; p < kB; p += 2) {
+      T r[4][2];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) Vec<T>::ld(buf + q * kB + p, r[q]);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        T v = zero ? T(0) : a[p + u];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v = fma(-g[q], r[q][u], v);
+        a[p - 4 + u] = v;
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) a[kB - 4 + c] = g[c];
+}
+
+// Warp 0, lane = row of D.  Lane 0 returns sum log|det P|.
+template <typename T>
+__device__ __forceinline__ double gj_diag(T (&a)[kB], T *slots, T tau, bool &bad) {
   using V = Vec<T>;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int l16 = lane & 15, pq = l16 >> 2, pc = l16 & 3;
   double ld = 0.0;
 #pragma unroll 1
   for (int K = 0; K < kB / 4; ++K) {
     const int c0 = 4 * K;
-    T *buf = prowT + (K & 1) * (kB * 4);
-    const bool inK = (warp == 0) && lane >= c0 && lane < c0 + 4;
+    T *buf = slots + K * kGjSlot;
+    const bool inK = lane >= c0 && lane < c0 + 4;
     if (inK) {
 #pragma unroll
-      for (int p = 0; p < kB; ++p) buf[p * 4 + (lane - c0)] = a[p];
+      for (int p = 0; p < kB; p += V::W) V::st(buf + (lane - c0) * kB + p, a + p);
     }
-    __syncthreads();
+    __syncwarp();
     // P^-1 in 16 lanes: lane (pq, pc) holds entry (pq, pc)
-    T mv = buf[pc * 4 + pq];
+    T mv = buf[pq * kB + pc];
     T det = T(1);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -598,7 +661,9 @@ __device__ __forceinline__ double panel_gauss_jordan(T (&a)[kB], bool active, T 
       if (pq > k && pc == k && !(dabs(fik * rp) <= tau)) bad = true;
       mv = (pq == k) ? ((pc == k) ? rp : prk * rp) : ((pc == k) ? -fik * rp : mv - fik * (prk * rp));
     }
-    if (threadIdx.x == 0) ld += log_abs(det);
+    if (lane < 16) buf[kB * 4 + lane] = mv;
+    named_arrive(kGjBar0 + K);  // super-step K is readable by the rows of C
+    if (lane == 0) ld += log_abs(det);
     // g = f P^-1, f = this row's pivot-column entries (unit vector for pivot rows)
     T f[4];
 #pragma unroll
@@ -611,32 +676,45 @@ __device__ __forceinline__ double panel_gauss_jordan(T (&a)[kB], bool active, T 
       for (int q = 0; q < 4; ++q) acc += f[q] * __shfl_sync(kFull, mv, 4 * q + c);
       g[c] = acc;
     }
-    if (active && (warp > 0 || lane >= c0 + 4)) {
+    if (lane >= c0 + 4) {
 #pragma unroll
       for (int c = 0; c < 4; ++c)
         if (!(dabs(g[c]) <= tau)) bad = true;
     }
-    if (warp == 0) {
-#pragma unroll
-      for (int p = 4; p < kB; ++p) {
-        T r[4];
-#pragma unroll
-        for (int q = 0; q < 4; q += V::W) V::ld(buf + p * 4 + q, r + q);
-        a[p - 4] = (inK ? T(0) : a[p]) - (g[0] * r[0] + g[1] * r[1] + g[2] * r[2] + g[3] * r[3]);
-      }
-    } else {
-#pragma unroll
-      for (int p = 4; p < kB; ++p) {
-        T r[4];
-#pragma unroll
-        for (int q = 0; q < 4; q += V::W) V::ld(buf + p * 4 + q, r + q);
-        a[p - 4] = a[p] - (g[0] * r[0] + g[1] * r[1] + g[2] * r[2] + g[3] * r[3]);
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < 4; ++c) a[kB - 4 + c] = g[c];
+    gj_update<T>(a, g, buf, inK);
   }
   return ld;
+}
+
+// Warps 1..7, one row of C per thread (active: the row exists).  rows: this warp
+// has at least one row; a warp without rows only takes part in the barriers.
+template <typename T>
+__device__ __forceinline__ void gj_rows(T (&a)[kB], bool active, bool rows, const T *slots, T tau,
+                                        bool &bad) {
+  using V = Vec<T>;
+#pragma unroll 1
+  for (int K = 0; K < kB / 4; ++K) {
+    named_sync(kGjBar0 + K);
+    if (!rows) continue;
+    const T *buf = slots + K * kGjSlot;
+    T pinv[16];
+#pragma unroll
+    for (int q = 0; q < 16; q += V::W) V::ld(buf + kB * 4 + q, pinv + q);
+    T g[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      T acc = T(0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc += a[q] * pinv[4 * q + c];
+      g[c] = acc;
+    }
+    if (active) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (!(dabs(g[c]) <= tau)) bad = true;
+    }
+    gj_update<T>(a, g, buf, false);
+  }
 }
 
 // Back solve of the block elimination, in place on v (length dp, shared):
@@ -1025,36 +1103,21 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         unsigned char *Lt = smem_raw + L.off_Lt, *Ut = smem_raw + L.off_Ut;
         for (int kb = 0; kb < nbk; ++kb) {
           const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
-          {
-            const int t = (warp - 1) * 32 + lane;  // row of C (warps 1..7)
-            const bool active = (warp == 0) || t < R;
-            T *rowp = A + (size_t)(warp == 0 ? k0 + lane : r0 + t) + (size_t)dp * k0;
+          if (warp == 0) {
+            // the rows of D: D^-1 by the warp-synchronous Gauss-Jordan
+            T *rowp = A + (size_t)(k0 + lane) + (size_t)dp * k0;
             T a[kB];
 #pragma unroll
-            for (int q = 0; q < kB; ++q) a[q] = active ? rowp[(size_t)dp * q] : T(0);
-            if (warp == 0 || (warp - 1) * 32 < R) {
-              ld_part += panel_gauss_jordan<T>(a, active, prow, tau, bad);
-            } else {
-              for (int K = 0; K < kB / 4; ++K) __syncthreads();  // the same barriers, no rows
-            }
-            if (warp > 0 && active) {
-              write_split_row(Lt, L.part_L, t, reinterpret_cast<const float(&)[kB]>(a));
-              if (solve) {
-                T acc = T(0);
-#pragma unroll
-                for (int q = 0; q < kB; ++q) acc += a[q] * z[k0 + q];
-                z[r0 + t] -= acc;
-              }
-            }
-            if (solve && active) {
-              // keep D^-1 and C D^-1 for the solves
+            for (int q = 0; q < kB; ++q) a[q] = rowp[(size_t)dp * q];
+            ld_part += gj_diag<T>(a, prow, tau, bad);
+            if (solve) {
 #pragma unroll
               for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = a[q];
             }
-          }
-          if (R > 0) {
-            // the row panel B (rows k0.., columns r0..), split, one column per thread
-            for (int t = tid; t < R; t += blockDim.x) {
+          } else {
+            // while warp 0 factors D: the row panel B (rows k0.., columns r0..),
+            // split, one column per thread
+            for (int t = tid - 32; t < R; t += kThreads - 32) {
               const float *colp = reinterpret_cast<const float *>(A) + (size_t)k0 + (size_t)dp * (r0 + t);
               float b[kB];
 #pragma unroll
@@ -1064,6 +1127,28 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
               }
               write_split_row(Ut, L.part_U, t, b);
             }
+            // then the rows of C: C D^-1, trailing warp 0 super-step by super-step
+            const int t = (warp - 1) * 32 + lane;
+            const bool active = t < R;
+            T *rowp = A + (size_t)(r0 + t) + (size_t)dp * k0;
+            T a[kB];
+#pragma unroll
+            for (int q = 0; q < kB; ++q) a[q] = active ? rowp[(size_t)dp * q] : T(0);
+            gj_rows<T>(a, active, (warp - 1) * 32 < R, prow, tau, bad);
+            if (active) {
+              write_split_row(Lt, L.part_L, t, reinterpret_cast<const float(&)[kB]>(a));
+              if (solve) {
+                T acc = T(0);
+#pragma unroll
+                for (int q = 0; q < kB; ++q) acc += a[q] * z[k0 + q];
+                z[r0 + t] -= acc;
+                // keep C D^-1 for the solves
+#pragma unroll
+                for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = a[q];
+              }
+            }
+          }
+          if (R > 0) {
             asm volatile("fence.proxy.async.shared::cta;");
             asm volatile("tcgen05.fence::before_thread_sync;");
             __syncthreads();
@@ -1089,11 +1174,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         T a[kB];
 #pragma unroll
         for (int q = 0; q < kB; ++q) a[q] = active ? rowp[(size_t)dp * q] : T(0);
-        if (warp == 0 || (warp - 1) * 32 < Rg) {
-          ld_part += panel_gauss_jordan<T>(a, active, prow, tau, bad);
-        } else {
-          for (int K = 0; K < kB / 4; ++K) __syncthreads();  // the same barriers, no rows
-        }
+        if (warp == 0)
+          ld_part += gj_diag<T>(a, prow, tau, bad);
+        else
+          gj_rows<T>(a, active, (warp - 1) * 32 < Rg, prow, tau, bad);
         if (warp == 0) {
 #pragma unroll
           for (int q = 0; q < kB; q += W) V::st(D + lane * kDs + q, a + q);
