@@ -54,8 +54,10 @@ constexpr int kDs = 36;  // row stride of D^-1 in shared memory (16-byte rows, 4
 constexpr int kUs = 36;  // stride of the row panel B, stored column by column: B[c][t] at t*kUs + c
 constexpr int kGjRows = 224;  // rows of C the panel Gauss-Jordan holds (warps 1..7)
 // one super-step of the panel Gauss-Jordan in shared memory: the pivot rows
-// (row q, position p at 32q + p), then P^-1 (entry (q, c) at 128 + 4q + c)
-constexpr int kGjSlot = kB * 4 + 16;
+// (row q, position p at kGjRow q + p; the padding keeps the four writers' 16-byte
+// stores on distinct banks), then P^-1 (entry (q, c) at 4 kGjRow + 4q + c)
+constexpr int kGjRow = kB + 4;
+constexpr int kGjSlot = 4 * kGjRow + 16;
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -90,8 +92,8 @@ __device__ double block_sum_det(double v, double *red) {
 // use.  prow holds the eight super-steps of the panel Gauss-Jordan.
 struct Smem {
   int Rmax, Mpad;
-  size_t off_D, off_prow, off_Lp, off_Up, off_vals, off_Lt, off_Ut, part_L, part_U, off_z, off_nu,
-      off_res, off_zf, off_yf, off_yd, off_red, off_bsum, total;
+  size_t off_D, off_prow, off_Dt, off_Lp, off_Up, off_vals, off_Lt, off_Ut, part_L, part_U, off_z,
+      off_nu, off_res, off_zf, off_yf, off_yd, off_red, off_bsum, total;
   __host__ __device__ Smem(int dp, int m, size_t tsz, int nv_smem, bool tc = false) {
     Rmax = dp - kB > 0 ? dp - kB : kB;
     Mpad = (Rmax + 127) / 128 * 128;
@@ -103,6 +105,9 @@ struct Smem {
     };
     off_D = take((size_t)kB * kDs * tsz);
     off_prow = take((size_t)(kB / 4) * kGjSlot * tsz);
+    // tensor-core path: D^-1 as the B operand of L = C D^-1 (three bf16 parts of
+    // 32 rows x 64 bytes)
+    off_Dt = tc ? take((size_t)3 * kB * 64) : o;
     // tensor-core path: three bf16 parts of C D^-1 (Mpad rows) and of B (Rmax
     // columns), each a K-major 32-wide UMMA tile of 64-byte rows
     part_L = (size_t)Mpad * 64;
@@ -426,11 +431,11 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
   d |= (uint64_t)1 << 46;           // descriptor version of tcgen05
   return d;                         // base offset 0, no swizzle
 }
-// kind::f16 instruction descriptor: D f32, A and B bf16, A negated, K-major,
-// M = 128, N columns.
-__device__ __forceinline__ uint32_t umma_idesc(int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 13) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(128 >> 4) << 24);
+// kind::f16 instruction descriptor: D f32, A and B bf16, K-major, M = 128, N
+// columns; negate: A negated (D -= A B).
+__device__ __forceinline__ uint32_t umma_idesc(int N, bool negate = true) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (negate ? (1u << 13) : 0u) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 }
 // byte offset of (row n, k) in a K-major 32-wide bf16 tile
 __device__ __forceinline__ int umma_off(int n, int k) {
@@ -465,6 +470,103 @@ __device__ __forceinline__ void write_split_row(unsigned char *tile, size_t part
     *reinterpret_cast<uint4 *>(d + part_bytes) = make_uint4(mm[0], mm[1], mm[2], mm[3]);
     *reinterpret_cast<uint4 *>(d + 2 * part_bytes) = make_uint4(l[0], l[1], l[2], l[3]);
   }
+}
+
+// Bounded wait for the MMA completion barrier (a timeout sets bad, and the draw
+// is redone by the pivoting pass).
+__device__ __forceinline__ void mma_wait(uint64_t *mbar, uint32_t &mphase, bool &bad) {
+  uint32_t done = 0;
+  for (int it = 0; it < (1 << 22) && !done; ++it)
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(mbar)), "r"(mphase));
+  if (!done) bad = true;
+  mphase ^= 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;");
+}
+
+// The six split products of one 128-row tile, K = 32 (two K-steps of 16):
+// D (+)= A B^T with A = la (three parts, part_a apart) and B = lb (part_b apart).
+__device__ __forceinline__ void umma_split_tile(uint32_t d_tmem, uint32_t la, size_t part_a,
+                                                uint32_t lb, size_t part_b, uint32_t idesc,
+                                                bool accumulate) {
+  const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+  for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const uint64_t ad = umma_desc(la + (uint32_t)(pa[q] * part_a) + ks * 256);
+      const uint64_t bd = umma_desc(lb + (uint32_t)(pb[q] * part_b) + ks * 256);
+      const uint32_t acc = (accumulate || ks > 0 || q > 0) ? 1u : 0u;
+      asm volatile(
+          "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+          "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+    }
+}
+
+// The block multipliers L = C D^-1 (R x 32) on the tensor cores: C split in Lt
+// (rows of C, K-major), D^-1 split in Dt (its columns as rows), one 128-row tile
+// per 32 columns of tensor memory.  Each thread then reads one row of L back,
+// checks |L| <= tau (the no-pivot criterion of the rows of C), writes it split
+// into Lt (in place of C: the MMAs have completed) as the A operand of the
+// trailing update and, when solving, applies it to the right-hand side and keeps
+// it in A.  Warp w reads tile w / 4, lanes 32 (w % 4) ..
+__device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int r0, int R,
+                                     unsigned char *Lt, size_t part_L, const unsigned char *Dt,
+                                     uint32_t tmem, uint64_t *mbar, uint32_t &mphase, float tau,
+                                     float *z, bool solve, bool &bad) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int mt = 0; mt < R; mt += 128)
+      umma_split_tile(tmem + (uint32_t)(mt / 128) * kB, smem_u32(Lt) + (uint32_t)(mt / 8) * 512,
+                      part_L, smem_u32(Dt), (size_t)kB * 64, umma_idesc(kB, false), false);
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(mbar)));
+  }
+  mma_wait(mbar, mphase, bad);
+  const int tile = warp >> 2, quarter = warp & 3;
+  if (tile * 128 < R) {
+    const int row = tile * 128 + quarter * 32 + lane;
+    uint32_t v[kB];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+          "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+          "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+          "=r"(v[31])
+        : "r"(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)tile * kB));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+    if (row < R) {
+      float l[kB];
+#pragma unroll
+      for (int q = 0; q < kB; ++q) {
+        l[q] = __uint_as_float(v[q]);
+        bad |= !(fabsf(l[q]) <= tau);
+      }
+      write_split_row(Lt, part_L, row, l);
+      if (solve) {
+        float acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < kB; ++q) acc += l[q] * z[k0 + q];
+        z[r0 + row] -= acc;
+        float *rowp = A + (size_t)(r0 + row) + (size_t)dp * k0;
+#pragma unroll
+        for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = l[q];
+      }
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
 }
 
 // E[r0:, r0:] (R x R, leading dimension dp) -= L U on the tensor cores, 128-row
@@ -502,33 +604,13 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const uint32_t la = smem_u32(Lt) + (uint32_t)(mt / 8) * 512, ua = smem_u32(Ut);
-      const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
-#pragma unroll
-      for (int ks = 0; ks < 2; ++ks)
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-          const uint64_t ad = umma_desc(la + (uint32_t)(pa[q] * part_L) + ks * 256);
-          const uint64_t bd = umma_desc(ua + (uint32_t)(pb[q] * part_U) + ks * 256);
-          asm volatile(
-              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-              "l"(ad), "l"(bd), "r"(idesc), "r"(1));
-        }
+      umma_split_tile(tmem, smem_u32(Lt) + (uint32_t)(mt / 8) * 512, part_L, smem_u32(Ut), part_U,
+                      idesc, true);
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
               smem_u32(mbar)));
     }
-    uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; ++it)
-      asm volatile(
-          "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-          "selp.u32 %0, 1, 0, p;\n}"
-          : "=r"(done)
-          : "r"(smem_u32(mbar)), "r"(mphase));
-    if (!done) bad = true;
-    mphase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;");
+    mma_wait(mbar, mphase, bad);
     for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 16) {
       uint32_t v[16];
       asm volatile(
@@ -585,20 +667,23 @@ __device__ __forceinline__ void named_sync(int id) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(kThreads) : "memory");
 }
 
-// The update of one super-step, with the rotation: a[p - 4] <- base[p] - g . M[K][p]
-// for p = 4..31 (base = a, or 0 for the pivot rows), M[K] the pivot rows in the
-// slot buf.  FP32: packed f32x2 FMAs over pairs of positions.
-template <typename T>
-__device__ __forceinline__ void gj_update(T (&a)[kB], const T (&g)[4], const T *buf, bool zero) {
+// The update of one super-step for the positions P0 <= p < P1 (multiples of 4):
+// a[p - 4] <- base[p] - g . M[K][p] (base = a, or 0 for the pivot rows), M[K] the
+// pivot rows in the slot buf.  Positions are updated in increasing order, so the
+// shift by four reads every position before it is overwritten.  FP32: packed
+// f32x2 FMAs over pairs of positions.
+template <int P0, int P1, typename T>
+__device__ __forceinline__ void gj_update_range(T (&a)[kB], const T (&g)[4], const T *buf,
+                                                bool zero) {
   if constexpr (sizeof(T) == 4) {
     float2 ng[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) ng[q] = make_float2(-g[q], -g[q]);
 #pragma unroll
-    for (int p = 4; p < kB; p += 4) {
+    for (int p = P0; p < P1; p += 4) {
       float4 r[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) r[q] = *reinterpret_cast<const float4 *>(buf + q * kB + p);
+      for (int q = 0; q < 4; ++q) r[q] = *reinterpret_cast<const float4 *>(buf + q * kGjRow + p);
       float2 lo = zero ? make_float2(0.f, 0.f) : make_float2(a[p], a[p + 1]);
       float2 hi = zero ? make_float2(0.f, 0.f) : make_float2(a[p + 2], a[p + 3]);
 #pragma unroll
@@ -613,10 +698,10 @@ __device__ __forceinline__ void gj_update(T (&a)[kB], const T (&g)[4], const T *
     }
   } else {
 #pragma unroll
-    for (int p = 4; p < kB; p += 2) {
+    for (int p = P0; p < P1; p += 2) {
       T r[4][2];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) Vec<T>::ld(buf + q * kB + p, r[q]);
+      for (int q = 0; q < 4; ++q) Vec<T>::ld(buf + q * kGjRow + p, r[q]);
 #pragma unroll
       for (int u = 0; u < 2; ++u) {
         T v = zero ? T(0) : a[p + u];
@@ -626,44 +711,109 @@ __device__ __forceinline__ void gj_update(T (&a)[kB], const T (&g)[4], const T *
       }
     }
   }
+}
+// The whole update of a super-step and the rotation (the new pivot columns g go
+// to positions 28..31).
+template <typename T>
+__device__ __forceinline__ void gj_update(T (&a)[kB], const T (&g)[4], const T *buf, bool zero) {
+  gj_update_range<4, kB>(a, g, buf, zero);
 #pragma unroll
   for (int c = 0; c < 4; ++c) a[kB - 4 + c] = g[c];
 }
 
-// Warp 0, lane = row of D.  Lane 0 returns sum log|det P|.
+// P^-1 of a 4 x 4 pivot block, in place, by Gauss-Jordan in registers (every
+// lane of the warp holds the whole block and computes the same inverse: no
+// shuffles in the dependent chain).  det = det P.  Flags zero / non-finite
+// pivots and LU multipliers of P above tau.
+template <int k, typename T>
+__device__ __forceinline__ void gj_invert4_step(T (&P)[4][4], T tau, bool &bad, T &det) {
+  {
+    const T pk = P[k][k];
+    bad |= !(finite_t(pk) && pk != T(0));
+    det *= pk;
+    const T rp = rcp_fast(pk);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j != k) P[k][j] *= rp;
+    P[k][k] = rp;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i == k) continue;
+      const T f = P[i][k];
+      if (i > k) bad |= !(dabs(f * rp) <= tau);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j != k) P[i][j] -= f * P[k][j];
+      P[i][k] = -f * rp;
+    }
+  }
+}
 template <typename T>
+__device__ __forceinline__ void gj_invert4(T (&P)[4][4], T tau, bool &bad, T &det) {
+  det = T(1);
+  gj_invert4_step<0>(P, tau, bad, det);
+  gj_invert4_step<1>(P, tau, bad, det);
+  gj_invert4_step<2>(P, tau, bad, det);
+  gj_invert4_step<3>(P, tau, bad, det);
+}
+
+// The pivot block (positions 0..3 of the slot's four pivot rows) into every lane.
+template <typename T>
+__device__ __forceinline__ void gj_load_block(const T *buf, T (&P)[4][4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; j += Vec<T>::W) Vec<T>::ld(buf + i * kGjRow + j, &P[i][j]);
+}
+__device__ __forceinline__ float log_abs_t(float v) { return logf(fabsf(v)); }
+__device__ __forceinline__ double log_abs_t(double v) { return log(fabs(v)); }
+
+// P^-1 into its slot (row-major after the pivot rows) for the rows of C.
+template <typename T>
+__device__ __forceinline__ void gj_put_inverse(const T (&P)[4][4], T *buf) {
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int c = 0; c < 4; c += Vec<T>::W) Vec<T>::st(buf + 4 * kGjRow + 4 * q + c, &P[q][c]);
+  }
+}
+
+// Warp 0, lane = row of D.  Software-pipelined: super-step K updates positions
+// 4..7 first (they are the next pivot block P_{K+1}), the four next pivot rows
+// put that block into slot K + 1 and every lane reads it back and inverts it,
+// then positions 8..31 are updated and the rest of the pivot rows (and, with
+// Publish, P_{K+1}^-1) complete the slot.  With Publish (rows of C trailing on
+// the named barriers) the slot is then published.  log|det P| accumulates in T
+// on every lane; lane 0 returns the sum.
+template <typename T, bool Publish>
 __device__ __forceinline__ double gj_diag(T (&a)[kB], T *slots, T tau, bool &bad) {
   using V = Vec<T>;
   const int lane = threadIdx.x & 31;
-  const int l16 = lane & 15, pq = l16 >> 2, pc = l16 & 3;
-  double ld = 0.0;
+  T ld = T(0);
+  T P[4][4];
+  // super-step 0: pivot rows 0..3 and P_0^-1
+  if (lane < 4) {
+#pragma unroll
+    for (int p = 0; p < kB; p += V::W) V::st(slots + lane * kGjRow + p, a + p);
+  }
+  __syncwarp();
+  gj_load_block<T>(slots, P);
+  {
+    T det;
+    gj_invert4<T>(P, tau, bad, det);
+    if (Publish) {
+      gj_put_inverse<T>(P, slots);
+      __syncwarp();
+      named_arrive(kGjBar0);
+    }
+    ld += log_abs_t(det);
+  }
 #pragma unroll 1
   for (int K = 0; K < kB / 4; ++K) {
     const int c0 = 4 * K;
-    T *buf = slots + K * kGjSlot;
+    const T *buf = slots + K * kGjSlot;
     const bool inK = lane >= c0 && lane < c0 + 4;
-    if (inK) {
-#pragma unroll
-      for (int p = 0; p < kB; p += V::W) V::st(buf + (lane - c0) * kB + p, a + p);
-    }
-    __syncwarp();
-    // P^-1 in 16 lanes: lane (pq, pc) holds entry (pq, pc)
-    T mv = buf[pq * kB + pc];
-    T det = T(1);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const T pk = __shfl_sync(kFull, mv, 5 * k);
-      if (!(finite_t(pk) && pk != T(0))) bad = true;
-      det *= pk;
-      const T rp = rcp_fast(pk);
-      const T prk = __shfl_sync(kFull, mv, 4 * k + pc);
-      const T fik = __shfl_sync(kFull, mv, 4 * pq + k);
-      if (pq > k && pc == k && !(dabs(fik * rp) <= tau)) bad = true;
-      mv = (pq == k) ? ((pc == k) ? rp : prk * rp) : ((pc == k) ? -fik * rp : mv - fik * (prk * rp));
-    }
-    if (lane < 16) buf[kB * 4 + lane] = mv;
-    named_arrive(kGjBar0 + K);  // super-step K is readable by the rows of C
-    if (lane == 0) ld += log_abs(det);
     // g = f P^-1, f = this row's pivot-column entries (unit vector for pivot rows)
     T f[4];
 #pragma unroll
@@ -673,17 +823,43 @@ __device__ __forceinline__ double gj_diag(T (&a)[kB], T *slots, T tau, bool &bad
     for (int c = 0; c < 4; ++c) {
       T acc = T(0);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc += f[q] * __shfl_sync(kFull, mv, 4 * q + c);
+      for (int q = 0; q < 4; ++q) acc += f[q] * P[q][c];
       g[c] = acc;
     }
     if (lane >= c0 + 4) {
 #pragma unroll
-      for (int c = 0; c < 4; ++c)
-        if (!(dabs(g[c]) <= tau)) bad = true;
+      for (int c = 0; c < 4; ++c) bad |= !(dabs(g[c]) <= tau);
     }
-    gj_update<T>(a, g, buf, inK);
+    gj_update_range<4, 8>(a, g, buf, inK);  // a[0..3]: the next pivot block's columns
+    if (K + 1 < kB / 4) {
+      T *nb = slots + (K + 1) * kGjSlot;
+      const bool next = lane >= c0 + 4 && lane < c0 + 8;
+      if (next) {
+#pragma unroll
+        for (int p = 0; p < 4; p += V::W) V::st(nb + (lane - c0 - 4) * kGjRow + p, a + p);
+      }
+      __syncwarp();
+      gj_load_block<T>(nb, P);
+      T det;
+      gj_invert4<T>(P, tau, bad, det);
+      gj_update_range<8, kB>(a, g, buf, inK);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) a[kB - 4 + c] = g[c];
+      if (next) {
+#pragma unroll
+        for (int p = 4; p < kB; p += V::W) V::st(nb + (lane - c0 - 4) * kGjRow + p, a + p);
+      }
+      if (Publish) gj_put_inverse<T>(P, nb);
+      __syncwarp();
+      if (Publish) named_arrive(kGjBar0 + K + 1);  // super-step K + 1 is readable by the rows of C
+      ld += log_abs_t(det);
+    } else {
+      gj_update_range<8, kB>(a, g, buf, inK);
+#pragma unroll
+      for (int c = 0; c < 4; ++c) a[kB - 4 + c] = g[c];
+    }
   }
-  return ld;
+  return lane == 0 ? (double)ld : 0.0;
 }
 
 // Warps 1..7, one row of C per thread (active: the row exists).  rows: this warp
@@ -699,7 +875,7 @@ __device__ __forceinline__ void gj_rows(T (&a)[kB], bool active, bool rows, cons
     const T *buf = slots + K * kGjSlot;
     T pinv[16];
 #pragma unroll
-    for (int q = 0; q < 16; q += V::W) V::ld(buf + kB * 4 + q, pinv + q);
+    for (int q = 0; q < 16; q += V::W) V::ld(buf + 4 * kGjRow + q, pinv + q);
     T g[4];
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -916,19 +1092,22 @@ __device__ __forceinline__ void copy_vals(T *__restrict__ dst, const T *__restri
   }
 }
 
-template <typename T>
+// TC: trailing updates on the tensor cores (FP32 draws, d_p <= 256); a separate
+// instantiation, so that the FFMA path's register tiles do not weigh on it.
+template <typename T, bool TC>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
-    k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, int tc, long n, EliminationPlan ep,
+    k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, long n, EliminationPlan ep,
          const unsigned *__restrict__ sp, const T *__restrict__ theta_sm,
          const T *__restrict__ theta_dm, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
          const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
          double *__restrict__ y, GammaRows rows) {
+  static_assert(!TC || sizeof(T) == 4, "tensor-core path: FP32 draws");
   using V = Vec<T>;
   constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Theta<T> theta{theta_sm, theta_dm, m, P, n};
-  const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0, tc != 0);
+  const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0, TC);
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);  // D^-1, row-major, stride kB
   T *prow = reinterpret_cast<T *>(smem_raw + L.off_prow);
   T *Lp = reinterpret_cast<T *>(smem_raw + L.off_Lp);
@@ -956,20 +1135,18 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   __shared__ uint32_t s_tmem;
   __shared__ __align__(8) uint64_t s_mbar;
   uint32_t mphase = 0;
-  if constexpr (sizeof(T) == 4) {
-    if (tc) {
-      if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
-            smem_u32(&s_tmem)));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-      }
-      if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_mbar)));
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      __syncthreads();
-      asm volatile("tcgen05.fence::after_thread_sync;");
+  if constexpr (TC) {
+    if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(
+          smem_u32(&s_tmem)));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_mbar)));
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
   }
-  const uint32_t tmem = (sizeof(T) == 4 && tc) ? s_tmem : 0u;
+  const uint32_t tmem = TC ? s_tmem : 0u;
 
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
     if (tid == 0) sflag = 0;
@@ -1096,11 +1273,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       for (int r = tid; r < dp; r += blockDim.x)
         z[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
     __syncthreads();
-    if constexpr (sizeof(T) == 4) {
-      if (tc) {
-        // d_p <= 256: the panel Gauss-Jordan holds every row of C; the trailing
-        // update runs on the tensor cores
+    if constexpr (TC) {
+      {
+        // d_p <= 256: warp 0 inverts the diagonal block; the block multipliers
+        // L = C D^-1 and the trailing update run on the tensor cores
         unsigned char *Lt = smem_raw + L.off_Lt, *Ut = smem_raw + L.off_Ut;
+        unsigned char *Dt = smem_raw + L.off_Dt;
         for (int kb = 0; kb < nbk; ++kb) {
           const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
           if (warp == 0) {
@@ -1109,14 +1287,25 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
             T a[kB];
 #pragma unroll
             for (int q = 0; q < kB; ++q) a[q] = rowp[(size_t)dp * q];
-            ld_part += gj_diag<T>(a, prow, tau, bad);
+            ld_part += gj_diag<T, false>(a, prow, tau, bad);
             if (solve) {
 #pragma unroll
               for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = a[q];
             }
+            if (R > 0) {
+              // D^-1 transposed through shared memory: lane n splits column n into
+              // row n of Dt
+#pragma unroll
+              for (int q = 0; q < kB; q += 4) V::st(D + lane * kDs + q, a + q);
+              __syncwarp();
+              float col[kB];
+#pragma unroll
+              for (int q = 0; q < kB; ++q) col[q] = D[q * kDs + lane];
+              write_split_row(Dt, (size_t)kB * 64, lane, col);
+            }
           } else {
-            // while warp 0 factors D: the row panel B (rows k0.., columns r0..),
-            // split, one column per thread
+            // while warp 0 inverts D: the row panel B (rows k0.., columns r0..) and
+            // the rows of C, split, one column of B and one row of C per thread
             for (int t = tid - 32; t < R; t += kThreads - 32) {
               const float *colp = reinterpret_cast<const float *>(A) + (size_t)k0 + (size_t)dp * (r0 + t);
               float b[kB];
@@ -1126,26 +1315,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
                 b[q] = v.x; b[q + 1] = v.y; b[q + 2] = v.z; b[q + 3] = v.w;
               }
               write_split_row(Ut, L.part_U, t, b);
-            }
-            // then the rows of C: C D^-1, trailing warp 0 super-step by super-step
-            const int t = (warp - 1) * 32 + lane;
-            const bool active = t < R;
-            T *rowp = A + (size_t)(r0 + t) + (size_t)dp * k0;
-            T a[kB];
+              const float *rowp = reinterpret_cast<const float *>(A) + (size_t)(r0 + t) + (size_t)dp * k0;
 #pragma unroll
-            for (int q = 0; q < kB; ++q) a[q] = active ? rowp[(size_t)dp * q] : T(0);
-            gj_rows<T>(a, active, (warp - 1) * 32 < R, prow, tau, bad);
-            if (active) {
-              write_split_row(Lt, L.part_L, t, reinterpret_cast<const float(&)[kB]>(a));
-              if (solve) {
-                T acc = T(0);
-#pragma unroll
-                for (int q = 0; q < kB; ++q) acc += a[q] * z[k0 + q];
-                z[r0 + t] -= acc;
-                // keep C D^-1 for the solves
-#pragma unroll
-                for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = a[q];
-              }
+              for (int q = 0; q < kB; ++q) b[q] = rowp[(size_t)dp * q];
+              write_split_row(Lt, L.part_L, t, b);
             }
           }
           if (R > 0) {
@@ -1153,6 +1326,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
             asm volatile("tcgen05.fence::before_thread_sync;");
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;");
+            tc_block_multipliers(reinterpret_cast<float *>(A), dp, k0, r0, R, Lt, L.part_L, Dt, tmem,
+                                 &s_mbar, mphase, tau, reinterpret_cast<float *>(z), solve, bad);
             tc_trailing_update(reinterpret_cast<float *>(A), dp, r0, R, Lt, Ut, L.part_L,
                                L.part_U, tmem, &s_mbar, mphase, bad);
           } else {
@@ -1161,7 +1336,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         }
       }
     }
-    if (!(sizeof(T) == 4 && tc)) for (int kb = 0; kb < nbk; ++kb) {
+    if constexpr (!TC) for (int kb = 0; kb < nbk; ++kb) {
       const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
       const int Rg = R < kGjRows ? R : kGjRows;  // rows of C inside the panel Gauss-Jordan
       // (a) the row panel B (and rows of C beyond Rg) in flight while the panel
@@ -1175,7 +1350,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
 #pragma unroll
         for (int q = 0; q < kB; ++q) a[q] = active ? rowp[(size_t)dp * q] : T(0);
         if (warp == 0)
-          ld_part += gj_diag<T>(a, prow, tau, bad);
+          ld_part += gj_diag<T, true>(a, prow, tau, bad);
         else
           gj_rows<T>(a, active, (warp - 1) * 32 < Rg, prow, tau, bad);
         if (warp == 0) {
@@ -1290,8 +1465,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     }
     __syncthreads();
   }
-  if constexpr (sizeof(T) == 4) {
-    if (tc && warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+  if constexpr (TC) {
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
   }
 }
 
@@ -1565,12 +1740,20 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
                GammaRows rows) {
   // opt in to exactly the shared memory this plan needs (a failure here shows up
   // as a launch error that the engine reports)
-  if (pl.smem > 48 * 1024)
-    cudaFuncSetAttribute(k_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
-  k_lu<T><<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
-                                             pl.vals_smem, pl.tc, n, ep, sp, theta, theta_dm, scratch,
-                                             logdet,
-                                             draw_flags, x, lambda, key, refine, y, rows);
+  auto run = [&](auto kernel) {
+    if (pl.smem > 48 * 1024)
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
+    kernel<<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
+                                              pl.vals_smem, n, ep, sp, theta, theta_dm, scratch,
+                                              logdet, draw_flags, x, lambda, key, refine, y, rows);
+  };
+  if constexpr (sizeof(T) == 4) {
+    if (pl.tc) {
+      run(k_lu<T, true>);
+      return;
+    }
+  }
+  run(k_lu<T, false>);
 }
 
 template <typename T>

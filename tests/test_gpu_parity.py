@@ -498,6 +498,44 @@ def test_benchmark_size_m400(built_lib, precision):
                                atol=1e-6 if precision == "mixed" else 1e-11)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_diagonally_dominant_draws_stay_on_fast_path(built_lib, precision):
+    """The benchmark's parental sets (m = 400) with |coefficients| <= 0.05 and a tight
+    posterior: every (I - Gamma_i) is strictly diagonally dominant, so LU without
+    pivoting is stable and the no-pivot pass must keep every draw (a flagged draw
+    would still be right, through the pivoting redo, and so would hide a fault of
+    the fast path); log|det| and forecasts against the oracle."""
+    import bench
+
+    wl = bench.make_workload(m=400, T=4, seed=11)
+    m, P, n = wl["m"], wl["P"], 1024
+    rng = np.random.default_rng(5)
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents(wl["p"], np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float))
+    s.setDiscountFactors(np.full(m, 0.99), np.full((P, P, m), 0.99))
+    mt = np.asfortranarray(rng.uniform(-0.05, 0.05, size=(P, m)))
+    C = np.asfortranarray(np.repeat((1e-8 * np.eye(P))[:, :, None], m, axis=2))
+    s.setPosteriorParameters(mt, C, np.full(m, 50.0), np.full(m, 1.0))
+    s.setRngState(33, 0)
+    s.computeVBPosterior(n, n)
+    assert s.getStats()["draws_pivoted"] == 0
+    d = s.getDraws()
+    k = 16
+    th = np.asfortranarray(d["thetas"][:, :, :k].transpose(0, 2, 1))
+    ld = oracle.logdet(wl["sp"], th)
+    np.testing.assert_allclose(d["log_dets"][:k], ld, rtol=0,
+                               atol=1e-10 if precision == "fp64" else 1e-4)
+    s.computePrior()
+    x = wl["F_of"](2, False)
+    out = s.computeForecastDebug(n, n, x)
+    assert s.getStats()["draws_pivoted"] == 0
+    lam = np.asfortranarray(out["lambdas"][:, :k].T)
+    th = np.asfortranarray(out["thetas"][:, :, :k].transpose(0, 2, 1))
+    y, _ = oracle.forecast(wl["sp"], lam, th, x, 33, 1)
+    np.testing.assert_allclose(out["y"][:, :k], y, rtol=1e-5 if precision == "mixed" else 1e-9,
+                               atol=1e-6 if precision == "mixed" else 1e-11)
+
+
 def test_dag_parents_have_unit_determinant(built_lib):
     """Parents only among lower-indexed series: (I - Gamma) is unit lower triangular,
     det = 1 for every draw, the weights are uniform and ESS = n."""
