@@ -509,11 +509,13 @@ __device__ __forceinline__ void umma_split_tile(uint32_t d_tmem, uint32_t la, si
 
 // The block multipliers L = C D^-1 (R x 32) on the tensor cores: C split in Lt
 // (rows of C, K-major), D^-1 split in Dt (its columns as rows), one 128-row tile
-// per 32 columns of tensor memory.  Each thread then reads one row of L back,
+// per 32 columns of tensor memory from column kTmemL (the columns below hold the
+// first tile of the trailing update, loaded meanwhile).  Each thread then reads one row of L back,
 // checks |L| <= tau (the no-pivot criterion of the rows of C), writes it split
 // into Lt (in place of C: the MMAs have completed) as the A operand of the
 // trailing update and, when solving, applies it to the right-hand side and keeps
 // it in A.  Warp w reads tile w / 4, lanes 32 (w % 4) ..
+constexpr int kTmemL = 192;
 __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int r0, int R,
                                      unsigned char *Lt, size_t part_L, const unsigned char *Dt,
                                      uint32_t tmem, uint64_t *mbar, uint32_t &mphase, float tau,
@@ -521,7 +523,7 @@ __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     for (int mt = 0; mt < R; mt += 128)
-      umma_split_tile(tmem + (uint32_t)(mt / 128) * kB, smem_u32(Lt) + (uint32_t)(mt / 8) * 512,
+      umma_split_tile(tmem + kTmemL + (uint32_t)(mt / 128) * kB, smem_u32(Lt) + (uint32_t)(mt / 8) * 512,
                       part_L, smem_u32(Dt), (size_t)kB * 64, umma_idesc(kB, false), false);
     asm volatile(
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -542,7 +544,7 @@ __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int 
           "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
           "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
           "=r"(v[31])
-        : "r"(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)tile * kB));
+        : "r"(tmem + ((uint32_t)(quarter * 32) << 16) + kTmemL + (uint32_t)tile * kB));
     asm volatile("tcgen05.wait::ld.sync.aligned;");
     if (row < R) {
       float l[kB];
@@ -569,65 +571,176 @@ __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int 
   asm volatile("tcgen05.fence::after_thread_sync;");
 }
 
-// E[r0:, r0:] (R x R, leading dimension dp) -= L U on the tensor cores, 128-row
-// tiles (rows beyond R are padding: loaded as 0, never stored).  E goes through
-// tensor memory (tmem: 128 lanes x up to 256 columns of this CTA); thread 0
-// issues the 12 MMAs of a tile and commits them to mbar; every thread waits with
-// a bounded spin (a timeout sets bad, and the draw is redone by the pivoting
-// pass).  All 8 warps load and store: warp w handles lanes 32 (w % 4) .. and the
-// column half w / 4.
+// Named barriers of the tensor-core path (barrier 0 is __syncthreads; 1..8 are
+// the Gauss-Jordan super-steps of the FFMA path).
+constexpr int kBarRest = 9;       // warps 1..7 (224 threads)
+constexpr int kBarQuarter0 = 10;  // warps 0 and 4 (64 threads): tensor-memory lanes 0..31
+__device__ __forceinline__ void named_arrive_n(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ void named_sync_n(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// Rows [row0, row0 + 32) of E (this warp's lanes of tensor memory), columns
+// [cb, ce) in 16-column chunks: global -> registers -> tensor memory (rows at or
+// beyond R load as 0), or back (rows beyond R are not stored).
+__device__ __forceinline__ void e_to_tmem(const float *E, int dp, int R, int row, int cb, int ce,
+                                          uint32_t tlane) {
+  for (int c0 = cb; c0 < ce; c0 += 16) {
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      v[j] = __float_as_uint(row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f);
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(tlane + (uint32_t)c0),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+        "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+        "r"(v[15]));
+  }
+  asm volatile("tcgen05.wait::st.sync.aligned;");
+}
+__device__ __forceinline__ void tmem_to_e(float *E, int dp, int R, int row, int cb, int ce,
+                                          uint32_t tlane) {
+  for (int c0 = cb; c0 < ce; c0 += 16) {
+    uint32_t v[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+          "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(tlane + (uint32_t)c0));
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+    if (row < R) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) E[(size_t)row + (size_t)dp * (c0 + j)] = __uint_as_float(v[j]);
+    }
+  }
+}
+
+// This warp's columns of a 128-row tile of E: lanes 32..127 split the columns in
+// halves between warps q and q + 4; lanes 0..31 (the next diagonal block's rows)
+// give warp 0 the first 32 columns and warp 4 the rest (with all columns in the
+// preload and in the second tile, where warp 0 takes no part).
+__device__ __forceinline__ void e_columns(int warp, int R, bool with_warp0, int &cb, int &ce) {
+  const int quarter = warp & 3, hc = R / 2;
+  if (quarter == 0) {
+    cb = (warp == 0 || !with_warp0) ? 0 : kB;
+    ce = warp == 0 ? kB : R;
+  } else {
+    cb = (warp >> 2) * hc;
+    ce = cb + hc;
+  }
+}
+
+// The first 128-row tile of E[r0:, r0:] into tensor memory (columns 0 .. R-1),
+// by warps 1..7 while warp 0 inverts the diagonal block.  after_d: warp 4 first
+// waits for warp 0 to have read the diagonal block out of lanes 0..31 (the
+// previous trailing update had no second tile, which would have waited for it).
+__device__ __forceinline__ void tc_preload_tile0(const float *A, int dp, int r0, int R,
+                                                 uint32_t tmem, bool after_d) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, quarter = warp & 3;
+  const float *E = A + (size_t)r0 + (size_t)dp * r0;
+  int cb, ce;
+  e_columns(warp, R, false, cb, ce);
+  if (warp == 4 && after_d) {
+    named_sync_n(kBarQuarter0, 64);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+  }
+  if (quarter * 32 < R)
+    e_to_tmem(E, dp, R, quarter * 32 + lane, cb, ce, tmem + ((uint32_t)(quarter * 32) << 16));
+}
+
+// E[r0:, r0:] (R x R, leading dimension dp, R <= 192) -= L U on the tensor cores,
+// 128-row tiles (rows beyond R are padding: loaded as 0, never stored).  E goes
+// through tensor memory (tmem: 128 lanes x R columns of this CTA; the first tile
+// was preloaded); one thread issues the 12 MMAs of a tile and commits them to
+// mbar; the waiting threads spin with a bound (a timeout sets bad, and the draw
+// is redone by the pivoting pass).  Warp w moves lanes 32 (w % 4) .. (columns:
+// e_columns).
+// Look-ahead: warp 0 takes part in the first tile only.  It reads the next
+// diagonal block (rows and columns r0 .. r0 + 31 of the updated matrix) out of
+// tensor memory into dnext (shared, row-major, stride kDs) instead of storing it
+// and returns, so that the next panel's Gauss-Jordan overlaps the rest of this
+// update.  Warps 1..7 do the second tile (R > 128) alone and meet on a named
+// barrier at the end, after which their stores are visible to each other.
 __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
                                    const unsigned char *Lt, const unsigned char *Ut,
                                    size_t part_L, size_t part_U, uint32_t tmem, uint64_t *mbar,
-                                   uint32_t &mphase, bool &bad) {
+                                   uint32_t &mphase, bool &bad, float *dnext) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, half = warp >> 2, hc = R / 2;
+  const int quarter = warp & 3;
   float *E = A + (size_t)r0 + (size_t)dp * r0;
   const uint32_t idesc = umma_idesc(R);
-  for (int mt = 0; mt < R; mt += 128) {
-    const int row = mt + quarter * 32 + lane;
-    const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
-    for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 16) {
-      uint32_t v[16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j)
-        v[j] = __float_as_uint(row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f);
-      asm volatile(
-          "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
-          "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(tlane + (uint32_t)c0),
-          "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
-          "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
-          "r"(v[15]));
-    }
-    asm volatile("tcgen05.wait::st.sync.aligned;");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
+  const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
+  int cb, ce;
+  e_columns(warp, R, true, cb, ce);
+  // ---- tile 0: rows 0..127 (in tensor memory already)
+  {
+    const int row = quarter * 32 + lane;
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      umma_split_tile(tmem, smem_u32(Lt) + (uint32_t)(mt / 8) * 512, part_L, smem_u32(Ut), part_U,
+      umma_split_tile(tmem, smem_u32(Lt), part_L, smem_u32(Ut), part_U, idesc, true);
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(mbar)));
+    }
+    mma_wait(mbar, mphase, bad);
+    if (warp == 0) {
+      uint32_t v[kB];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+            "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+            "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+            "=r"(v[31])
+          : "r"(tlane));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+      for (int q = 0; q < kB; q += 4)
+        *reinterpret_cast<uint4 *>(dnext + lane * kDs + q) = make_uint4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      // warp 4 may overwrite lanes 0..31 now: it waits for this in the second tile
+      // (R > 128) or else in the next panel's preload (there is one when R > 32)
+      if (R > kB) named_arrive_n(kBarQuarter0, 64);
+      if (R > 128) mphase ^= 1u;  // the second tile's commit, not waited for here
+      __syncwarp();
+      return;
+    }
+    if (quarter * 32 < R) tmem_to_e(E, dp, R, row, cb, ce, tlane);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    named_sync_n(kBarRest, kThreads - 32);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+  }
+  // ---- tile 1: rows 128..R-1 (warps 1..7; lanes 0..31 all columns by warp 4)
+  if (R > 128) {
+    const int row = 128 + quarter * 32 + lane;
+    const int cb1 = quarter == 0 ? 0 : cb, ce1 = quarter == 0 ? R : ce;
+    if (warp == 4) {
+      named_sync_n(kBarQuarter0, 64);
+      asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+    if (128 + quarter * 32 < R) e_to_tmem(E, dp, R, row, cb1, ce1, tlane);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    named_sync_n(kBarRest, kThreads - 32);
+    if (tid == 32) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      umma_split_tile(tmem, smem_u32(Lt) + (uint32_t)(128 / 8) * 512, part_L, smem_u32(Ut), part_U,
                       idesc, true);
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
               smem_u32(mbar)));
     }
     mma_wait(mbar, mphase, bad);
-    for (int c0 = half * hc; c0 < (half + 1) * hc; c0 += 16) {
-      uint32_t v[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-          : "r"(tlane + (uint32_t)c0));
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (row < R) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) E[(size_t)row + (size_t)dp * (c0 + j)] = __uint_as_float(v[j]);
-      }
-    }
+    if (128 + quarter * 32 < R) tmem_to_e(E, dp, R, row, cb1, ce1, tlane);
     asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
+    named_sync_n(kBarRest, kThreads - 32);
     asm volatile("tcgen05.fence::after_thread_sync;");
   }
 }
@@ -1092,7 +1205,7 @@ __device__ __forceinline__ void copy_vals(T *__restrict__ dst, const T *__restri
   }
 }
 
-// TC: trailing updates on the tensor cores (FP32 draws, d_p <= 256); a separate
+// TC: trailing updates on the tensor cores (FP32 draws, d_p <= 224); a separate
 // instantiation, so that the FFMA path's register tiles do not weigh on it.
 template <typename T, bool TC>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
@@ -1130,7 +1243,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   const bool solve = (x != nullptr);
   const T tau = (T)kPivotThreshold;
   __shared__ int sflag;
-  // tensor-core trailing updates (FP32 draws, d_p <= 256): 256 columns of tensor
+  // tensor-core trailing updates (FP32 draws, d_p <= 224): 256 columns of tensor
   // memory for this CTA and the MMA completion barrier
   __shared__ uint32_t s_tmem;
   __shared__ __align__(8) uint64_t s_mbar;
@@ -1275,18 +1388,28 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     __syncthreads();
     if constexpr (TC) {
       {
-        // d_p <= 256: warp 0 inverts the diagonal block; the block multipliers
-        // L = C D^-1 and the trailing update run on the tensor cores
+        // d_p <= 224: warp 0 inverts the diagonal block; the block multipliers
+        // L = C D^-1 and the trailing update run on the tensor cores.  Warp 0
+        // leaves each trailing update after its first tile with the next diagonal
+        // block, so that its Gauss-Jordan overlaps the rest of the update and the
+        // other warps' splits of the next panel.
         unsigned char *Lt = smem_raw + L.off_Lt, *Ut = smem_raw + L.off_Ut;
         unsigned char *Dt = smem_raw + L.off_Dt;
         for (int kb = 0; kb < nbk; ++kb) {
           const int k0 = kb * kB, r0 = k0 + kB, R = dp - r0;
           if (warp == 0) {
-            // the rows of D: D^-1 by the warp-synchronous Gauss-Jordan
+            // the rows of D (the first panel's from the core, later ones as the
+            // previous trailing update left them in shared memory): D^-1 by the
+            // warp-synchronous Gauss-Jordan
             T *rowp = A + (size_t)(k0 + lane) + (size_t)dp * k0;
             T a[kB];
+            if (kb == 0) {
 #pragma unroll
-            for (int q = 0; q < kB; ++q) a[q] = rowp[(size_t)dp * q];
+              for (int q = 0; q < kB; ++q) a[q] = rowp[(size_t)dp * q];
+            } else {
+#pragma unroll
+              for (int q = 0; q < kB; q += 4) V::ld(D + lane * kDs + q, a + q);
+            }
             ld_part += gj_diag<T, false>(a, prow, tau, bad);
             if (solve) {
 #pragma unroll
@@ -1304,21 +1427,29 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
               write_split_row(Dt, (size_t)kB * 64, lane, col);
             }
           } else {
-            // while warp 0 inverts D: the row panel B (rows k0.., columns r0..) and
-            // the rows of C, split, one column of B and one row of C per thread
-            for (int t = tid - 32; t < R; t += kThreads - 32) {
-              const float *colp = reinterpret_cast<const float *>(A) + (size_t)k0 + (size_t)dp * (r0 + t);
-              float b[kB];
+            // while warp 0 inverts D: the first tile of the trailing update into
+            // tensor memory, and the row panel B (rows k0.., columns r0..) and the
+            // rows of C, split, one column of B and one row of C per thread of
+            // warps 1..3, 5..7 (warp 4 loads all columns of lanes 0..31)
+            if (R > 0)
+              tc_preload_tile0(reinterpret_cast<const float *>(A), dp, r0, R, tmem,
+                               kb > 0 && R + kB <= 128);
+            if (warp != 4) {
+              const int s0 = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;
+              for (int t = s0; t < R; t += kThreads - 64) {
+                const float *colp = reinterpret_cast<const float *>(A) + (size_t)k0 + (size_t)dp * (r0 + t);
+                float b[kB];
 #pragma unroll
-              for (int q = 0; q < kB; q += 4) {
-                const float4 v = *reinterpret_cast<const float4 *>(colp + q);
-                b[q] = v.x; b[q + 1] = v.y; b[q + 2] = v.z; b[q + 3] = v.w;
+                for (int q = 0; q < kB; q += 4) {
+                  const float4 v = *reinterpret_cast<const float4 *>(colp + q);
+                  b[q] = v.x; b[q + 1] = v.y; b[q + 2] = v.z; b[q + 3] = v.w;
+                }
+                write_split_row(Ut, L.part_U, t, b);
+                const float *rowp = reinterpret_cast<const float *>(A) + (size_t)(r0 + t) + (size_t)dp * k0;
+#pragma unroll
+                for (int q = 0; q < kB; ++q) b[q] = rowp[(size_t)dp * q];
+                write_split_row(Lt, L.part_L, t, b);
               }
-              write_split_row(Ut, L.part_U, t, b);
-              const float *rowp = reinterpret_cast<const float *>(A) + (size_t)(r0 + t) + (size_t)dp * k0;
-#pragma unroll
-              for (int q = 0; q < kB; ++q) b[q] = rowp[(size_t)dp * q];
-              write_split_row(Lt, L.part_L, t, b);
             }
           }
           if (R > 0) {
@@ -1329,7 +1460,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
             tc_block_multipliers(reinterpret_cast<float *>(A), dp, k0, r0, R, Lt, L.part_L, Dt, tmem,
                                  &s_mbar, mphase, tau, reinterpret_cast<float *>(z), solve, bad);
             tc_trailing_update(reinterpret_cast<float *>(A), dp, r0, R, Lt, Ut, L.part_L,
-                               L.part_U, tmem, &s_mbar, mphase, bad);
+                               L.part_U, tmem, &s_mbar, mphase, bad, reinterpret_cast<float *>(D));
           } else {
             __syncthreads();
           }
@@ -1703,9 +1834,10 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv) {
   pl.block = kThreads;
   // value slots in shared memory when that keeps the target occupancy
   const int target = sizeof(T) == 4 ? 2 : 1;
-  // tensor-core trailing updates for FP32 draws while the 32-wide panel holds every
-  // row of the core (d_p <= 256: N <= 224 columns in 256 columns of tensor memory)
-  pl.tc = (sizeof(T) == 4 && pl.dp <= 256) ? 1 : 0;
+  // tensor-core path for FP32 draws while the trailing update's first tile (R <= 192
+  // columns) and the block multipliers (64 columns) fit the CTA's 256 columns of
+  // tensor memory together: d_p <= 224
+  pl.tc = (sizeof(T) == 4 && pl.dp <= 224) ? 1 : 0;
   const size_t with_vals = Smem(pl.dp, m, sizeof(T), nv, pl.tc != 0).total;
   pl.vals_smem = (nv > 0 && with_vals <= smem_budget(target)) ? 1 : 0;
   pl.smem = Smem(pl.dp, m, sizeof(T), pl.vals_smem ? nv : 0, pl.tc != 0).total;
