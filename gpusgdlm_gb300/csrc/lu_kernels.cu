@@ -53,6 +53,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kDs = 36;  // row stride of D^-1 in shared memory (16-byte rows, 4-way store conflicts)
 constexpr int kUs = 36;  // stride of the row panel B, stored column by column: B[c][t] at t*kUs + c
 constexpr int kGjRows = 224;  // rows of C the panel Gauss-Jordan holds (warps 1..7)
+constexpr int kLevFlight = 8;  // chunks of a sparse level in flight per warp
 // one super-step of the panel Gauss-Jordan in shared memory: the pivot rows
 // (row q, position p at kGjRow q + p; the padding keeps the four writers' 16-byte
 // stores on distinct banks), then P^-1 (entry (q, c) at 4 kGjRow + 4q + c)
@@ -1313,7 +1314,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       __syncthreads();
       // new entries: warp w takes chunks c_begin + w + 8i; lane l prefetches the term
       // offsets of its warp's chunk i = base + l, so that the term loads do not wait
-      // on a dependent load; four chunks are in flight at a time
+      // on a dependent load; kLevFlight chunks are in flight at a time (the plan's
+      // words come from L2: the rounds are latency-bound)
       const int c_begin = ep.lev_chunk[lev], c_end = ep.lev_chunk[lev + 1];
       const int n_w = (c_begin + warp < c_end) ? (c_end - c_begin - warp + kWarps - 1) / kWarps : 0;
       for (int base = 0; base < n_w; base += 32) {
@@ -1324,35 +1326,42 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
           my_t1 = ep.chunk_tofs[ci + 1];
         }
         const int n_here = min(32, n_w - base);
-        for (int i0 = 0; i0 < n_here; i0 += 4) {
-          unsigned e[4];
-          const unsigned *tp[4];
-          int K[4];
+        for (int i0 = 0; i0 < n_here; i0 += kLevFlight) {
+          unsigned e[kLevFlight];
+          int toff[kLevFlight], K[kLevFlight];
 #pragma unroll
-          for (int h = 0; h < 4; ++h) {
+          for (int h = 0; h < kLevFlight; ++h) {
             const int ii = i0 + h;
             const int t0 = __shfl_sync(kFull, my_t0, ii & 31);
             const int t1 = __shfl_sync(kFull, my_t1, ii & 31);
             const bool ok = ii < n_here;
             const int ch = c_begin + warp + (base + ii) * kWarps;
-            e[h] = ok ? ep.ent[(size_t)ch * 32 + lane] : kSlotNone;  // none: no store, base 0
+            e[h] = ok ? __ldg(ep.ent + (size_t)ch * 32 + lane) : kSlotNone;  // none: no store, base 0
             K[h] = ok ? (t1 - t0) >> 5 : 0;
-            tp[h] = ep.terms + t0 + lane;
+            toff[h] = t0 + lane;
           }
-          T v[4];
+          // the first term's word is loaded before the entry word is first used, so
+          // that the two loads from L2 overlap (most entries have one term)
+          unsigned w0[kLevFlight];
 #pragma unroll
-          for (int h = 0; h < 4; ++h) v[h] = vals[hi16(e[h])];
-          const int Kmax = max(max(K[0], K[1]), max(K[2], K[3]));
-#pragma unroll 2
-          for (int k = 0; k < Kmax; ++k) {
-            unsigned w[4];
+          for (int h = 0; h < kLevFlight; ++h) w0[h] = K[h] > 0 ? __ldg(ep.terms + toff[h]) : 0u;
+          T v[kLevFlight];
+          int Kmax = 0;
 #pragma unroll
-            for (int h = 0; h < 4; ++h) w[h] = (k < K[h]) ? tp[h][32 * k] : 0u;
+          for (int h = 0; h < kLevFlight; ++h) {
+            v[h] = vals[hi16(e[h])] - vals[lo16(w0[h])] * vals[hi16(w0[h])];
+            Kmax = max(Kmax, K[h]);
+          }
+#pragma unroll 1
+          for (int k = 1; k < Kmax; ++k) {
+            unsigned w[kLevFlight];
 #pragma unroll
-            for (int h = 0; h < 4; ++h) v[h] -= vals[lo16(w[h])] * vals[hi16(w[h])];
+            for (int h = 0; h < kLevFlight; ++h) w[h] = (k < K[h]) ? __ldg(ep.terms + toff[h] + 32 * k) : 0u;
+#pragma unroll
+            for (int h = 0; h < kLevFlight; ++h) v[h] -= vals[lo16(w[h])] * vals[hi16(w[h])];
           }
 #pragma unroll
-          for (int h = 0; h < 4; ++h)
+          for (int h = 0; h < kLevFlight; ++h)
             if ((unsigned)lo16(e[h]) != kSlotNone) vals[lo16(e[h])] = v[h];
         }
       }
