@@ -1018,6 +1018,12 @@ __device__ void be_back_solve(const T *__restrict__ A, int dp, T *v, T *bsum) {
   const int tid = threadIdx.x, lane = tid & 31;
   for (int kb = dp / kB - 1; kb >= 0; --kb) {
     const int k0 = kb * kB;
+    // this thread's first row above the block: its coefficients do not depend on
+    // x_k, so their loads are issued before the barrier that publishes x_k
+    const bool first = tid < k0;
+    T b[kB];
+#pragma unroll
+    for (int c = 0; c < kB; ++c) b[c] = first ? A[(size_t)tid + (size_t)dp * (k0 + c)] : T(0);
     if (tid < 32) {
       T dinv[kB];
 #pragma unroll
@@ -1030,8 +1036,13 @@ __device__ void be_back_solve(const T *__restrict__ A, int dp, T *v, T *bsum) {
     }
     __syncthreads();
     if (tid < 32) v[k0 + tid] = bsum[tid];
-    for (int r = tid; r < k0; r += blockDim.x) {
-      T b[kB];
+    if (first) {
+      T acc = T(0);
+#pragma unroll
+      for (int c = 0; c < kB; ++c) acc += b[c] * bsum[c];
+      v[tid] -= acc;
+    }
+    for (int r = tid + blockDim.x; r < k0; r += blockDim.x) {
 #pragma unroll
       for (int c = 0; c < kB; ++c) b[c] = A[(size_t)r + (size_t)dp * (k0 + c)];
       T acc = T(0);
@@ -1127,15 +1138,21 @@ __device__ __forceinline__ int lo16(unsigned w) { return (int)(w & 0xFFFFu); }
 __device__ __forceinline__ int hi16(unsigned w) { return (int)(w >> 16); }
 
 // Forward program of one level on the node-indexed vector z: z[r] -= L[r][t] z[t].
+// A node's program words come from L2; they are gathered eight at a time so that
+// their loads overlap (a node has about ten terms).
 template <typename T>
 __device__ __forceinline__ void level_forward(const EliminationPlan &ep, int lev, const T *vals,
                                               T *z) {
   for (int g = ep.lev_fwd_nodes[lev] + threadIdx.x; g < ep.lev_fwd_nodes[lev + 1]; g += blockDim.x) {
-    const int r = ep.fwd_node[g];
+    const int r = __ldg(ep.fwd_node + g), q1 = __ldg(ep.fwd_ptr + g + 1);
     T acc = z[r];
-    for (int q = ep.fwd_ptr[g]; q < ep.fwd_ptr[g + 1]; ++q) {
-      const unsigned f = ep.fwd[q];
-      acc -= vals[lo16(f)] * z[hi16(f)];
+    for (int q = __ldg(ep.fwd_ptr + g); q < q1; q += 8) {
+      unsigned f[8];
+#pragma unroll
+      for (int h = 0; h < 8; ++h) f[h] = q + h < q1 ? __ldg(ep.fwd + q + h) : 0u;
+#pragma unroll
+      for (int h = 0; h < 8; ++h)
+        if (q + h < q1) acc -= vals[lo16(f[h])] * z[hi16(f[h])];
     }
     z[r] = acc;
   }
@@ -1191,6 +1208,49 @@ __device__ void residual(int m, int P, long n, long i, GammaRows rows, Theta<T> 
     res[r] = v;
   }
   __syncthreads();
+}
+
+// The refinement's right-hand side, out = nu - (I - Gamma) y rounded to T, for the
+// fast pass.  FP64 draws: the FP64 residual above.  FP32 draws: double-float
+// arithmetic in FP32 (FP64 is a narrow pipe on this GPU) -- nu_r - y_r in FP64,
+// split into two floats; each product theta y is exact as p + e with
+// e = fma(theta, y, -p); the sum is compensated with Knuth's TwoSum.  About 48
+// bits, ample for a residual that is rounded to FP32 afterwards.
+template <typename T>
+__device__ void residual_rhs(int m, int P, long n, long i, GammaRows rows, Theta<T> theta,
+                             const double *nu, const T *y, double *res, T *out) {
+  if constexpr (sizeof(T) == 8) {
+    residual<T>(m, P, n, i, rows, theta, nu, y, res);
+    for (int r = threadIdx.x; r < m; r += blockDim.x) out[r] = (T)res[r];
+  } else {
+    for (int r = threadIdx.x; r < m; r += blockDim.x) {
+      const double v0 = nu[r] - (double)y[r];
+      float sh = (float)v0, sl = (float)(v0 - (double)sh);
+      const int q1 = __ldg(rows.rowptr + r + 1);
+      for (int q0 = __ldg(rows.rowptr + r); q0 < q1; q0 += 8) {
+        int2 ec[8];
+#pragma unroll
+        for (int h = 0; h < 8; ++h) ec[h] = (q0 + h < q1) ? __ldg(rows.ent + q0 + h) : make_int2(-1, 0);
+        float th[8];
+#pragma unroll
+        for (int h = 0; h < 8; ++h) th[h] = ec[h].x >= 0 ? (float)theta.at(i, ec[h].x) : 0.f;
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+          if (ec[h].x < 0) continue;
+          // explicitly rounded operations: no contraction into FMAs, which would
+          // break the error-free transformations
+          const float yc = (float)y[ec[h].y];
+          const float pr = __fmul_rn(th[h], yc), pe = fmaf(th[h], yc, -pr);
+          const float t = __fadd_rn(sh, pr), bb = __fsub_rn(t, sh);
+          const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(pr, bb));
+          sh = t;
+          sl = __fadd_rn(sl, __fadd_rn(err, pe));
+        }
+      }
+      out[r] = (T)(sh + sl);
+    }
+    __syncthreads();
+  }
 }
 
 // Copies n values between shared and global memory (16-byte vectors; both
@@ -1585,8 +1645,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       __syncthreads();
       levels_backward<T>(ep, vals, zf, yf);
       if (refine) {
-        residual<T>(m, P, n, i, rows, theta, nu, yf, res);
-        for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)res[r];
+        residual_rhs<T>(m, P, n, i, rows, theta, nu, yf, res, zf);
         __syncthreads();
         levels_forward<T>(ep, vals, zf);
         for (int r = tid; r < dp; r += blockDim.x)
