@@ -625,9 +625,10 @@ __device__ __forceinline__ void tmem_to_e(float *E, int dp, int R, int row, int 
 // halves between warps q and q + 4; lanes 0..31 (the next diagonal block's rows)
 // give warp 0 the first 32 columns and warp 4 the rest (with all columns in the
 // preload and in the second tile, where warp 0 takes no part).
-__device__ __forceinline__ void e_columns(int warp, int R, bool with_warp0, int &cb, int &ce) {
+__device__ __forceinline__ void e_columns(int warp, int R, bool with_warp0, int &cb, int &ce,
+                                          bool halves = false) {
   const int quarter = warp & 3, hc = R / 2;
-  if (quarter == 0) {
+  if (quarter == 0 && !halves) {
     cb = (warp == 0 || !with_warp0) ? 0 : kB;
     ce = warp == 0 ? kB : R;
   } else {
@@ -661,23 +662,27 @@ __device__ __forceinline__ void tc_preload_tile0(const float *A, int dp, int r0,
 // mbar; the waiting threads spin with a bound (a timeout sets bad, and the draw
 // is redone by the pivoting pass).  Warp w moves lanes 32 (w % 4) .. (columns:
 // e_columns).
-// Look-ahead: warp 0 takes part in the first tile only.  It reads the next
-// diagonal block (rows and columns r0 .. r0 + 31 of the updated matrix) out of
-// tensor memory into dnext (shared, row-major, stride kDs) instead of storing it
-// and returns, so that the next panel's Gauss-Jordan overlaps the rest of this
-// update.  Warps 1..7 do the second tile (R > 128) alone and meet on a named
-// barrier at the end, after which their stores are visible to each other.
+// Look-ahead (R <= 128, one tile): warp 0 reads the next diagonal block (rows
+// and columns r0 .. r0 + 31 of the updated matrix) out of tensor memory into
+// dnext (shared, row-major, stride kDs) instead of storing it and returns, so that
+// the next panel's Gauss-Jordan overlaps the rest of this update and the next
+// panel's preload and splits; warps 1..7 meet on a named barrier at the end.
+// With two tiles (R > 128) warp 4 would carry lanes 0..31 alone through both
+// tiles while warp 0 waits for the panel anyway, so there all eight warps share
+// the work (lanes 0..31 in halves, as the other quarters), warp 0 stashes the
+// next diagonal block from the first tile, and the update ends on __syncthreads.
 __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
                                    const unsigned char *Lt, const unsigned char *Ut,
                                    size_t part_L, size_t part_U, uint32_t tmem, uint64_t *mbar,
                                    uint32_t &mphase, bool &bad, float *dnext) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3;
+  const bool two = R > 128;
   float *E = A + (size_t)r0 + (size_t)dp * r0;
   const uint32_t idesc = umma_idesc(R);
   const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
   int cb, ce;
-  e_columns(warp, R, true, cb, ce);
+  e_columns(warp, R, true, cb, ce, two);
   // ---- tile 0: rows 0..127 (in tensor memory already)
   {
     const int row = quarter * 32 + lane;
@@ -706,31 +711,32 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
 #pragma unroll
       for (int q = 0; q < kB; q += 4)
         *reinterpret_cast<uint4 *>(dnext + lane * kDs + q) = make_uint4(v[q], v[q + 1], v[q + 2], v[q + 3]);
-      asm volatile("tcgen05.fence::before_thread_sync;");
-      // warp 4 may overwrite lanes 0..31 now: it waits for this in the second tile
-      // (R > 128) or else in the next panel's preload (there is one when R > 32)
-      if (R > kB) named_arrive_n(kBarQuarter0, 64);
-      if (R > 128) mphase ^= 1u;  // the second tile's commit, not waited for here
-      __syncwarp();
-      return;
+      if (!two) {
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        // warp 4 may overwrite lanes 0..31 now, in the next panel's preload (there
+        // is one when R > 32)
+        if (R > kB) named_arrive_n(kBarQuarter0, 64);
+        __syncwarp();
+        return;
+      }
+      tmem_to_e(E, dp, R, row, kB, ce, tlane);  // the rest of warp 0's half
+    } else if (quarter * 32 < R) {
+      tmem_to_e(E, dp, R, row, cb, ce, tlane);
     }
-    if (quarter * 32 < R) tmem_to_e(E, dp, R, row, cb, ce, tlane);
     asm volatile("tcgen05.fence::before_thread_sync;");
-    named_sync_n(kBarRest, kThreads - 32);
+    if (two)
+      __syncthreads();
+    else
+      named_sync_n(kBarRest, kThreads - 32);
     asm volatile("tcgen05.fence::after_thread_sync;");
   }
-  // ---- tile 1: rows 128..R-1 (warps 1..7; lanes 0..31 all columns by warp 4)
-  if (R > 128) {
+  // ---- tile 1: rows 128..R-1, all eight warps
+  if (two) {
     const int row = 128 + quarter * 32 + lane;
-    const int cb1 = quarter == 0 ? 0 : cb, ce1 = quarter == 0 ? R : ce;
-    if (warp == 4) {
-      named_sync_n(kBarQuarter0, 64);
-      asm volatile("tcgen05.fence::after_thread_sync;");
-    }
-    if (128 + quarter * 32 < R) e_to_tmem(E, dp, R, row, cb1, ce1, tlane);
+    if (128 + quarter * 32 < R) e_to_tmem(E, dp, R, row, cb, ce, tlane);
     asm volatile("tcgen05.fence::before_thread_sync;");
-    named_sync_n(kBarRest, kThreads - 32);
-    if (tid == 32) {
+    __syncthreads();
+    if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       umma_split_tile(tmem, smem_u32(Lt) + (uint32_t)(128 / 8) * 512, part_L, smem_u32(Ut), part_U,
                       idesc, true);
@@ -739,9 +745,9 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
               smem_u32(mbar)));
     }
     mma_wait(mbar, mphase, bad);
-    if (128 + quarter * 32 < R) tmem_to_e(E, dp, R, row, cb1, ce1, tlane);
+    if (128 + quarter * 32 < R) tmem_to_e(E, dp, R, row, cb, ce, tlane);
     asm volatile("tcgen05.fence::before_thread_sync;");
-    named_sync_n(kBarRest, kThreads - 32);
+    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
   }
 }
