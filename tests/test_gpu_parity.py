@@ -536,6 +536,51 @@ def test_diagonally_dominant_draws_stay_on_fast_path(built_lib, precision):
                                atol=1e-6 if precision == "mixed" else 1e-11)
 
 
+@pytest.mark.parametrize("m", [40, 100, 150, 190, 224, 240, 300])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_dense_core_sizes(built_lib, precision, m):
+    """No sparse levels, so the dense core is all m nodes: d_p = 64 .. 320 covers the
+    panel schedules of the tensor-core LU (one 128-row tile from the start at
+    d_p = 160, two tiles at 192 and 224) and the FFMA instantiation (d_p = 256, 320,
+    where the panel Gauss-Jordan also hands rows beyond 224 to the separate
+    multiplier GEMM).  Diagonally dominant draws: no draw may be redone with
+    pivoting; log|det| and forecasts against the oracle."""
+    import bench
+
+    wl = bench.make_workload(m=m, T=4, seed=100 + m)
+    P, n = wl["P"], 256
+    rng = np.random.default_rng(m)
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents(wl["p"], np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float))
+    s.setEliminationLevels(0)
+    assert s.getEliminationInfo()["core_n"] == m
+    s.setDiscountFactors(np.full(m, 0.99), np.full((P, P, m), 0.99))
+    mt = np.asfortranarray(rng.uniform(-0.05, 0.05, size=(P, m)))
+    C = np.asfortranarray(np.repeat((1e-8 * np.eye(P))[:, :, None], m, axis=2))
+    s.setPosteriorParameters(mt, C, np.full(m, 50.0), np.full(m, 1.0))
+    s.setRngState(44, 0)
+    s.computeVBPosterior(n, n)
+    assert s.getStats()["draws_pivoted"] == 0
+    d = s.getDraws()
+    k = 12
+    th = np.asfortranarray(d["thetas"][:, :, :k].transpose(0, 2, 1))
+    ld = oracle.logdet(wl["sp"], th)
+    np.testing.assert_allclose(d["log_dets"][:k], ld, rtol=0,
+                               atol=1e-10 if precision == "fp64" else 1e-4)
+    s.computePrior()
+    x = wl["F_of"](2, False)
+    out = s.computeForecastDebug(n, n, x)
+    assert s.getStats()["draws_pivoted"] == 0
+    lam = np.asfortranarray(out["lambdas"][:, :k].T)
+    th = np.asfortranarray(out["thetas"][:, :, :k].transpose(0, 2, 1))
+    y, _ = oracle.forecast(wl["sp"], lam, th, x, 44, 1)
+    # mixed: the oracle regenerates nu's normals in FP64, the GPU by FP32 Box-Muller
+    # (absolute error ~1e-6); that error, carried through (I - Gamma)^-1, bounds the
+    # agreement of the refined solves, hence the absolute term
+    np.testing.assert_allclose(out["y"][:, :k], y, rtol=1e-5 if precision == "mixed" else 1e-9,
+                               atol=5e-6 if precision == "mixed" else 1e-11)
+
+
 def test_dag_parents_have_unit_determinant(built_lib):
     """Parents only among lower-indexed series: (I - Gamma) is unit lower triangular,
     det = 1 for every draw, the weights are uniform and ESS = n."""
