@@ -72,8 +72,9 @@ __global__ void __launch_bounds__(kSampleThreads)
         z[4 * q] = z[4 * q + 1] = z[4 * q + 2] = z[4 * q + 3] = T(0);
       }
     }
-    // theta = m + (U' z) / sqrt(s lambda)   (makeVB_MVN, kernel_functions.cuh:72-83)
-    const T den = dev_sqrt((T)sj * lam);
+    // theta = m + (U' z) / sqrt(s lambda)   (makeVB_MVN, kernel_functions.cuh:72-83);
+    // one reciprocal instead of P divisions (within 1-2 ulp of the quotients)
+    const T rden = T(1) / dev_sqrt((T)sj * lam);
     T *row = stage + (size_t)threadIdx.x * P;
 #pragma unroll
     for (int k = 0; k < PMAX; ++k) {
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(kSampleThreads)
         T acc = T(0);
 #pragma unroll
         for (int l = 0; l <= k; ++l) acc += Us[l + P * k] * z[l];
-        row[k] = ms[k] + acc / den;
+        row[k] = ms[k] + acc * rden;
       }
     }
     lambda[(size_t)j * n + i] = lam;
@@ -91,7 +92,15 @@ __global__ void __launch_bounds__(kSampleThreads)
   __syncthreads();
   const long cnt = (long)min((long)blockDim.x, n - i0) * P;
   T *dst = theta + ((size_t)j * n + i0) * P;
-  for (long e = threadIdx.x; e < cnt; e += blockDim.x) dst[e] = stage[e];
+  if (((size_t)j * n + i0) * P * sizeof(T) % 16 == 0 && cnt * sizeof(T) % 16 == 0 &&
+      (reinterpret_cast<uintptr_t>(stage) & 15) == 0) {
+    // 16-byte copies (the staged run, its length and its destination are aligned)
+    constexpr int W = (int)(16 / sizeof(T));
+    for (long e = (long)threadIdx.x * W; e < cnt; e += (long)blockDim.x * W)
+      *reinterpret_cast<uint4 *>(dst + e) = *reinterpret_cast<const uint4 *>(stage + e);
+  } else {
+    for (long e = threadIdx.x; e < cnt; e += blockDim.x) dst[e] = stage[e];
+  }
 }
 
 // eta ~ Beta(beta r/2, (1-beta) r/2) / beta via two gammas (make_gamma_1 and

@@ -40,6 +40,11 @@ __device__ __forceinline__ double warp_max(double v) {
 }
 
 // Block-wide sum; every thread gets the result.  `red` needs 32 doubles.
+template <typename T> __device__ __forceinline__ T warp_sum_t(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 __device__ double block_sum(double v, double *red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   v = warp_sum(v);
@@ -140,18 +145,30 @@ __global__ void __launch_bounds__(kVbThreads)
     for (int k = 0; k < PMAX; ++k)
       if (k < P) st[k] += wl * th[k];
   }
-  double *out = part_a + ((size_t)c * m + j) * (P + 2);
-  double v = block_sum((double)sl, red);
-  if (threadIdx.x == 0) out[0] = v;
-  v = block_sum((double)sll, red);
-  if (threadIdx.x == 0) out[1] = v;
+  // all P + 2 sums in one round: warp shuffles in the working precision, one
+  // shared-memory exchange, and thread k adds the eight warps' partials in FP64
+  __shared__ T wpart[kVbThreads / 32][PMAX + 2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  sl = warp_sum_t(sl);
+  sll = warp_sum_t(sll);
 #pragma unroll
-  for (int k = 0; k < PMAX; ++k) {
-    if (k < P) {
-      v = block_sum((double)st[k], red);
-      if (threadIdx.x == 0) out[2 + k] = v;
-    }
+  for (int k = 0; k < PMAX; ++k)
+    if (k < P) st[k] = warp_sum_t(st[k]);
+  if (lane == 0) {
+    wpart[warp][0] = sl;
+    wpart[warp][1] = sll;
+#pragma unroll
+    for (int k = 0; k < PMAX; ++k)
+      if (k < P) wpart[warp][2 + k] = st[k];
   }
+  __syncthreads();
+  double *out = part_a + ((size_t)c * m + j) * (P + 2);
+  if (threadIdx.x < P + 2) {
+    double v = 0.0;
+    for (int w8 = 0; w8 < kVbThreads / 32; ++w8) v += (double)wpart[w8][threadIdx.x];
+    out[threadIdx.x] = v;
+  }
+  (void)red;
 }
 
 // Combines the chunk partials of pass A: E_w lambda, E_w log lambda, and the
@@ -196,26 +213,40 @@ __global__ void __launch_bounds__(kVbThreads)
   double *acc64 = reinterpret_cast<double *>(smem_raw);             // npairs
   T *mb = reinterpret_cast<T *>(acc64 + (npairs > 0 ? npairs : 1));  // P
   T *X = mb + P;                                                     // kSub * P
+  T *sc = X + (size_t)kSub * P;                                      // kSub
   for (int q = threadIdx.x; q < npairs; q += blockDim.x) acc64[q] = 0.0;
   for (int k = threadIdx.x; k < P; k += blockDim.x) mb[k] = (T)mbar_full[(size_t)j * P + k];
+  // this thread's pair q = threadIdx.x -> (x, y), x <= y, column-major over the
+  // upper triangle (npairs <= 2080 < kVbThreads * 9: a thread may own several;
+  // the first is decoded once here, the others in the loop)
+  int px = 0, py = 0;
+  if (threadIdx.x < npairs) {
+    int y = 0;
+    while ((y + 1) * (y + 2) / 2 <= (int)threadIdx.x) ++y;
+    py = y;
+    px = threadIdx.x - y * (y + 1) / 2;
+  }
   __syncthreads();
   const long i0 = (long)c * kChunk;
   const long i1 = min(n, i0 + kChunk);
   for (long s0 = i0; s0 < i1; s0 += kSub) {
     const int cnt = (int)min((long)kSub, i1 - s0);
+    for (int s = threadIdx.x; s < cnt; s += blockDim.x)
+      sc[s] = tsqrt<T>((T)w[s0 + s] * lambda[(size_t)j * n + s0 + s]);
+    __syncthreads();
+    const T *thb = theta + ((size_t)j * n + s0) * P;
     for (int e = threadIdx.x; e < cnt * P; e += blockDim.x) {
-      const int s = e / P, k = e % P;
-      const long i = s0 + s;
-      const T sc = tsqrt<T>((T)w[i] * lambda[(size_t)j * n + i]);
-      X[e] = sc * (theta[((size_t)j * n + i) * P + k] - mb[k]);
+      const int s = e / P, k = e - s * P;
+      X[e] = sc[s] * (thb[e] - mb[k]);
     }
     __syncthreads();
     for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-      // pair index q -> (x, y) with x <= y: column-major over the upper triangle
-      int y = (int)((sqrt(8.0 * q + 1.0) - 1.0) * 0.5);
-      while ((y + 1) * (y + 2) / 2 <= q) ++y;
-      while (y * (y + 1) / 2 > q) --y;
-      const int x = q - y * (y + 1) / 2;
+      int x = px, y = py;
+      if (q != (int)threadIdx.x) {
+        y = 0;
+        while ((y + 1) * (y + 2) / 2 <= q) ++y;
+        x = q - y * (y + 1) / 2;
+      }
       T a = T(0);
       for (int s = 0; s < cnt; ++s) a += X[s * P + x] * X[s * P + y];
       acc64[q] += (double)a;
@@ -405,7 +436,8 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
   k_vb_a_fin<<<(m + 127) / 128, 128, 0, s>>>(m, P, chunks, scr.part_a, mean_lambda,
                                              mean_log_lambda, mbar_full);
   const size_t npairs = (size_t)P * (P + 1) / 2;
-  const size_t smem_b = npairs * sizeof(double) + ((size_t)P + (size_t)kSub * P) * sizeof(T) + 16;
+  const size_t smem_b =
+      npairs * sizeof(double) + ((size_t)P + (size_t)kSub * P + kSub) * sizeof(T) + 16;
   const size_t smem_f = ((size_t)P * P * 3 + P) * sizeof(double);
   if (smem_b > 48 * 1024)
     cudaFuncSetAttribute(k_vb_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
