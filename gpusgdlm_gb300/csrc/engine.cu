@@ -102,7 +102,7 @@ struct sgdlm_engine {
   std::vector<unsigned> h_p, h_sp;
   // simulation
   DevBuf<unsigned char> lambda, theta, theta_dm, lu_scratch;
-  DevBuf<double> logdet, w, y_fc, stats6, part_a, part_b;
+  DevBuf<double> logdet, w, y_fc, stats6, wpart, part_a, part_b;
   DevBuf<int> draw_flags, series_flags;
   DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
   DevBuf<uint32_t> dev_epoch;
@@ -331,6 +331,7 @@ int alloc_state(sgdlm_engine *h) {
   CK(h->mean_Q.alloc(m));
   CK(h->series_flags.alloc(m));
   CK(h->stats6.alloc(8));
+  CK(h->wpart.alloc(4 * (size_t)kWeightBlocks));
   CK(h->dev_epoch.alloc(1));
   h->h_p.assign(m, 0);
   h->h_sp.assign(P * m, 0xFFFFFFFFu);
@@ -362,7 +363,7 @@ void release_all(sgdlm_engine *h) {
   for (auto *b : {&h->m_t, &h->C_t, &h->n_t, &h->s_t, &h->W_t, &h->beta, &h->delta, &h->y_t,
                   &h->F_t, &h->x_t, &h->fm_t, &h->fC_t, &h->fn_t, &h->fs_t, &h->fW_t,
                   &h->U64, &h->mean_m, &h->mean_C, &h->mean_n, &h->mean_s, &h->mean_lambda,
-                  &h->mean_log_lambda, &h->mean_Q, &h->stats6})
+                  &h->mean_log_lambda, &h->mean_Q, &h->stats6, &h->wpart})
     b->release();
   h->U32.release();
   h->p.release();
@@ -540,8 +541,8 @@ int vb_posterior(sgdlm_engine *h, double *o_m, double *o_C, double *o_n, double 
   CK(cudaEventRecord(h->ev[1], s));
   lu_draws<T>(h, nullptr, key, nullptr);
   CK(cudaEventRecord(h->ev[2], s));
-  launch_weights(s, (long)n, h->logdet.ptr, h->w.ptr, h->stats6.ptr);
-  h->launches += 1;
+  launch_weights(s, (long)n, h->logdet.ptr, h->w.ptr, h->stats6.ptr, h->wpart.ptr);
+  h->launches += 3;
   CK(cudaEventRecord(h->ev[3], s));
   vb_moments<T>(h, h->w.ptr);
   CK(cudaEventRecord(h->ev[4], s));
@@ -673,13 +674,13 @@ int filter_step(sgdlm_engine *h, const double *d_y, const double *d_F, const dou
   CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
   sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, key_vb);
   lu_draws<T>(h, nullptr, key_vb, nullptr);
-  launch_weights(s, n, h->logdet.ptr, w, h->stats6.ptr);
+  launch_weights(s, n, h->logdet.ptr, w, h->stats6.ptr, h->wpart.ptr);
   vb_moments<T>(h, w);
   launch_gate(s, m, P, h->stats6.ptr, ess_threshold, h->mean_m.ptr, h->mean_C.ptr,
               h->mean_n.ptr, h->mean_s.ptr, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr,
               h->stats6.ptr + 6);
   launch_prior(s, m, P, h->p.ptr, h->C_t.ptr, h->n_t.ptr, h->W_t.ptr, h->beta.ptr, h->delta.ptr);
-  h->launches += 3;
+  h->launches += 5;  // three for the weights, the gate, the prior
   if (d_x) {
     int st = copy_forecast_priors(h);
     if (st) return st;

@@ -115,10 +115,12 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n,
                         double *logdet, int *draw_flags, const double *x,
                         const T *lambda, RngKey key, double *y, GammaRows rows);
 
-// (a5) importance weights from log|det| by FP64 log-sum-exp.
-// out6 = {sum_det, ess, max_logdet, n_finite, sum_w2, 0}.  rSGDLM/src/SGDLM/SGDLM.cu:325-335
+// (a5) importance weights from log|det| by FP64 log-sum-exp (three launches).
+// out6 = {sum_det, ess, max_logdet, n_finite, sum_w2, 0}; part: scratch of
+// 4 * kWeightBlocks doubles.  rSGDLM/src/SGDLM/SGDLM.cu:325-335
+constexpr int kWeightBlocks = 1024;
 void launch_weights(cudaStream_t s, long n, const double *logdet, double *w,
-                    double *out6);
+                    double *out6, double *part);
 
 // (a6)/(a7) VB moments and refit.  rSGDLM/src/SGDLM/SGDLM.cu:341-500
 struct VbScratch {

@@ -73,11 +73,28 @@ __device__ __forceinline__ bool finite_ld(double v) { return v == v && fabs(v) <
 // out6 = {sum |det|, ESS, max logdet, #finite, sum w^2, 0}.
 // A draw whose log|det| is not finite gets weight 0, as detFromLU gives a NaN/Inf
 // determinant weight 0 (kernel_functions.cuh:905-926).
-__global__ void k_weights(long n, const double *__restrict__ logdet, double *__restrict__ w,
-                          double *__restrict__ out6) {
+// Importance weights over many blocks (FP64; the exponentials spread over the
+// SMs instead of one block's FP64 pipe), three launches:
+//   1. per block: max and count of the finite log|det|;
+//   2. every block combines the maxima (M); e_i = exp(ld_i - M) into w, and the
+//      block's sums of e_i and e_i^2;
+//   3. every block combines the sums (S, Q); w_i = e_i / S (NaN for every draw when
+//      S = 0: the reference divides 0 by 0); block 0 writes
+//      out6 = {exp(M) S, 1 / sum w^2, M, count, sum w^2 = Q / S^2, 0}.
+// part: 4 doubles per block (max, count, sum e, sum e^2).
+constexpr int kWThreads = 256;
+__device__ __forceinline__ void w_range(long n, long &b, long &e) {
+  const long per = (n + gridDim.x - 1) / gridDim.x;
+  b = (long)blockIdx.x * per;
+  e = min(n, b + per);
+}
+__global__ void __launch_bounds__(kWThreads)
+    k_w_max(long n, const double *__restrict__ logdet, double *__restrict__ part) {
   __shared__ double red[32];
+  long b, e;
+  w_range(n, b, e);
   double mx = -INFINITY, cnt = 0.0;
-  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+  for (long i = b + threadIdx.x; i < e; i += blockDim.x) {
     const double v = logdet[i];
     if (finite_ld(v)) {
       mx = fmax(mx, v);
@@ -86,25 +103,55 @@ __global__ void k_weights(long n, const double *__restrict__ logdet, double *__r
   }
   mx = block_max(mx, red);
   cnt = block_sum(cnt, red);
-  double s = 0.0;
-  for (long i = threadIdx.x; i < n; i += blockDim.x) {
+  if (threadIdx.x == 0) {
+    part[4 * blockIdx.x] = mx;
+    part[4 * blockIdx.x + 1] = cnt;
+  }
+}
+__global__ void __launch_bounds__(kWThreads)
+    k_w_exp(long n, const double *__restrict__ logdet, double *__restrict__ w,
+            double *__restrict__ part) {
+  __shared__ double red[32];
+  double mx = -INFINITY;
+  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) mx = fmax(mx, part[4 * c]);
+  mx = block_max(mx, red);
+  long b, e;
+  w_range(n, b, e);
+  double s = 0.0, q = 0.0;
+  for (long i = b + threadIdx.x; i < e; i += blockDim.x) {
     const double v = logdet[i];
-    if (finite_ld(v)) s += exp(v - mx);
+    const double ei = finite_ld(v) ? exp(v - mx) : 0.0;
+    w[i] = ei;
+    s += ei;
+    q += ei * ei;
   }
   s = block_sum(s, red);
-  double s2 = 0.0;
-  for (long i = threadIdx.x; i < n; i += blockDim.x) {
-    const double v = logdet[i];
-    double wi;
-    if (s > 0.0)
-      wi = finite_ld(v) ? exp(v - mx) / s : 0.0;
-    else
-      wi = NAN;  // every determinant was zero: the reference divides 0 by 0
-    w[i] = wi;
-    s2 += wi * wi;
-  }
-  s2 = block_sum(s2, red);
+  q = block_sum(q, red);
   if (threadIdx.x == 0) {
+    part[4 * blockIdx.x + 2] = s;
+    part[4 * blockIdx.x + 3] = q;
+  }
+}
+__global__ void __launch_bounds__(kWThreads)
+    k_w_norm(long n, double *__restrict__ w, const double *__restrict__ part,
+             double *__restrict__ out6) {
+  __shared__ double red[32];
+  double mx = -INFINITY, cnt = 0.0, s = 0.0, q = 0.0;
+  for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) {
+    mx = fmax(mx, part[4 * c]);
+    cnt += part[4 * c + 1];
+    s += part[4 * c + 2];
+    q += part[4 * c + 3];
+  }
+  mx = block_max(mx, red);
+  cnt = block_sum(cnt, red);
+  s = block_sum(s, red);
+  q = block_sum(q, red);
+  long b, e;
+  w_range(n, b, e);
+  for (long i = b + threadIdx.x; i < e; i += blockDim.x) w[i] = (s > 0.0) ? w[i] / s : NAN;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double s2 = q / (s * s);
     out6[0] = (s > 0.0) ? exp(mx) * s : 0.0;
     out6[1] = 1.0 / s2;
     out6[2] = mx;
@@ -410,8 +457,14 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
 
 size_t vb_chunks(long n) { return (size_t)((n + kChunk - 1) / kChunk); }
 
-void launch_weights(cudaStream_t s, long n, const double *logdet, double *w, double *out6) {
-  k_weights<<<1, 1024, 0, s>>>(n, logdet, w, out6);
+void launch_weights(cudaStream_t s, long n, const double *logdet, double *w, double *out6,
+                    double *part) {
+  long blocks = (n + kWThreads - 1) / kWThreads;
+  if (blocks > kWeightBlocks) blocks = kWeightBlocks;
+  if (blocks < 1) blocks = 1;
+  k_w_max<<<(unsigned)blocks, kWThreads, 0, s>>>(n, logdet, part);
+  k_w_exp<<<(unsigned)blocks, kWThreads, 0, s>>>(n, logdet, w, part);
+  k_w_norm<<<(unsigned)blocks, kWThreads, 0, s>>>(n, w, part, out6);
 }
 
 template <typename T>
