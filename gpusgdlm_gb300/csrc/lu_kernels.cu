@@ -845,11 +845,12 @@ __device__ __forceinline__ void gj_update(T (&a)[kB], const T (&g)[4], const T *
 // lane of the warp holds the whole block and computes the same inverse: no
 // shuffles in the dependent chain).  det = det P.  Flags zero / non-finite
 // pivots and LU multipliers of P above tau.
+// Step k; mult collects the largest |LU multiplier| of P (the entries below the
+// pivot, scaled: -P[i][k] after the step).
 template <int k, typename T>
-__device__ __forceinline__ void gj_invert4_step(T (&P)[4][4], T tau, bool &bad, T &det) {
+__device__ __forceinline__ void gj_invert4_step(T (&P)[4][4], T &det, T &mult) {
   {
     const T pk = P[k][k];
-    bad |= !(finite_t(pk) && pk != T(0));
     det *= pk;
     const T rp = rcp_fast(pk);
 #pragma unroll
@@ -860,21 +861,26 @@ __device__ __forceinline__ void gj_invert4_step(T (&P)[4][4], T tau, bool &bad, 
     for (int i = 0; i < 4; ++i) {
       if (i == k) continue;
       const T f = P[i][k];
-      if (i > k) bad |= !(dabs(f * rp) <= tau);
 #pragma unroll
       for (int j = 0; j < 4; ++j)
         if (j != k) P[i][j] -= f * P[k][j];
       P[i][k] = -f * rp;
+      if (i > k) mult = fmax(mult, dabs(P[i][k]));
     }
   }
 }
+// The check of the pivots uses det = their product: a zero or non-finite pivot
+// makes it zero or non-finite (so does an extreme block whose product under- or
+// overflows: it goes to the pivoting redo as well).
 template <typename T>
 __device__ __forceinline__ void gj_invert4(T (&P)[4][4], T tau, bool &bad, T &det) {
   det = T(1);
-  gj_invert4_step<0>(P, tau, bad, det);
-  gj_invert4_step<1>(P, tau, bad, det);
-  gj_invert4_step<2>(P, tau, bad, det);
-  gj_invert4_step<3>(P, tau, bad, det);
+  T mult = T(0);
+  gj_invert4_step<0>(P, det, mult);
+  gj_invert4_step<1>(P, det, mult);
+  gj_invert4_step<2>(P, det, mult);
+  gj_invert4_step<3>(P, det, mult);
+  bad |= !(finite_t(det) && det != T(0) && mult <= tau);
 }
 
 // The pivot block (positions 0..3 of the slot's four pivot rows) into every lane.
