@@ -47,17 +47,23 @@ __global__ void __launch_bounds__(kSampleThreads)
   T *Us = reinterpret_cast<T *>(smem_raw);  // P*P, U[row + P*col]
   T *ms = Us + P * P;                       // P
   T *stage = ms + P;                        // blockDim.x * P
+  __shared__ T ser[3];                      // the series' gamma shape and rate, s_j
   const int j = blockIdx.y;
   for (int e = threadIdx.x; e < P * P; e += blockDim.x) Us[e] = U[(size_t)j * P * P + e];
   for (int e = threadIdx.x; e < P; e += blockDim.x) ms[e] = (T)m_t[(size_t)j * P + e];
+  if (threadIdx.x == 0) {
+    // FP64 once per series (FP64 is a narrow pipe on this GPU)
+    const double nj = n_t[j], sj = s_t[j];
+    ser[0] = (T)(0.5 * nj);
+    ser[1] = (T)(0.5 * nj * sj);
+    ser[2] = (T)sj;
+  }
   __syncthreads();
   const long i0 = (long)blockIdx.x * blockDim.x;
   const long i = i0 + threadIdx.x;
   if (i < n) {
     const uint32_t ep = key_epoch(key);
-    const double nj = n_t[j], sj = s_t[j];
-    const T alpha = (T)(0.5 * nj);
-    const T rate = (T)(0.5 * nj * sj);
+    const T alpha = ser[0], rate = ser[1];
     bool fail = false;
     const T lam = gamma_mt<T>(alpha, (uint32_t)i, (uint32_t)j, TAG_GAMMA, ep, key.k0,
                               key.k1, false, &fail) / rate;
@@ -74,7 +80,7 @@ __global__ void __launch_bounds__(kSampleThreads)
     }
     // theta = m + (U' z) / sqrt(s lambda)   (makeVB_MVN, kernel_functions.cuh:72-83);
     // one reciprocal instead of P divisions (within 1-2 ulp of the quotients)
-    const T rden = T(1) / dev_sqrt((T)sj * lam);
+    const T rden = T(1) / dev_sqrt(ser[2] * lam);
     T *row = stage + (size_t)threadIdx.x * P;
 #pragma unroll
     for (int k = 0; k < PMAX; ++k) {
@@ -211,6 +217,7 @@ void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
   if (smem > 48 * 1024) {
     cudaFuncSetAttribute(k_sample<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_sample<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_sample<T, 24>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_sample<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_sample<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   }
@@ -219,6 +226,9 @@ void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                                                       lambda, theta, theta_dm, draw_flags);
   else if (P <= 16)
     k_sample<T, 16><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
+                                                       lambda, theta, theta_dm, draw_flags);
+  else if (P <= 24)
+    k_sample<T, 24><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
                                                        lambda, theta, theta_dm, draw_flags);
   else if (P <= 32)
     k_sample<T, 32><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,

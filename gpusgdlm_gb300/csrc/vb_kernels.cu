@@ -247,7 +247,7 @@ __global__ void k_vb_a_fin(int m, int P, int chunks, const double *__restrict__ 
 // Draws are staged kSub at a time as X_i = sqrt(w_i lambda_i) (theta_i - m_bar);
 // each thread owns upper-triangle pairs (x <= y), accumulates a sub-chunk in the
 // working precision and flushes it to an FP64 shared accumulator.
-template <typename T>
+template <typename T, int PMAX>
 __global__ void __launch_bounds__(kVbThreads)
     k_vb_b(int m, int P, long n, const unsigned *__restrict__ p,
            const double *__restrict__ w, const T *__restrict__ lambda,
@@ -278,13 +278,26 @@ __global__ void __launch_bounds__(kVbThreads)
   const long i1 = min(n, i0 + kChunk);
   for (long s0 = i0; s0 < i1; s0 += kSub) {
     const int cnt = (int)min((long)kSub, i1 - s0);
+    // this thread's theta values of the sub-chunk: every load in flight at once
+    // (at most kSub * PMAX / kVbThreads per thread), then the per-draw scales
+    const T *thb = theta + ((size_t)j * n + s0) * P;
+    const int tot = cnt * P;
+    T v[kSub * PMAX / kVbThreads];
+#pragma unroll
+    for (int h = 0; h < kSub * PMAX / kVbThreads; ++h) {
+      const int e = threadIdx.x + h * kVbThreads;
+      v[h] = e < tot ? thb[e] : T(0);
+    }
     for (int s = threadIdx.x; s < cnt; s += blockDim.x)
       sc[s] = tsqrt<T>((T)w[s0 + s] * lambda[(size_t)j * n + s0 + s]);
     __syncthreads();
-    const T *thb = theta + ((size_t)j * n + s0) * P;
-    for (int e = threadIdx.x; e < cnt * P; e += blockDim.x) {
-      const int s = e / P, k = e - s * P;
-      X[e] = sc[s] * (thb[e] - mb[k]);
+#pragma unroll
+    for (int h = 0; h < kSub * PMAX / kVbThreads; ++h) {
+      const int e = threadIdx.x + h * kVbThreads;
+      if (e < tot) {
+        const int s = e / P, k = e - s * P;
+        X[e] = sc[s] * (v[h] - mb[k]);
+      }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
@@ -492,12 +505,26 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
   const size_t smem_b =
       npairs * sizeof(double) + ((size_t)P + (size_t)kSub * P + kSub) * sizeof(T) + 16;
   const size_t smem_f = ((size_t)P * P * 3 + P) * sizeof(double);
-  if (smem_b > 48 * 1024)
-    cudaFuncSetAttribute(k_vb_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+  if (smem_b > 48 * 1024) {
+    cudaFuncSetAttribute(k_vb_b<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+    cudaFuncSetAttribute(k_vb_b<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+    cudaFuncSetAttribute(k_vb_b<T, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+    cudaFuncSetAttribute(k_vb_b<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
+  }
   if (smem_f > 48 * 1024)
     cudaFuncSetAttribute(k_vb_fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
-  k_vb_b<T><<<grid, kVbThreads, smem_b, s>>>(m, P, n, p, w, lambda, theta, mbar_full,
-                                             scr.part_b);
+#define SGDLM_VB_B(PM)                                                                \
+  k_vb_b<T, PM><<<grid, kVbThreads, smem_b, s>>>(m, P, n, p, w, lambda, theta, mbar_full, \
+                                                 scr.part_b)
+  if (P <= 8)
+    SGDLM_VB_B(8);
+  else if (P <= 16)
+    SGDLM_VB_B(16);
+  else if (P <= 32)
+    SGDLM_VB_B(32);
+  else
+    SGDLM_VB_B(64);
+#undef SGDLM_VB_B
   k_vb_fin<<<m, 32, smem_f, s>>>(m, P, chunks, p, n_t, s_t, scr.part_b, mean_lambda,
                                  mean_log_lambda, mbar_full, mean_m, mean_C, mean_n,
                                  mean_s, mean_Q, series_flags);
