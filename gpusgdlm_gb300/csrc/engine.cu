@@ -102,7 +102,7 @@ struct sgdlm_engine {
   std::vector<unsigned> h_p, h_sp;
   // simulation
   DevBuf<unsigned char> lambda, theta, theta_dm, lu_scratch;
-  DevBuf<double> logdet, w, y_fc, stats6, wpart, part_a, part_b;
+  DevBuf<double> logdet, w, y_fc, nu_fc, stats6, wpart, part_a, part_b;
   DevBuf<int> draw_flags, series_flags;
   DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
   DevBuf<uint32_t> dev_epoch;
@@ -350,6 +350,7 @@ void release_sim(sgdlm_engine *h) {
   h->logdet.release();
   h->w.release();
   h->y_fc.release();
+  h->nu_fc.release();
   h->part_a.release();
   h->part_b.release();
   h->draw_flags.release();
@@ -414,6 +415,7 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   CK(h->logdet.alloc(nsim));
   CK(h->w.alloc(nsim));
   CK(h->y_fc.alloc(nsim * m));
+  CK(h->nu_fc.alloc(nsim * m));
   CK(h->draw_flags.alloc(nsim));
   CK(h->part_a.alloc((size_t)h->chunks * m * (P + 2) + m * P));
   CK(h->part_b.alloc((size_t)h->chunks * m * P * P));
@@ -480,9 +482,14 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   const long n = (long)h->nsim;
   const bool refine = (h->precision != SGDLM_PRECISION_FP64);
   const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr, h->g_extptr.ptr, h->g_extk.ptr};
+  if (x) {
+    launch_forecast_nu<T>(h->stream, (int)h->m, (int)h->P, n, rows, as<T>(h->theta), x,
+                          as<T>(h->lambda), key, h->nu_fc.ptr);
+    h->launches += 1;
+  }
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
                as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
-               refine, y, rows);
+               refine, y, rows, x ? h->nu_fc.ptr : nullptr);
   launch_lu_fallback<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta),
                         as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
                         as<T>(h->lambda), key, y, rows);

@@ -108,7 +108,16 @@ void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan
                double *logdet, int *draw_flags,
                // forecast solve (x == nullptr: log|det| only)
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
-               GammaRows rows);
+               GammaRows rows,
+               // the forecast right-hand sides of all draws (launch_forecast_nu), or
+               // nullptr: the LU kernel generates them itself
+               const double *nu_in = nullptr);
+// The forecast right-hand sides nu_ij = z_ij / sqrt(lambda_ij) + x_j' phi_ij of all
+// draws (series-major, nu[j*n + i]); theta series-major.  SGDLM.cu:574-590
+// (batchedComputeNuPlusMu, kernel_functions.cuh:1156-1178).
+template <typename T>
+void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, const T *theta,
+                        const double *x, const T *lambda, RngKey key, double *nu);
 template <typename T>
 void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n,
                         const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,

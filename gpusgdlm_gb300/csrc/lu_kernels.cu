@@ -201,6 +201,32 @@ __device__ void forecast_rhs(int m, int P, long n, long i, GammaRows rows, Theta
   }
 }
 
+// The forecast right-hand sides of every (draw, series) pair in one launch, the
+// same values as forecast_rhs (same Philox stream and operations), written
+// series-major (nu[j*n + i], coalesced over draws); the LU kernel then reads its
+// draw's m values in one round instead of generating them on its critical path.
+template <typename T>
+__global__ void __launch_bounds__(128)
+    k_forecast_nu(int m, int P, long n, GammaRows rows, const T *__restrict__ theta,
+                  const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
+                  double *__restrict__ nu) {
+  const int j = blockIdx.y;
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t ep = key_epoch(key);
+  const U4 g = philox((uint32_t)i, (uint32_t)j, tag_sub(TAG_NU, 0), ep, key.k0, key.k1);
+  T z0, z1;
+  box_muller<T>(g.x, g.y, z0, z1);
+  const T lam = lambda[(size_t)j * n + i];
+  double v = (double)(z0 / dev_sqrt(lam));
+  const T *th = theta + ((size_t)j * n + i) * P;
+  for (int q = rows.ext_ptr[j]; q < rows.ext_ptr[j + 1]; ++q) {
+    const int k = rows.ext_k[q];
+    v += x[(size_t)j * P + k] * (double)th[k];
+  }
+  nu[(size_t)j * n + i] = v;
+}
+
 // Writes the identity plus the scattered -theta entries of draw i into the full
 // mp x mp matrix A (fillGammas, kernel_functions.cuh:822-842).
 template <typename T>
@@ -1287,7 +1313,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
          const T *__restrict__ theta_dm, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
          const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
-         double *__restrict__ y, GammaRows rows) {
+         double *__restrict__ y, GammaRows rows, const double *__restrict__ nu_in) {
   static_assert(!TC || sizeof(T) == 4, "tensor-core path: FP32 draws");
   using V = Vec<T>;
   constexpr int W = V::W;
@@ -1366,8 +1392,17 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       build_full<T>(m, P, dp, n, i, sp, theta, A);
     }
     if (solve) {
-      forecast_rhs<T>(m, P, n, i, rows, theta, x, lambda, key, nu);
-      for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)nu[r];
+      if (nu_in) {
+        // the right-hand side computed for all draws beforehand (k_forecast_nu)
+        for (int r = tid; r < m; r += blockDim.x) {
+          const double v = nu_in[(size_t)r * n + i];
+          nu[r] = v;
+          zf[r] = (T)v;
+        }
+      } else {
+        forecast_rhs<T>(m, P, n, i, rows, theta, x, lambda, key, nu);
+        for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)nu[r];
+      }
     }
     __syncthreads();
     // ---- sparse levels
@@ -1949,7 +1984,7 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
                const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
                double *logdet, int *draw_flags,
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
-               GammaRows rows) {
+               GammaRows rows, const double *nu_in) {
   // opt in to exactly the shared memory this plan needs (a failure here shows up
   // as a launch error that the engine reports)
   auto run = [&](auto kernel) {
@@ -1957,7 +1992,8 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
     kernel<<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
                                               pl.vals_smem, n, ep, sp, theta, theta_dm, scratch,
-                                              logdet, draw_flags, x, lambda, key, refine, y, rows);
+                                              logdet, draw_flags, x, lambda, key, refine, y, rows,
+                                              nu_in);
   };
   if constexpr (sizeof(T) == 4) {
     if (pl.tc) {
@@ -1966,6 +2002,13 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
     }
   }
   run(k_lu<T, false>);
+}
+
+template <typename T>
+void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, const T *theta,
+                        const double *x, const T *lambda, RngKey key, double *nu) {
+  const dim3 grid((unsigned)((n + 127) / 128), (unsigned)m);
+  k_forecast_nu<T><<<grid, 128, 0, s>>>(m, P, n, rows, theta, x, lambda, key, nu);
 }
 
 template <typename T>
@@ -1987,12 +2030,17 @@ template LuPlan plan_lu<double>(int, int, long, int, int, int);
 template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
                                const unsigned *, const float *, const float *, float *,
                                double *, int *,
-                               const double *, const float *, RngKey, bool, double *, GammaRows);
+                               const double *, const float *, RngKey, bool, double *, GammaRows,
+                               const double *);
 template void launch_lu<double>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
                                 const unsigned *, const double *, const double *, double *,
                                 double *, int *,
                                 const double *, const double *, RngKey, bool, double *,
-                                GammaRows);
+                                GammaRows, const double *);
+template void launch_forecast_nu<float>(cudaStream_t, int, int, long, GammaRows, const float *,
+                                        const double *, const float *, RngKey, double *);
+template void launch_forecast_nu<double>(cudaStream_t, int, int, long, GammaRows, const double *,
+                                         const double *, const double *, RngKey, double *);
 template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long, const unsigned *,
                                         const float *, const float *, float *, double *, int *,
                                         const double *,
