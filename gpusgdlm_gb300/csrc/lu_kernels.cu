@@ -499,6 +499,31 @@ __device__ __forceinline__ void write_split_row(unsigned char *tile, size_t part
   }
 }
 
+// Writes K-chunk c (values 8c .. 8c + 7, given in x) of row n of a split operand.
+__device__ __forceinline__ void write_split_chunk(unsigned char *tile, size_t part_bytes, int n,
+                                                  int c, const float (&x)[8]) {
+  uint32_t h[4], mm[4], l[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    __nv_bfloat16 hv[2], mv[2], lv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const float v = x[2 * e + u];
+      hv[u] = __float2bfloat16_rn(v);
+      const float r1 = v - __bfloat162float(hv[u]);
+      mv[u] = __float2bfloat16_rn(r1);
+      lv[u] = __float2bfloat16_rn(r1 - __bfloat162float(mv[u]));
+    }
+    h[e] = bf16_pair(hv[0], hv[1]);
+    mm[e] = bf16_pair(mv[0], mv[1]);
+    l[e] = bf16_pair(lv[0], lv[1]);
+  }
+  unsigned char *d = tile + umma_off(n, 8 * c);
+  *reinterpret_cast<uint4 *>(d) = make_uint4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<uint4 *>(d + part_bytes) = make_uint4(mm[0], mm[1], mm[2], mm[3]);
+  *reinterpret_cast<uint4 *>(d + 2 * part_bytes) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
 // Bounded wait for the MMA completion barrier (a timeout sets bad, and the draw
 // is redone by the pivoting pass).
 __device__ __forceinline__ void mma_wait(uint64_t *mbar, uint32_t &mphase, bool &bad) {
@@ -602,6 +627,7 @@ __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int 
 // the Gauss-Jordan super-steps of the FFMA path).
 constexpr int kBarRest = 9;       // warps 1..7 (224 threads)
 constexpr int kBarQuarter0 = 10;  // warps 0 and 4 (64 threads): tensor-memory lanes 0..31
+constexpr int kBarDt = 11;        // warp 0 and warps 1, 2, 3, 5 (160 threads): D^-1 -> Dt
 __device__ __forceinline__ void named_arrive_n(int id, int n) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
@@ -1532,15 +1558,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
               for (int q = 0; q < kB; ++q) rowp[(size_t)dp * q] = a[q];
             }
             if (R > 0) {
-              // D^-1 transposed through shared memory: lane n splits column n into
-              // row n of Dt
+              // D^-1's rows to shared memory; warps 1, 2, 3, 5 transpose and split
+              // them into Dt (its columns as rows) off this warp's chain
 #pragma unroll
               for (int q = 0; q < kB; q += 4) V::st(D + lane * kDs + q, a + q);
               __syncwarp();
-              float col[kB];
-#pragma unroll
-              for (int q = 0; q < kB; ++q) col[q] = D[q * kDs + lane];
-              write_split_row(Dt, (size_t)kB * 64, lane, col);
+              named_arrive_n(kBarDt, 160);
             }
           } else {
             // while warp 0 inverts D: the first tile of the trailing update into
@@ -1566,6 +1589,16 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
                 for (int q = 0; q < kB; ++q) b[q] = rowp[(size_t)dp * q];
                 write_split_row(Lt, L.part_L, t, b);
               }
+            }
+            if (R > 0 && (warp <= 3 || warp == 5)) {
+              // Dt row n = column n of D^-1: thread (n, c) splits its values 8c .. 8c+7
+              named_sync_n(kBarDt, 160);
+              const int hidx = (warp == 5 ? 3 : warp - 1) * 32 + lane;
+              const int n = hidx & 31, c = hidx >> 5;
+              float col[8];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) col[e] = D[(8 * c + e) * kDs + n];
+              write_split_chunk(Dt, (size_t)kB * 64, n, c, col);
             }
           }
           if (R > 0) {
