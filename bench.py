@@ -282,13 +282,21 @@ def barrier(world):
 
 
 def max_over_ranks(x, world):
+    """The largest value of x over the ranks (the replicas' timing is the slowest one)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def job_value(ms_max, steps, world):
+    """Whole-job time-steps/s: every replica advances its own filter `steps` times;
+    the job's time is the slowest rank's."""
+    return world * steps / (ms_max / 1000.0)
 
 
 # --------------------------------------------------------------- CPU arms
@@ -382,7 +390,7 @@ def main():
     e2e_s = max_over_ranks(r["e2e"]["seconds"], world)
     if rank != 0:
         return
-    value = world * args.steps / (ms / 1000.0)
+    value = job_value(ms, args.steps, world)
     pk, which = peaks()
     lu_flops = args.nsim * LU_FLOPS_PER_DRAW(args.m)
     achieved = lu_flops / (r["lu_ms"] / 1000.0) / 1e12
