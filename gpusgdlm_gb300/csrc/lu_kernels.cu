@@ -1136,6 +1136,59 @@ __device__ void be_forward(const T *__restrict__ A, int dp, T *v) {
   }
 }
 
+// The same two sweeps as a pipeline between warps, for d_p <= 256 (warp w owns
+// the 32 rows of block w, one per lane): a block's solution is published in
+// shared memory and announced on named barrier 1 + block (count: the publishing
+// warp and the warps that still need it), so each warp subtracts a later block's
+// contribution as soon as that block is solved -- no CTA-wide barrier per block,
+// and a warp's coefficients of the next block are loaded while it waits.  The
+// named barriers 1..7 are free in the solve phase (the dense phase is over).
+// xs: dp values of shared scratch.
+template <typename T>
+__device__ void be_back_solve_pipe(const T *__restrict__ A, int dp, T *v, T *xs) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nb = dp / kB;
+  if (warp >= nb) return;
+  const int r = warp * kB + lane;
+  T acc = v[r];
+  for (int kb = nb - 1; kb > warp; --kb) {
+    // this row's coefficients of block kb are in flight while the block is solved
+    T b[kB];
+#pragma unroll
+    for (int c = 0; c < kB; ++c) b[c] = A[(size_t)r + (size_t)dp * (kb * kB + c)];
+    named_sync_n(1 + kb, (kb + 1) * 32);  // x of block kb is published
+#pragma unroll
+    for (int c = 0; c < kB; ++c) acc -= b[c] * xs[kb * kB + c];
+  }
+  // x_w = D_w^-1 acc_w (row lane of D_w^-1 against the warp's accumulated values)
+  T x = T(0);
+#pragma unroll
+  for (int c = 0; c < kB; ++c)
+    x += A[(size_t)r + (size_t)dp * (warp * kB + c)] * __shfl_sync(kFull, acc, c);
+  xs[r] = x;
+  v[r] = x;
+  if (warp > 0) named_arrive_n(1 + warp, (warp + 1) * 32);
+}
+
+template <typename T>
+__device__ void be_forward_pipe(const T *__restrict__ A, int dp, T *v, T *xs) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nb = dp / kB;
+  if (warp >= nb) return;
+  const int r = warp * kB + lane;
+  T acc = v[r];
+  for (int kb = 0; kb < warp; ++kb) {
+    T b[kB];
+#pragma unroll
+    for (int c = 0; c < kB; ++c) b[c] = A[(size_t)r + (size_t)dp * (kb * kB + c)];
+    // block kb is final once its own warp has applied every earlier block
+    named_sync_n(1 + kb, (nb - kb) * 32);
+#pragma unroll
+    for (int c = 0; c < kB; ++c) acc -= b[c] * xs[kb * kB + c];
+  }
+  xs[r] = acc;
+  v[r] = acc;
+  if (warp + 1 < nb) named_arrive_n(1 + warp, (nb - warp) * 32);
+}
+
 // Copies the 32 x 32 diagonal block at k0 of the stored factors into D (warp 0).
 template <typename T>
 __device__ __forceinline__ void load_diag_block(const T *__restrict__ A, int mp, int k0, T *D) {
@@ -1720,7 +1773,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         copy_vals<T>(vals, vals_g, ep.n_solve);
         __syncthreads();
       }
-      be_back_solve<T>(A, dp, z, bsum);  // core part of y0
+      // core part of y0
+      if (dp <= kThreads) {
+        be_back_solve_pipe<T>(A, dp, z, bsum);
+        __syncthreads();
+      } else {
+        be_back_solve<T>(A, dp, z, bsum);
+      }
       for (int r = tid; r < ep.core_n; r += blockDim.x) yf[planned ? ep.core_node[r] : r] = z[r];
       __syncthreads();
       levels_backward<T>(ep, vals, zf, yf);
@@ -1731,8 +1790,15 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         for (int r = tid; r < dp; r += blockDim.x)
           z[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
         __syncthreads();
-        be_forward<T>(A, dp, z);
-        be_back_solve<T>(A, dp, z, bsum);
+        if (dp <= kThreads) {
+          be_forward_pipe<T>(A, dp, z, bsum);
+          __syncthreads();
+          be_back_solve_pipe<T>(A, dp, z, bsum);
+          __syncthreads();
+        } else {
+          be_forward<T>(A, dp, z);
+          be_back_solve<T>(A, dp, z, bsum);
+        }
         for (int r = tid; r < ep.core_n; r += blockDim.x) yd[planned ? ep.core_node[r] : r] = z[r];
         __syncthreads();
         levels_backward<T>(ep, vals, zf, yd);

@@ -581,6 +581,26 @@ def test_dense_core_sizes(built_lib, precision, m):
                                atol=5e-6 if precision == "mixed" else 1e-11)
 
 
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_all_draws_singular_give_nan_weights(built_lib, precision):
+    """Two series, each the other's only parent, with coefficients exactly 1 and no
+    posterior spread: every (I - Gamma_i) = [[1, -1], [-1, 1]] is singular.  The
+    reference then divides 0 by 0 for every weight (SGDLM.cu:325-335); here the
+    weights are NaN as well and sum |det| is 0 (the weights run over several
+    blocks: n spans more than one)."""
+    m, P, n = 2, 1, 700
+    sp = np.array([[0 + 2 * 1, 1 + 2 * 0]], dtype=np.float64)  # 0 <- 1, 1 <- 0
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setSimultaneousParents([1, 1], sp)
+    s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
+    s.setPosteriorParameters(np.ones((P, m)), np.zeros((P, P, m)), np.full(m, 20.0),
+                             np.full(m, 1.0))
+    s.setRngState(3, 0)
+    vb = s.computeVBPosterior(n, n)
+    assert np.isnan(vb["IS_weights"]).all()
+    assert vb["sum_det_weights"] == 0.0
+
+
 def test_dag_parents_have_unit_determinant(built_lib):
     """Parents only among lower-indexed series: (I - Gamma) is unit lower triangular,
     det = 1 for every draw, the weights are uniform and ESS = n."""
