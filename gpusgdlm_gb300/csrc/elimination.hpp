@@ -96,6 +96,10 @@ struct EliminationPlan {
   const unsigned *bwd;
   const int *core_node;
   const uint16_t *core_map;
+  // the solve programs (lev_fwd_nodes .. bwd) are one contiguous, 16-byte aligned
+  // run of prog_len ints starting at prog, so that a kernel can stage them
+  const int *prog;
+  int prog_len;
 };
 
 // Builds the plan from the parental sets (sp: max_p x m, entries < m*m address

@@ -286,6 +286,8 @@ int upload_elimination(sgdlm_engine *h) {
   d.chunk_tofs = b + offs[k++];
   d.ent = u(k++);
   d.terms = u(k++);
+  d.prog = b + offs[k];
+  d.prog_len = (int)(offs[k + 9] - offs[k]);  // lev_fwd_nodes .. bwd (core_node follows)
   d.lev_fwd_nodes = b + offs[k++];
   d.fwd_node = b + offs[k++];
   d.fwd_ptr = b + offs[k++];
@@ -386,8 +388,10 @@ int plan_sim(sgdlm_engine *h, long n, LuPlan *out) {
   const int core_n = h->elim_dev.core_n > 0 ? h->elim_dev.core_n : (int)h->m;
   const int nv = h->elim_dev.nv;
   LuPlan pl = (h->precision == SGDLM_PRECISION_FP64)
-                  ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv)
-                  : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv);
+                  ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv,
+                                    h->elim_dev.n_solve, h->elim_dev.prog_len)
+                  : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv,
+                                   h->elim_dev.n_solve, h->elim_dev.prog_len);
   if (pl.smem > 227 * 1024 - 64 || pl.smem_fallback > 227 * 1024 - 64) {
     char buf[200];
     snprintf(buf, sizeof buf,

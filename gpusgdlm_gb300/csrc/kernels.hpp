@@ -83,12 +83,16 @@ struct LuPlan {
   int fb_grid;         // grid of the pivoting redo
   size_t smem, smem_fallback;
   int vals_smem;       // the sparse levels' value slots live in shared memory
+  int prog_smem;       // the solve phase stages the level programs in shared memory
   int tc;              // trailing updates on the tensor cores (tcgen05)
   size_t scratch_elems_per_cta;  // dense core + per-draw values of the sparse levels
   size_t scratch_elems_total;    // covers both passes
 };
-// core_n / nv come from the elimination plan (core_n = m, nv = 0 without one).
-template <typename T> LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv);
+// core_n / nv / n_solve / prog_len come from the elimination plan (core_n = m and
+// the others 0 without one).
+template <typename T>
+LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solve = 0,
+               int prog_len = 0);
 // Row-wise list of the Gamma entries of (I - Gamma): for row r, entries
 // rowptr[r] .. rowptr[r+1]-1 are (e = j*P + k, column).  Built on the host from
 // the parental sets; gives the forecast residual a fixed summation order.

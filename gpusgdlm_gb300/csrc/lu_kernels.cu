@@ -1255,18 +1255,19 @@ __device__ __forceinline__ int lo16(unsigned w) { return (int)(w & 0xFFFFu); }
 __device__ __forceinline__ int hi16(unsigned w) { return (int)(w >> 16); }
 
 // Forward program of one level on the node-indexed vector z: z[r] -= L[r][t] z[t].
-// A node's program words come from L2; they are gathered eight at a time so that
-// their loads overlap (a node has about ten terms).
+// A node's program words are gathered eight at a time so that their loads overlap
+// (a node has about ten terms).  The program is read through generic pointers: in
+// the global plan, or staged in shared memory for the solve phase.
 template <typename T>
 __device__ __forceinline__ void level_forward(const EliminationPlan &ep, int lev, const T *vals,
                                               T *z) {
   for (int g = ep.lev_fwd_nodes[lev] + threadIdx.x; g < ep.lev_fwd_nodes[lev + 1]; g += blockDim.x) {
-    const int r = __ldg(ep.fwd_node + g), q1 = __ldg(ep.fwd_ptr + g + 1);
+    const int r = ep.fwd_node[g], q1 = ep.fwd_ptr[g + 1];
     T acc = z[r];
-    for (int q = __ldg(ep.fwd_ptr + g); q < q1; q += 8) {
+    for (int q = ep.fwd_ptr[g]; q < q1; q += 8) {
       unsigned f[8];
 #pragma unroll
-      for (int h = 0; h < 8; ++h) f[h] = q + h < q1 ? __ldg(ep.fwd + q + h) : 0u;
+      for (int h = 0; h < 8; ++h) f[h] = q + h < q1 ? ep.fwd[q + h] : 0u;
 #pragma unroll
       for (int h = 0; h < 8; ++h)
         if (q + h < q1) acc -= vals[lo16(f[h])] * z[hi16(f[h])];
@@ -1387,7 +1388,8 @@ __device__ __forceinline__ void copy_vals(T *__restrict__ dst, const T *__restri
 // instantiation, so that the FFMA path's register tiles do not weigh on it.
 template <typename T, bool TC>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
-    k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, long n, EliminationPlan ep,
+    k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, int prog_smem, long n,
+         EliminationPlan ep,
          const unsigned *__restrict__ sp, const T *__restrict__ theta_sm,
          const T *__restrict__ theta_dm, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
@@ -1769,8 +1771,27 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       if (flagged) atomicOr(&draw_flags[i], DRAW_FLAG_PIVOT);
     }
     if (solve && !flagged) {
+      EliminationPlan eps = ep;  // the solve programs, staged in shared memory when they fit
       if (planned && vals_smem) {
         copy_vals<T>(vals, vals_g, ep.n_solve);
+        if (prog_smem) {
+          // after the n_solve value slots in the (now free) union region
+          int *sprog = reinterpret_cast<int *>(
+              smem_raw + L.off_vals + ((((size_t)ep.n_solve + 3) / 4 * 4 * sizeof(T) + 15) & ~(size_t)15));
+          const int4 *src = reinterpret_cast<const int4 *>(ep.prog);
+          for (int q = tid; q < ep.prog_len / 4; q += blockDim.x)
+            reinterpret_cast<int4 *>(sprog)[q] = src[q];
+          auto at = [&](const int *g) { return sprog + (g - ep.prog); };
+          eps.lev_fwd_nodes = at(ep.lev_fwd_nodes);
+          eps.fwd_node = at(ep.fwd_node);
+          eps.fwd_ptr = at(ep.fwd_ptr);
+          eps.fwd = reinterpret_cast<const unsigned *>(at(reinterpret_cast<const int *>(ep.fwd)));
+          eps.lev_bwd_nodes = at(ep.lev_bwd_nodes);
+          eps.bwd_node = at(ep.bwd_node);
+          eps.bwd_diag = at(ep.bwd_diag);
+          eps.bwd_ptr = at(ep.bwd_ptr);
+          eps.bwd = reinterpret_cast<const unsigned *>(at(reinterpret_cast<const int *>(ep.bwd)));
+        }
         __syncthreads();
       }
       // core part of y0
@@ -1782,11 +1803,11 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       }
       for (int r = tid; r < ep.core_n; r += blockDim.x) yf[planned ? ep.core_node[r] : r] = z[r];
       __syncthreads();
-      levels_backward<T>(ep, vals, zf, yf);
+      levels_backward<T>(eps, vals, zf, yf);
       if (refine) {
         residual_rhs<T>(m, P, n, i, rows, theta, nu, yf, res, zf);
         __syncthreads();
-        levels_forward<T>(ep, vals, zf);
+        levels_forward<T>(eps, vals, zf);
         for (int r = tid; r < dp; r += blockDim.x)
           z[r] = (r < ep.core_n) ? zf[planned ? ep.core_node[r] : r] : T(0);
         __syncthreads();
@@ -1801,7 +1822,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         }
         for (int r = tid; r < ep.core_n; r += blockDim.x) yd[planned ? ep.core_node[r] : r] = z[r];
         __syncthreads();
-        levels_backward<T>(ep, vals, zf, yd);
+        levels_backward<T>(eps, vals, zf, yd);
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)yf[r] + (double)yd[r];
       } else {
@@ -2038,7 +2059,7 @@ size_t smem_budget(int per_sm) {
 }  // namespace
 
 template <typename T>
-LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv) {
+LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solve, int prog_len) {
   LuPlan pl{};
   pl.m = m;
   pl.P = P;
@@ -2055,6 +2076,13 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv) {
   const size_t with_vals = Smem(pl.dp, m, sizeof(T), nv, pl.tc != 0).total;
   pl.vals_smem = (nv > 0 && with_vals <= smem_budget(target)) ? 1 : 0;
   pl.smem = Smem(pl.dp, m, sizeof(T), pl.vals_smem ? nv : 0, pl.tc != 0).total;
+  {
+    // the solve programs fit after the solve slots in the union region
+    const Smem L(pl.dp, m, sizeof(T), pl.vals_smem ? nv : 0, pl.tc != 0);
+    const size_t region = L.off_z - L.off_vals;
+    const size_t used = (((size_t)n_solve + 3) / 4 * 4 * sizeof(T) + 15) & ~(size_t)15;
+    pl.prog_smem = (pl.vals_smem && prog_len > 0 && used + (size_t)prog_len * 4 <= region) ? 1 : 0;
+  }
   pl.smem_fallback = FallbackSmem(pl.mp, m, sizeof(T)).total;
   int ctas_per_sm = pl.smem <= smem_budget(2) ? 2 : 1;
   if (sizeof(T) == 8) ctas_per_sm = 1;
@@ -2090,7 +2118,8 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
     if (pl.smem > 48 * 1024)
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
     kernel<<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
-                                              pl.vals_smem, n, ep, sp, theta, theta_dm, scratch,
+                                              pl.vals_smem, pl.prog_smem, n, ep, sp, theta,
+                                              theta_dm, scratch,
                                               logdet, draw_flags, x, lambda, key, refine, y, rows,
                                               nu_in);
   };
@@ -2124,8 +2153,8 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const unsigned
       rows);
 }
 
-template LuPlan plan_lu<float>(int, int, long, int, int, int);
-template LuPlan plan_lu<double>(int, int, long, int, int, int);
+template LuPlan plan_lu<float>(int, int, long, int, int, int, int, int);
+template LuPlan plan_lu<double>(int, int, long, int, int, int, int, int);
 template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
                                const unsigned *, const float *, const float *, float *,
                                double *, int *,
