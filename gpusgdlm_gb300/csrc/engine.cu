@@ -90,6 +90,7 @@ struct sgdlm_engine {
   // evolution matrices G (P x P x m, FP64 and the FP32 copy the draws use)
   DevBuf<double> G_t;
   DevBuf<float> G32;
+  DevBuf<float> x32;  // FP32 copy of a forecast's x (the right-hand sides of FP32 draws)
   // sparse pre-elimination plan of (I - Gamma) (elimination.hpp)
   int elim_levels = 4;
   EliminationPlanHost eplan;
@@ -334,6 +335,7 @@ int alloc_state(sgdlm_engine *h) {
   CK(h->series_flags.alloc(m));
   CK(h->stats6.alloc(8));
   CK(h->wpart.alloc(4 * (size_t)kWeightBlocks));
+  CK(h->x32.alloc(P * m));
   CK(h->dev_epoch.alloc(1));
   h->h_p.assign(m, 0);
   h->h_sp.assign(P * m, 0xFFFFFFFFu);
@@ -377,6 +379,7 @@ void release_all(sgdlm_engine *h) {
   h->g_extk.release();
   h->G_t.release();
   h->G32.release();
+  h->x32.release();
   h->elim_buf.release();
   h->elim_dev = EliminationPlan{};
   h->series_flags.release();
@@ -487,9 +490,11 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   const bool refine = (h->precision != SGDLM_PRECISION_FP64);
   const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr, h->g_extptr.ptr, h->g_extk.ptr};
   if (x) {
+    const size_t nx = h->m * h->P;
+    launch_to_float(h->stream, nx, x, h->x32.ptr);
     launch_forecast_nu<T>(h->stream, (int)h->m, (int)h->P, n, rows, as<T>(h->theta), x,
-                          as<T>(h->lambda), key, h->nu_fc.ptr);
-    h->launches += 1;
+                          h->x32.ptr, as<T>(h->lambda), key, h->nu_fc.ptr);
+    h->launches += 2;
   }
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
                as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,

@@ -117,11 +117,13 @@ void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan
                // nullptr: the LU kernel generates them itself
                const double *nu_in = nullptr);
 // The forecast right-hand sides nu_ij = z_ij / sqrt(lambda_ij) + x_j' phi_ij of all
-// draws (series-major, nu[j*n + i]); theta series-major.  SGDLM.cu:574-590
-// (batchedComputeNuPlusMu, kernel_functions.cuh:1156-1178).
+// draws (series-major, nu[j*n + i]); theta series-major; x32: an FP32 copy of x
+// (used for FP32 draws).  SGDLM.cu:574-590 (batchedComputeNuPlusMu,
+// kernel_functions.cuh:1156-1178).
 template <typename T>
 void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, const T *theta,
-                        const double *x, const T *lambda, RngKey key, double *nu);
+                        const double *x, const float *x32, const T *lambda, RngKey key,
+                        double *nu);
 template <typename T>
 void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n,
                         const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,

@@ -201,15 +201,17 @@ __device__ void forecast_rhs(int m, int P, long n, long i, GammaRows rows, Theta
   }
 }
 
-// The forecast right-hand sides of every (draw, series) pair in one launch, the
-// same values as forecast_rhs (same Philox stream and operations), written
-// series-major (nu[j*n + i], coalesced over draws); the LU kernel then reads its
-// draw's m values in one round instead of generating them on its critical path.
+// The forecast right-hand sides of every (draw, series) pair in one launch (the
+// Philox stream of forecast_rhs), written series-major (nu[j*n + i], coalesced
+// over draws); the LU kernel then reads its draw's m values in one round instead
+// of generating them on its critical path.  FP32 draws: the sum in FP32 with an
+// FP32 copy of x (x32; FP64 is a narrow pipe on this GPU, and the normals are
+// FP32 already), one conversion for the stored value; FP64 draws: in FP64.
 template <typename T>
 __global__ void __launch_bounds__(128)
     k_forecast_nu(int m, int P, long n, GammaRows rows, const T *__restrict__ theta,
-                  const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
-                  double *__restrict__ nu) {
+                  const double *__restrict__ x, const float *__restrict__ x32,
+                  const T *__restrict__ lambda, RngKey key, double *__restrict__ nu) {
   const int j = blockIdx.y;
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -218,13 +220,22 @@ __global__ void __launch_bounds__(128)
   T z0, z1;
   box_muller<T>(g.x, g.y, z0, z1);
   const T lam = lambda[(size_t)j * n + i];
-  double v = (double)(z0 / dev_sqrt(lam));
   const T *th = theta + ((size_t)j * n + i) * P;
-  for (int q = rows.ext_ptr[j]; q < rows.ext_ptr[j + 1]; ++q) {
-    const int k = rows.ext_k[q];
-    v += x[(size_t)j * P + k] * (double)th[k];
+  if constexpr (sizeof(T) == 4) {
+    float v = z0 / dev_sqrt(lam);
+    for (int q = rows.ext_ptr[j]; q < rows.ext_ptr[j + 1]; ++q) {
+      const int k = rows.ext_k[q];
+      v = fmaf(x32[(size_t)j * P + k], th[k], v);
+    }
+    nu[(size_t)j * n + i] = (double)v;
+  } else {
+    double v = (double)(z0 / dev_sqrt(lam));
+    for (int q = rows.ext_ptr[j]; q < rows.ext_ptr[j + 1]; ++q) {
+      const int k = rows.ext_k[q];
+      v += x[(size_t)j * P + k] * (double)th[k];
+    }
+    nu[(size_t)j * n + i] = v;
   }
-  nu[(size_t)j * n + i] = v;
 }
 
 // Writes the identity plus the scattered -theta entries of draw i into the full
@@ -2134,9 +2145,10 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
 
 template <typename T>
 void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, const T *theta,
-                        const double *x, const T *lambda, RngKey key, double *nu) {
+                        const double *x, const float *x32, const T *lambda, RngKey key,
+                        double *nu) {
   const dim3 grid((unsigned)((n + 127) / 128), (unsigned)m);
-  k_forecast_nu<T><<<grid, 128, 0, s>>>(m, P, n, rows, theta, x, lambda, key, nu);
+  k_forecast_nu<T><<<grid, 128, 0, s>>>(m, P, n, rows, theta, x, x32, lambda, key, nu);
 }
 
 template <typename T>
@@ -2166,9 +2178,11 @@ template void launch_lu<double>(cudaStream_t, const LuPlan &, long, const Elimin
                                 const double *, const double *, RngKey, bool, double *,
                                 GammaRows, const double *);
 template void launch_forecast_nu<float>(cudaStream_t, int, int, long, GammaRows, const float *,
-                                        const double *, const float *, RngKey, double *);
-template void launch_forecast_nu<double>(cudaStream_t, int, int, long, GammaRows, const double *,
-                                         const double *, const double *, RngKey, double *);
+                                        const double *, const float *, const float *, RngKey,
+                                        double *);
+template void launch_forecast_nu<double>(cudaStream_t, int, int, long, GammaRows,
+                                         const double *, const double *, const float *,
+                                         const double *, RngKey, double *);
 template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long, const unsigned *,
                                         const float *, const float *, float *, double *, int *,
                                         const double *,
