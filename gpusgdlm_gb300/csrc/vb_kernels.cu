@@ -244,9 +244,23 @@ __global__ void k_vb_a_fin(int m, int P, int chunks, const double *__restrict__ 
 
 // Pass B: per (chunk, series): V = sum w lambda (theta - m_bar)(theta - m_bar)' over
 // the leading p x p block (meanBatchedVecVecT, kernel_functions.cuh:1103-1133).
-// Draws are staged kSub at a time as X_i = sqrt(w_i lambda_i) (theta_i - m_bar);
-// each thread owns upper-triangle pairs (x <= y), accumulates a sub-chunk in the
-// working precision and flushes it to an FP64 shared accumulator.
+// Draws are staged kSub at a time as X_i = sqrt(w_i lambda_i) (theta_i - m_bar)
+// (rows padded to a multiple of 4, padding zero; a thread's theta loads of a
+// sub-chunk are all in flight at once).  The upper triangle is cut into 4 x 4
+// tiles; thread (tile, group) accumulates its tile over the draws of its group in
+// registers in the working precision -- two 16-byte shared loads per draw for 16
+// FMAs -- and the groups' partials are added in FP64 at the end.
+// four consecutive values from a 16-byte aligned shared address
+__device__ __forceinline__ void load4(const float *a, float *v) {
+  const float4 q = *reinterpret_cast<const float4 *>(a);
+  v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+}
+__device__ __forceinline__ void load4(const double *a, double *v) {
+  const double2 q0 = reinterpret_cast<const double2 *>(a)[0];
+  const double2 q1 = reinterpret_cast<const double2 *>(a)[1];
+  v[0] = q0.x, v[1] = q0.y, v[2] = q1.x, v[3] = q1.y;
+}
+
 template <typename T, int PMAX>
 __global__ void __launch_bounds__(kVbThreads)
     k_vb_b(int m, int P, long n, const unsigned *__restrict__ p,
@@ -256,30 +270,33 @@ __global__ void __launch_bounds__(kVbThreads)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int j = blockIdx.y, c = blockIdx.x;
   const int pj = (int)min((unsigned)P, p[j]);
-  const int npairs = pj * (pj + 1) / 2;
-  double *acc64 = reinterpret_cast<double *>(smem_raw);             // npairs
-  T *mb = reinterpret_cast<T *>(acc64 + (npairs > 0 ? npairs : 1));  // P
-  T *X = mb + P;                                                     // kSub * P
-  T *sc = X + (size_t)kSub * P;                                      // kSub
-  for (int q = threadIdx.x; q < npairs; q += blockDim.x) acc64[q] = 0.0;
-  for (int k = threadIdx.x; k < P; k += blockDim.x) mb[k] = (T)mbar_full[(size_t)j * P + k];
-  // this thread's pair q = threadIdx.x -> (x, y), x <= y, column-major over the
-  // upper triangle (npairs <= 2080 < kVbThreads * 9: a thread may own several;
-  // the first is decoded once here, the others in the loop)
-  int px = 0, py = 0;
-  if (threadIdx.x < npairs) {
-    int y = 0;
-    while ((y + 1) * (y + 2) / 2 <= (int)threadIdx.x) ++y;
-    py = y;
-    px = threadIdx.x - y * (y + 1) / 2;
-  }
+  const int PX = (P + 3) / 4 * 4;  // padded row of X
+  const int nb = (pj + 3) / 4, ntiles = nb * (nb + 1) / 2;
+  const int G = ntiles > 0 ? kVbThreads / ntiles : 0;  // draw groups
+  T *X = reinterpret_cast<T *>(smem_raw);  // kSub * PX
+  T *mb = X + (size_t)kSub * PX;           // PX
+  T *sc = mb + PX;                         // kSub
+  T *red = sc + kSub;                      // G * ntiles * 16 (at the end)
+  for (int k = threadIdx.x; k < PX; k += blockDim.x)
+    mb[k] = k < P ? (T)mbar_full[(size_t)j * P + k] : T(0);
+  // the rows' padding stays zero (the data never writes it)
+  if (PX > P)
+    for (int e = threadIdx.x; e < kSub * PX; e += blockDim.x)
+      if (e % PX >= P) X[e] = T(0);
+  // this thread's tile (bx <= by, column-major over the upper triangle) and group
+  const int t = G > 0 ? (int)threadIdx.x % ntiles : 0;
+  const int g = G > 0 ? (int)threadIdx.x / ntiles : 1 << 30;
+  int by = 0;
+  while ((by + 1) * (by + 2) / 2 <= t) ++by;
+  const int bx = t - by * (by + 1) / 2;
+  T acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = T(0);
   __syncthreads();
   const long i0 = (long)c * kChunk;
   const long i1 = min(n, i0 + kChunk);
   for (long s0 = i0; s0 < i1; s0 += kSub) {
     const int cnt = (int)min((long)kSub, i1 - s0);
-    // this thread's theta values of the sub-chunk: every load in flight at once
-    // (at most kSub * PMAX / kVbThreads per thread), then the per-draw scales
     const T *thb = theta + ((size_t)j * n + s0) * P;
     const int tot = cnt * P;
     T v[kSub * PMAX / kVbThreads];
@@ -296,30 +313,40 @@ __global__ void __launch_bounds__(kVbThreads)
       const int e = threadIdx.x + h * kVbThreads;
       if (e < tot) {
         const int s = e / P, k = e - s * P;
-        X[e] = sc[s] * (v[h] - mb[k]);
+        X[s * PX + k] = sc[s] * (v[h] - mb[k]);
       }
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-      int x = px, y = py;
-      if (q != (int)threadIdx.x) {
-        y = 0;
-        while ((y + 1) * (y + 2) / 2 <= q) ++y;
-        x = q - y * (y + 1) / 2;
+    if (g < G) {
+      for (int s = g; s < cnt; s += G) {
+        T xa[4], xb[4];
+        load4(X + s * PX + 4 * bx, xa);
+        load4(X + s * PX + 4 * by, xb);
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) acc[4 * a + b] += xa[a] * xb[b];
       }
-      T a = T(0);
-      for (int s = 0; s < cnt; ++s) a += X[s * P + x] * X[s * P + y];
-      acc64[q] += (double)a;
     }
     __syncthreads();
   }
+  if (g < G) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) red[((size_t)g * ntiles + t) * 16 + q] = acc[q];
+  }
+  __syncthreads();
   double *out = part_b + ((size_t)c * m + j) * P * P;
-  for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-    int y = (int)((sqrt(8.0 * q + 1.0) - 1.0) * 0.5);
-    while ((y + 1) * (y + 2) / 2 <= q) ++y;
-    while (y * (y + 1) / 2 > q) --y;
-    const int x = q - y * (y + 1) / 2;
-    out[x + P * y] = acc64[q];
+  for (int e = threadIdx.x; e < ntiles * 16; e += blockDim.x) {
+    const int tt = e / 16, q = e % 16;
+    int yy = 0;
+    while ((yy + 1) * (yy + 2) / 2 <= tt) ++yy;
+    const int xx = tt - yy * (yy + 1) / 2;
+    const int x = 4 * xx + q / 4, y = 4 * yy + q % 4;
+    if (x <= y && y < pj) {
+      double vv = 0.0;
+      for (int gg = 0; gg < G; ++gg) vv += (double)red[((size_t)gg * ntiles + tt) * 16 + q];
+      out[x + P * y] = vv;
+    }
   }
 }
 
@@ -501,9 +528,8 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
   double *mbar_full = scr.part_a + (size_t)chunks * m * (P + 2);
   k_vb_a_fin<<<(m + 127) / 128, 128, 0, s>>>(m, P, chunks, scr.part_a, mean_lambda,
                                              mean_log_lambda, mbar_full);
-  const size_t npairs = (size_t)P * (P + 1) / 2;
-  const size_t smem_b =
-      npairs * sizeof(double) + ((size_t)P + (size_t)kSub * P + kSub) * sizeof(T) + 16;
+  const size_t PX = (size_t)(P + 3) / 4 * 4;
+  const size_t smem_b = ((size_t)kSub * PX + PX + kSub + (size_t)kVbThreads * 16) * sizeof(T);
   const size_t smem_f = ((size_t)P * P * 3 + P) * sizeof(double);
   if (smem_b > 48 * 1024) {
     cudaFuncSetAttribute(k_vb_b<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
