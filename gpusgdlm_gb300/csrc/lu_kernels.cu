@@ -1155,26 +1155,49 @@ __device__ void be_forward(const T *__restrict__ A, int dp, T *v) {
 // and a warp's coefficients of the next block are loaded while it waits.  The
 // named barriers 1..7 are free in the solve phase (the dense phase is over).
 // xs: dp values of shared scratch.
+// Sum over c of b[c] x[c] for 32 values of x in shared memory (16-byte aligned),
+// in four interleaved partial sums.
+template <typename T>
+__device__ __forceinline__ T dot_block(const T *b, const T *x) {
+  using V = Vec<T>;
+  T part[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+  for (int c = 0; c < kB; c += V::W) {
+    T xv[V::W];
+    V::ld(x + c, xv);
+#pragma unroll
+    for (int e = 0; e < V::W; ++e) part[(c + e) & 3] += b[c + e] * xv[e];
+  }
+  return (part[0] + part[1]) + (part[2] + part[3]);
+}
+
+// Back sweep: the row segments of blocks nb-1 .. w+1 and finally of D_w^-1 are
+// one stream of 32-value loads, double-buffered, so that the next segment is in
+// flight while the warp waits for a block; D_w^-1 is applied to the warp's
+// accumulated values through a broadcast from v (its own rows, free until x is
+// written back).
 template <typename T>
 __device__ void be_back_solve_pipe(const T *__restrict__ A, int dp, T *v, T *xs) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nb = dp / kB;
   if (warp >= nb) return;
   const int r = warp * kB + lane;
   T acc = v[r];
+  T cur[kB], nxt[kB];
+#pragma unroll
+  for (int c = 0; c < kB; ++c) cur[c] = A[(size_t)r + (size_t)dp * ((nb - 1) * kB + c)];
   for (int kb = nb - 1; kb > warp; --kb) {
-    // this row's coefficients of block kb are in flight while the block is solved
-    T b[kB];
 #pragma unroll
-    for (int c = 0; c < kB; ++c) b[c] = A[(size_t)r + (size_t)dp * (kb * kB + c)];
+    for (int c = 0; c < kB; ++c) nxt[c] = A[(size_t)r + (size_t)dp * ((kb - 1) * kB + c)];
     named_sync_n(1 + kb, (kb + 1) * 32);  // x of block kb is published
+    acc -= dot_block<T>(cur, xs + kb * kB);
 #pragma unroll
-    for (int c = 0; c < kB; ++c) acc -= b[c] * xs[kb * kB + c];
+    for (int c = 0; c < kB; ++c) cur[c] = nxt[c];
   }
-  // x_w = D_w^-1 acc_w (row lane of D_w^-1 against the warp's accumulated values)
-  T x = T(0);
-#pragma unroll
-  for (int c = 0; c < kB; ++c)
-    x += A[(size_t)r + (size_t)dp * (warp * kB + c)] * __shfl_sync(kFull, acc, c);
+  // x_w = D_w^-1 acc_w (cur holds row lane of D_w^-1)
+  v[r] = acc;
+  __syncwarp();
+  const T x = dot_block<T>(cur, v + warp * kB);
+  __syncwarp();
   xs[r] = x;
   v[r] = x;
   if (warp > 0) named_arrive_n(1 + warp, (warp + 1) * 32);
