@@ -105,6 +105,7 @@ struct sgdlm_engine {
   DevBuf<unsigned char> lambda, theta, theta_dm, lu_scratch;
   DevBuf<double> logdet, w, y_fc, nu_fc, stats6, wpart, part_a, part_b;
   DevBuf<int> draw_flags, series_flags;
+  DevBuf<int> pivot_list;  // nsim + 1: count, then the draws flagged for the redo
   DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
   DevBuf<uint32_t> dev_epoch;
   LuPlan plan{};
@@ -358,6 +359,7 @@ void release_sim(sgdlm_engine *h) {
   h->part_a.release();
   h->part_b.release();
   h->draw_flags.release();
+  h->pivot_list.release();
   h->sim_init = false;
   h->nsim = 0;
   h->nsim_batch = 0;
@@ -424,6 +426,7 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   CK(h->y_fc.alloc(nsim * m));
   CK(h->nu_fc.alloc(nsim * m));
   CK(h->draw_flags.alloc(nsim));
+  CK(h->pivot_list.alloc(nsim + 1));
   CK(h->part_a.alloc((size_t)h->chunks * m * (P + 2) + m * P));
   CK(h->part_b.alloc((size_t)h->chunks * m * P * P));
   h->nsim = nsim;
@@ -496,12 +499,14 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
                           h->x32.ptr, as<T>(h->lambda), key, h->nu_fc.ptr);
     h->launches += 2;
   }
+  // the fast pass appends the draws it flags to pivot_list; the redo visits those
+  cudaMemsetAsync(h->pivot_list.ptr, 0, sizeof(int), h->stream);
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
                as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
-               refine, y, rows, x ? h->nu_fc.ptr : nullptr);
+               refine, y, rows, x ? h->nu_fc.ptr : nullptr, h->pivot_list.ptr);
   launch_lu_fallback<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta),
                         as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
-                        as<T>(h->lambda), key, y, rows);
+                        as<T>(h->lambda), key, y, rows, h->pivot_list.ptr);
   h->launches += 2;
 }
 

@@ -115,7 +115,10 @@ void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan
                GammaRows rows,
                // the forecast right-hand sides of all draws (launch_forecast_nu), or
                // nullptr: the LU kernel generates them itself
-               const double *nu_in = nullptr);
+               const double *nu_in = nullptr,
+               // n + 1 ints, [0] zero on entry: the draws flagged for the pivoted redo
+               // are appended ([0] their count, [1..] their indices), or nullptr
+               int *pivot_list = nullptr);
 // The forecast right-hand sides nu_ij = z_ij / sqrt(lambda_ij) + x_j' phi_ij of all
 // draws (series-major, nu[j*n + i]); theta series-major; x32: an FP32 copy of x
 // (used for FP32 draws).  SGDLM.cu:574-590 (batchedComputeNuPlusMu,
@@ -128,7 +131,10 @@ template <typename T>
 void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n,
                         const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
                         double *logdet, int *draw_flags, const double *x,
-                        const T *lambda, RngKey key, double *y, GammaRows rows);
+                        const T *lambda, RngKey key, double *y, GammaRows rows,
+                        // the list launch_lu appended to (only those draws are
+                        // visited), or nullptr: every draw's flag is read
+                        const int *pivot_list = nullptr);
 
 // (a5) importance weights from log|det| by FP64 log-sum-exp (three launches).
 // out6 = {sum_det, ess, max_logdet, n_finite, sum_w2, 0}; part: scratch of

@@ -1428,7 +1428,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
          const T *__restrict__ theta_dm, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
          const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
-         double *__restrict__ y, GammaRows rows, const double *__restrict__ nu_in) {
+         double *__restrict__ y, GammaRows rows, const double *__restrict__ nu_in,
+         int *__restrict__ pivot_list) {
   static_assert(!TC || sizeof(T) == 4, "tensor-core path: FP32 draws");
   using V = Vec<T>;
   constexpr int W = V::W;
@@ -1802,7 +1803,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     const bool flagged = (sflag != 0);
     if (tid == 0) {
       logdet[i] = ld_total;
-      if (flagged) atomicOr(&draw_flags[i], DRAW_FLAG_PIVOT);
+      if (flagged) {
+        atomicOr(&draw_flags[i], DRAW_FLAG_PIVOT);
+        if (pivot_list) {
+          const int q = atomicAdd(pivot_list, 1);
+          if (q < n) pivot_list[1 + q] = (int)i;
+        }
+      }
     }
     if (solve && !flagged) {
       EliminationPlan eps = ep;  // the solve programs, staged in shared memory when they fit
@@ -1888,7 +1895,7 @@ __global__ void __launch_bounds__(kThreads)
                   T *__restrict__ scratch,
                   double *__restrict__ logdet, int *__restrict__ draw_flags,
                   const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
-                  double *__restrict__ y, GammaRows rows) {
+                  double *__restrict__ y, GammaRows rows, const int *__restrict__ pivot_list) {
   using V = Vec<T>;
   constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1913,7 +1920,10 @@ __global__ void __launch_bounds__(kThreads)
   const bool solve = (x != nullptr);
   __shared__ bool s_singular;
 
-  for (long i = blockIdx.x; i < n; i += gridDim.x) {
+  // the flagged draws: the fast pass's list, or all n draws' flags
+  const long cnt = pivot_list ? min((long)pivot_list[0], n) : n;
+  for (long q = blockIdx.x; q < cnt; q += gridDim.x) {
+    const long i = pivot_list ? (long)pivot_list[1 + q] : q;
     if (!(draw_flags[i] & DRAW_FLAG_PIVOT)) continue;
     build_full<T>(m, P, mp, n, i, sp, theta, A);
     if (solve) {
@@ -2145,7 +2155,7 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
                const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
                double *logdet, int *draw_flags,
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
-               GammaRows rows, const double *nu_in) {
+               GammaRows rows, const double *nu_in, int *pivot_list) {
   // opt in to exactly the shared memory this plan needs (a failure here shows up
   // as a launch error that the engine reports)
   auto run = [&](auto kernel) {
@@ -2155,7 +2165,7 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
                                               pl.vals_smem, pl.prog_smem, n, ep, sp, theta,
                                               theta_dm, scratch,
                                               logdet, draw_flags, x, lambda, key, refine, y, rows,
-                                              nu_in);
+                                              nu_in, pivot_list);
   };
   if constexpr (sizeof(T) == 4) {
     if (pl.tc) {
@@ -2179,13 +2189,13 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const unsigned
                         const T *theta, const T *theta_dm, T *scratch, double *logdet,
                         int *draw_flags,
                         const double *x, const T *lambda, RngKey key, double *y,
-                        GammaRows rows) {
+                        GammaRows rows, const int *pivot_list) {
   if (pl.smem_fallback > 48 * 1024)
     cudaFuncSetAttribute(k_lu_fallback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)pl.smem_fallback);
   k_lu_fallback<T><<<pl.fb_grid, pl.block, pl.smem_fallback, s>>>(
       pl.m, pl.P, pl.mp, n, sp, theta, theta_dm, scratch, logdet, draw_flags, x, lambda, key, y,
-      rows);
+      rows, pivot_list);
 }
 
 template LuPlan plan_lu<float>(int, int, long, int, int, int, int, int);
@@ -2194,12 +2204,12 @@ template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const Elimina
                                const unsigned *, const float *, const float *, float *,
                                double *, int *,
                                const double *, const float *, RngKey, bool, double *, GammaRows,
-                               const double *);
+                               const double *, int *);
 template void launch_lu<double>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
                                 const unsigned *, const double *, const double *, double *,
                                 double *, int *,
                                 const double *, const double *, RngKey, bool, double *,
-                                GammaRows, const double *);
+                                GammaRows, const double *, int *);
 template void launch_forecast_nu<float>(cudaStream_t, int, int, long, GammaRows, const float *,
                                         const double *, const float *, const float *, RngKey,
                                         double *);
@@ -2209,11 +2219,11 @@ template void launch_forecast_nu<double>(cudaStream_t, int, int, long, GammaRows
 template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long, const unsigned *,
                                         const float *, const float *, float *, double *, int *,
                                         const double *,
-                                        const float *, RngKey, double *, GammaRows);
+                                        const float *, RngKey, double *, GammaRows, const int *);
 template void launch_lu_fallback<double>(cudaStream_t, const LuPlan &, long, const unsigned *,
                                          const double *, const double *, double *, double *,
                                          int *,
                                          const double *, const double *, RngKey, double *,
-                                         GammaRows);
+                                         GammaRows, const int *);
 
 }  // namespace sgdlm

@@ -353,17 +353,27 @@ __global__ void __launch_bounds__(kVbThreads)
 // The reference's digamma and trigamma (kernel_functions.cuh:1006-1022): the
 // asymptotic (Stirling) series truncated after the x^-14 and x^-9 terms, applied
 // at any x.  Reproduced as is, including its error at small x.
-__device__ __forceinline__ double psi_series(double x) {
-  const double x2 = x * x, x4 = x2 * x2, x6 = x4 * x2, x8 = x4 * x4;
-  const double x10 = x8 * x2, x12 = x8 * x4, x14 = x12 * x2;
-  return log(x) - 1.0 / (2.0 * x) - 1.0 / (12.0 * x2) + 1.0 / (120.0 * x4) -
-         1.0 / (252.0 * x6) + 1.0 / (240.0 * x8) - 5.0 / (660.0 * x10) +
-         691.0 / (32760.0 * x12) - 1.0 / (12.0 * x14);
+// The same asymptotic series evaluated in r = 1/x (one division) by Horner's rule.
+__device__ __forceinline__ double psi_series_r(double logx, double r) {
+  const double t = r * r;
+  const double s =
+      t * (-1.0 / 12.0 +
+           t * (1.0 / 120.0 +
+                t * (-1.0 / 252.0 +
+                     t * (1.0 / 240.0 +
+                          t * (-5.0 / 660.0 + t * (691.0 / 32760.0 + t * (-1.0 / 12.0)))))));
+  return logx - 0.5 * r + s;
 }
-__device__ __forceinline__ double psi1_series(double x) {
-  const double x2 = x * x, x3 = x2 * x, x5 = x3 * x2, x7 = x5 * x2, x9 = x7 * x2;
-  return 1.0 / x + 1.0 / (2.0 * x2) + 1.0 / (6.0 * x3) - 1.0 / (30.0 * x5) +
-         1.0 / (42.0 * x7) - 1.0 / (30.0 * x9);
+__device__ __forceinline__ double psi1_series_r(double r) {
+  const double t = r * r;
+  return r + 0.5 * t + t * r * (1.0 / 6.0 + t * (-1.0 / 30.0 + t * (1.0 / 42.0 + t * (-1.0 / 30.0))));
+}
+
+// Orders |v| like the serial pivot scan's "v > best": the magnitude's bits as an
+// integer (monotone for non-negative doubles), NaN below every number.
+__device__ __forceinline__ long long pivot_key(double v) {
+  const long long b = __double_as_longlong(v) & 0x7fffffffffffffffLL;
+  return b > 0x7ff0000000000000LL ? -1LL : b;
 }
 
 // Per-series refit, one warp per series (FP64):
@@ -387,7 +397,6 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
   double *V = sh;                      // P x P, V[x + P*y]
   double *G = V + (size_t)P * P;       // p x 2p augmented [V | I], G[r + pj*c]
   double *f = G + (size_t)2 * P * P;   // multipliers of the current column
-  __shared__ int s_piv;
   __shared__ int s_bad;
   __shared__ double s_sb;
   if (lane == 0) s_bad = 0;
@@ -406,23 +415,34 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
     G[e] = (cidx < pj) ? V[r + P * cidx] : ((cidx - pj) == r ? 1.0 : 0.0);
   }
   __syncwarp();
-  // Gauss-Jordan with partial pivoting on [V | I] -> [I | V^-1]
+  // Gauss-Jordan with partial pivoting on [V | I] -> [I | V^-1].  The pivot row is
+  // the first row of the largest |entry| at or below the diagonal, as a serial scan
+  // with "v > best" finds it (a NaN diagonal entry stays the pivot; NaN below it is
+  // never chosen): a warp reduction over integer keys, ties to the lower row.
+  double *grow = f + P;  // the normalised pivot row (2p values)
   for (int k = 0; k < pj; ++k) {
-    if (lane == 0) {
-      int best = k;
-      double bv = fabs(G[k + pj * k]);
-      for (int r = k + 1; r < pj; ++r) {
-        const double v = fabs(G[r + pj * k]);
-        if (v > bv) {
-          bv = v;
-          best = r;
-        }
-      }
-      s_piv = best;
-      if (!(bv > 0.0)) s_bad = 1;
+    const double dk = G[k + pj * k];
+    long long key = -2;
+    int idx = k;
+    if (lane >= k && lane < pj) {
+      key = lane == k ? pivot_key(dk) : pivot_key(G[lane + pj * k]);
+      idx = lane;
     }
-    __syncwarp();
-    const int pr = s_piv;
+    if (pj > 32)
+      for (int r = lane + 32; r < pj; r += 32) {
+        if (r < k) continue;
+        const long long kr = pivot_key(G[r + pj * k]);
+        if (kr > key) key = kr, idx = r;
+      }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ko = __shfl_xor_sync(0xffffffffu, key, o);
+      const int io = __shfl_xor_sync(0xffffffffu, idx, o);
+      if (ko > key || (ko == key && io < idx)) key = ko, idx = io;
+    }
+    const bool nan_diag = isnan(dk);
+    const int pr = nan_diag ? k : idx;
+    if (lane == 0 && !((nan_diag ? -1LL : key) > 0)) s_bad = 1;  // |pivot| > 0 fails
     if (pr != k)
       for (int cidx = lane; cidx < 2 * pj; cidx += 32) {
         const double t = G[k + pj * cidx];
@@ -430,14 +450,18 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
         G[pr + pj * cidx] = t;
       }
     __syncwarp();
-    const double piv = G[k + pj * k];
+    const double rpiv = 1.0 / G[k + pj * k];
     for (int r = lane; r < pj; r += 32) f[r] = G[r + pj * k];
     __syncwarp();
     for (int cidx = lane; cidx < 2 * pj; cidx += 32) {
-      const double gk = G[k + pj * cidx] / piv;
+      const double gk = G[k + pj * cidx] * rpiv;
       G[k + pj * cidx] = gk;
-      for (int r = 0; r < pj; ++r)
-        if (r != k) G[r + pj * cidx] -= f[r] * gk;
+      grow[cidx] = gk;
+    }
+    __syncwarp();
+    for (int e = lane; e < 2 * pj * pj; e += 32) {
+      const int r = e % pj, cidx = e / pj;
+      if (r != k) G[e] -= f[r] * grow[cidx];
     }
     __syncwarp();
   }
@@ -458,10 +482,12 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
     double mn = n_t[j];
     double fun, dfun, step = 0.0;
     size_t iter = 0;
+    const double log2El = log(2 * El), dq = pd - q;
     do {
       mn -= step;
-      fun = log(mn + pd - q) - psi_series(mn / 2) - (pd - q) / mn - log(2 * El) + Ell;
-      dfun = 1 / (mn + pd - q) - .5 * psi1_series(mn / 2) + (pd - q) / (mn * mn);
+      const double rmn = 1.0 / mn, r = 2.0 * rmn;  // r = 1 / (mn / 2)
+      fun = log(mn + dq) - psi_series_r(log(0.5 * mn), r) - dq * rmn - log2El + Ell;
+      dfun = 1.0 / (mn + dq) - .5 * psi1_series_r(r) + dq * rmn * rmn;
       step = fun / dfun;
       if (step > mn) step = .5 * mn;
     } while (fabs(fun) > 1e-6 && iter++ < 50);
@@ -530,7 +556,7 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
                                              mean_log_lambda, mbar_full);
   const size_t PX = (size_t)(P + 3) / 4 * 4;
   const size_t smem_b = ((size_t)kSub * PX + PX + kSub + (size_t)kVbThreads * 16) * sizeof(T);
-  const size_t smem_f = ((size_t)P * P * 3 + P) * sizeof(double);
+  const size_t smem_f = ((size_t)P * P * 3 + 3 * (size_t)P) * sizeof(double);
   if (smem_b > 48 * 1024) {
     cudaFuncSetAttribute(k_vb_b<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
     cudaFuncSetAttribute(k_vb_b<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
