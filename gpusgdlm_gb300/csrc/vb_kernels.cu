@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(kVbThreads)
   T st[PMAX];
 #pragma unroll
   for (int k = 0; k < PMAX; ++k) st[k] = T(0);
+  const bool vec_rows = (P * sizeof(T)) % 16 == 0 && (reinterpret_cast<uintptr_t>(theta) & 15) == 0;
   for (long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const T wi = (T)w[i];
     const T lam = lambda[(size_t)j * n + i];
@@ -188,9 +189,28 @@ __global__ void __launch_bounds__(kVbThreads)
     sl += wl;
     sll += wi * tlog(lam);
     const T *th = theta + ((size_t)j * n + i) * P;
+    if (vec_rows) {
+      // 16-byte loads of the row (P * sizeof(T) a multiple of 16)
+      constexpr int VW = (int)(16 / sizeof(T));
 #pragma unroll
-    for (int k = 0; k < PMAX; ++k)
-      if (k < P) st[k] += wl * th[k];
+      for (int k = 0; k < PMAX; k += VW)
+        if (k < P) {
+          T t[VW];
+          if constexpr (sizeof(T) == 4) {
+            const float4 q = *reinterpret_cast<const float4 *>(th + k);
+            t[0] = q.x, t[1] = q.y, t[2] = q.z, t[3] = q.w;
+          } else {
+            const double2 q = *reinterpret_cast<const double2 *>(th + k);
+            t[0] = q.x, t[1] = q.y;
+          }
+#pragma unroll
+          for (int e = 0; e < VW; ++e) st[k + e] += wl * t[e];
+        }
+    } else {
+#pragma unroll
+      for (int k = 0; k < PMAX; ++k)
+        if (k < P) st[k] += wl * th[k];
+    }
   }
   // all P + 2 sums in one round: warp shuffles in the working precision, one
   // shared-memory exchange, and thread k adds the eight warps' partials in FP64
