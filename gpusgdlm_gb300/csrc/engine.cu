@@ -602,9 +602,21 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
   if (!use_existing)
     sample_draws<T>(h, h->fm_t.ptr, h->fC_t.ptr, h->fn_t.ptr, h->fs_t.ptr, key);
   CK(cudaEventRecord(h->ev[1], s));
-  lu_draws<T>(h, h->x_t.ptr, key, h->y_fc.ptr);
+  // a page-locked, device-mapped destination receives the draws straight from the
+  // LU kernels (over the host link while they run); any other goes through y_fc
+  double *ydst = h->y_fc.ptr;
+  if (o_y) {
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, o_y) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+        pa.devicePointer != nullptr)
+      ydst = static_cast<double *>(pa.devicePointer);
+    else
+      (void)cudaGetLastError();  // pageable memory is not an error here
+  }
+  lu_draws<T>(h, h->x_t.ptr, key, ydst);
   CK(cudaEventRecord(h->ev[2], s));
-  if (o_y && (st = d2h(h, o_y, h->y_fc.ptr, n * m * sizeof(double)))) return st;
+  if (o_y && ydst == h->y_fc.ptr && (st = d2h(h, o_y, h->y_fc.ptr, n * m * sizeof(double))))
+    return st;
   std::vector<T> lam, th;
   if (o_lambda) {
     lam.resize(m * n);

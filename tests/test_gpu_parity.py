@@ -110,6 +110,37 @@ def test_forecast_fp64_matches_reference(built_lib, golden, name):
     np.testing.assert_allclose(out["y"], g["y_ref"].T, rtol=1e-9, atol=1e-11)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_forecast_into_page_locked_buffer(built_lib, golden, precision):
+    """A page-locked destination receives the forecast draws straight from the LU
+    kernels; they equal the copied-back draws of a pageable destination."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    g = golden("readme_vb_forecast.npz")
+    n, seed, epoch = int(g["n"]), int(g["seed"]), int(g["epoch"])
+    P, m = g["sp"].shape
+    s = model_from(g, precision, seed=seed, epoch=epoch)
+    s.setPriorParameters(g["m_t"], g["C_t"], g["n_t"], g["s_t"])
+    assert s._ensure_sim(n, n)
+    lib, h = s._lib, s._h
+    dp = C.POINTER(C.c_double)
+    x = np.asfortranarray(g["x"], dtype=np.float64)
+
+    def run(buf):
+        s.setRngState(seed, epoch)
+        assert lib.sgdlm_init_forecast_priors(h) == 0
+        assert lib.sgdlm_compute_forecast(h, buf.ctypes.data_as(dp), x.ctypes.data_as(dp),
+                                          None, None, 0) == 0
+
+    pageable = np.full(m * n, np.nan)
+    run(pageable)
+    locked = torch.full((m * n,), float("nan"), dtype=torch.float64).pin_memory().numpy()
+    run(locked)
+    assert np.isfinite(pageable).all()
+    np.testing.assert_array_equal(locked, pageable)
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_forecast_mixed_refined(built_lib, golden, name):
     g = golden(f"{name}_vb_forecast.npz")
