@@ -116,6 +116,9 @@ int sgdlm_evolve_forecast_samples(sgdlm_handle h);                              
  * evolution of forecast draws with theta = G theta before adding chol(W)' omega. */
 int sgdlm_compute_evo_prior(sgdlm_handle h, const double *G_tp1, int evolve_forecast_variables);
 int sgdlm_evolve_forecast_samples_evo(sgdlm_handle h, const double *G_tp1);
+/* y_tp1 (m x nsim, draw-major) in page-locked, device-mapped host memory (e.g.
+ * cudaHostAlloc) is written by the LU kernels directly over the host link; any
+ * other destination receives a copy after them.  The values are the same. */
 int sgdlm_compute_forecast(sgdlm_handle h, double *y_tp1, const double *x_tp1,
                            double *lambdas, double *thetas,
                            int use_existing_lambdas_and_thetas);                   /* :949 */
