@@ -341,10 +341,16 @@ def cpu_baseline(args):
     sample = args.cpu_sample
     secs = run_cpu(args.m, None, sample, threads, args.seed)
     per_step = secs * (args.nsim / sample)  # LU work and moments are linear in draws
+    # the same on one thread, on a tenth of the sample
+    sample1 = max(50, sample // 10)
+    secs1 = run_cpu(args.m, None, sample1, 1, args.seed)
     return {"value": 1.0 / per_step, "unit": "time-steps/s", "cores": threads, "kind": "port",
             "sample": f"one full step with {sample} VB + {sample} forecast draws at m={args.m} "
                       f"in {secs:.2f} s on {threads} threads (FP64 oracle, OpenMP), "
-                      f"scaled linearly to {args.nsim} draws"}
+                      f"scaled linearly to {args.nsim} draws",
+            "single_thread": {"value": 1.0 / (secs1 * (args.nsim / sample1)), "unit": "time-steps/s",
+                              "sample": f"{sample1} VB + {sample1} forecast draws in {secs1:.2f} s "
+                                        f"on 1 thread, scaled linearly to {args.nsim} draws"}}
 
 
 # --------------------------------------------------------------------- main
