@@ -109,7 +109,8 @@ struct sgdlm_engine {
   DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
   DevBuf<uint32_t> dev_epoch;
   LuPlan plan{};
-  int chunks = 0;
+  int chunks = 0;          // VB draw chunks and draws per chunk (vb_chunking)
+  long chunk_draws = 0;
   cudaEvent_t ev[8] = {};
 
   void log(int level, const char *fmt, ...) {
@@ -416,7 +417,7 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   if (st) return st;
   release_sim(h);
   h->plan = pl;
-  h->chunks = (int)vb_chunks((long)nsim);
+  vb_chunking((long)nsim, (int)m, h->num_sms, &h->chunks, &h->chunk_draws);
   CK(h->lambda.alloc(m * nsim * ts));
   CK(h->theta.alloc(m * nsim * P * ts));
   CK(h->theta_dm.alloc(m * nsim * P * ts));
@@ -513,7 +514,7 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
 template <typename T> void vb_moments(sgdlm_engine *h, double *w) {
   const int m = (int)h->m, P = (int)h->P;
   const long n = (long)h->nsim;
-  VbScratch scr{h->part_a.ptr, h->part_b.ptr, h->chunks, 0};
+  VbScratch scr{h->part_a.ptr, h->part_b.ptr, h->chunks, h->chunk_draws};
   launch_vb<T>(h->stream, m, P, n, h->p.ptr, h->n_t.ptr, h->s_t.ptr, w, as<T>(h->lambda),
                as<T>(h->theta), scr, h->mean_m.ptr, h->mean_C.ptr, h->mean_n.ptr,
                h->mean_s.ptr, h->mean_lambda.ptr, h->mean_log_lambda.ptr, h->mean_Q.ptr,

@@ -148,9 +148,11 @@ struct VbScratch {
   double *part_a;   // chunks x m x (P + 2)
   double *part_b;   // chunks x m x P*P
   int chunks;
-  int chunk_draws;
+  long chunk_draws;  // draws per chunk (a multiple of the passes' 128-draw sub-chunk)
 };
-size_t vb_chunks(long n);
+// The VB passes run one block per (chunk of draws, series); the chunks are sized
+// for the SM count (about two full waves of blocks).
+void vb_chunking(long n, int m, int num_sms, int *chunks, long *chunk_draws);
 template <typename T>
 void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p,
                const double *n_t, const double *s_t, const double *w, const T *lambda,

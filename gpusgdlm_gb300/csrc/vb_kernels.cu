@@ -24,7 +24,6 @@
 namespace sgdlm {
 namespace {
 
-constexpr int kChunk = 2048;
 constexpr int kVbThreads = 256;
 constexpr int kSub = 128;
 
@@ -171,12 +170,13 @@ template <> __device__ __forceinline__ double tsqrt<double>(double v) { return s
 // Pass A: per (chunk, series): sum w lambda, sum w log lambda, sum w lambda theta_k.
 template <typename T, int PMAX>
 __global__ void __launch_bounds__(kVbThreads)
-    k_vb_a(int m, int P, long n, const double *__restrict__ w, const T *__restrict__ lambda,
-           const T *__restrict__ theta, double *__restrict__ part_a) {
+    k_vb_a(int m, int P, long n, long chunk, const double *__restrict__ w,
+           const T *__restrict__ lambda, const T *__restrict__ theta,
+           double *__restrict__ part_a) {
   __shared__ double red[32];
   const int j = blockIdx.y, c = blockIdx.x;
-  const long i0 = (long)c * kChunk;
-  const long i1 = min(n, i0 + kChunk);
+  const long i0 = (long)c * chunk;
+  const long i1 = min(n, i0 + chunk);
   T sl = T(0), sll = T(0);
   T st[PMAX];
 #pragma unroll
@@ -283,7 +283,7 @@ __device__ __forceinline__ void load4(const double *a, double *v) {
 
 template <typename T, int PMAX>
 __global__ void __launch_bounds__(kVbThreads)
-    k_vb_b(int m, int P, long n, const unsigned *__restrict__ p,
+    k_vb_b(int m, int P, long n, long chunk, const unsigned *__restrict__ p,
            const double *__restrict__ w, const T *__restrict__ lambda,
            const T *__restrict__ theta, const double *__restrict__ mbar_full,
            double *__restrict__ part_b) {
@@ -313,8 +313,8 @@ __global__ void __launch_bounds__(kVbThreads)
 #pragma unroll
   for (int q = 0; q < 16; ++q) acc[q] = T(0);
   __syncthreads();
-  const long i0 = (long)c * kChunk;
-  const long i1 = min(n, i0 + kChunk);
+  const long i0 = (long)c * chunk;
+  const long i1 = min(n, i0 + chunk);
   for (long s0 = i0; s0 < i1; s0 += kSub) {
     const int cnt = (int)min((long)kSub, i1 - s0);
     const T *thb = theta + ((size_t)j * n + s0) * P;
@@ -541,7 +541,17 @@ __global__ void k_vb_fin(int m, int P, int chunks, const unsigned *__restrict__ 
 
 }  // namespace
 
-size_t vb_chunks(long n) { return (size_t)((n + kChunk - 1) / kChunk); }
+void vb_chunking(long n, int m, int num_sms, int *chunks, long *chunk_draws) {
+  // about two full waves of the second-moment pass (four 256-thread blocks per SM)
+  long c = ((long)num_sms * 8 + m / 2) / (m > 0 ? m : 1);
+  if (c < 1) c = 1;
+  long d = (n + c - 1) / c;
+  d = (d + kSub - 1) / kSub * kSub;
+  if (d < kSub) d = kSub;
+  c = (n + d - 1) / d;
+  *chunks = (int)(c < 1 ? 1 : c);
+  *chunk_draws = d;
+}
 
 void launch_weights(cudaStream_t s, long n, const double *logdet, double *w, double *out6,
                     double *part) {
@@ -560,15 +570,16 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
                double *mean_s, double *mean_lambda, double *mean_log_lambda,
                double *mean_Q, int *series_flags) {
   const int chunks = scr.chunks;
+  const long chunk = scr.chunk_draws;
   dim3 grid((unsigned)chunks, (unsigned)m);
   if (P <= 8)
-    k_vb_a<T, 8><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+    k_vb_a<T, 8><<<grid, kVbThreads, 0, s>>>(m, P, n, chunk, w, lambda, theta, scr.part_a);
   else if (P <= 16)
-    k_vb_a<T, 16><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+    k_vb_a<T, 16><<<grid, kVbThreads, 0, s>>>(m, P, n, chunk, w, lambda, theta, scr.part_a);
   else if (P <= 32)
-    k_vb_a<T, 32><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+    k_vb_a<T, 32><<<grid, kVbThreads, 0, s>>>(m, P, n, chunk, w, lambda, theta, scr.part_a);
   else
-    k_vb_a<T, 64><<<grid, kVbThreads, 0, s>>>(m, P, n, w, lambda, theta, scr.part_a);
+    k_vb_a<T, 64><<<grid, kVbThreads, 0, s>>>(m, P, n, chunk, w, lambda, theta, scr.part_a);
   // mbar_full lives in mean_m's slot until the refit overwrites it with the cut mean;
   // a separate buffer keeps the kernels independent.
   double *mbar_full = scr.part_a + (size_t)chunks * m * (P + 2);
@@ -586,7 +597,7 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
   if (smem_f > 48 * 1024)
     cudaFuncSetAttribute(k_vb_fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
 #define SGDLM_VB_B(PM)                                                                \
-  k_vb_b<T, PM><<<grid, kVbThreads, smem_b, s>>>(m, P, n, p, w, lambda, theta, mbar_full, \
+  k_vb_b<T, PM><<<grid, kVbThreads, smem_b, s>>>(m, P, n, chunk, p, w, lambda, theta, mbar_full, \
                                                  scr.part_b)
   if (P <= 8)
     SGDLM_VB_B(8);
