@@ -370,6 +370,140 @@ __global__ void __launch_bounds__(kVbThreads)
   }
 }
 
+// Asynchronous global -> shared copies of 16, 8 or 4 bytes (cp.async), committed
+// as groups; wait_group<N> returns when at most N of this thread's groups are in
+// flight.
+__device__ __forceinline__ void cpa16(void *sm, const void *g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(sm)), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa8(void *sm, const void *g) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(sm)), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa4(void *sm, const void *g) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(sm)), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Pass B for FP32 draws: the same tiles and sums as k_vb_b, with the draws of the
+// next sub-chunk (theta rows, w, lambda) copied into a second shared buffer by
+// cp.async while the current one is accumulated, so that a block always has a
+// sub-chunk in flight from HBM.
+__global__ void __launch_bounds__(kVbThreads)
+    k_vb_b_f32(int m, int P, long n, long chunk, const unsigned *__restrict__ p,
+               const double *__restrict__ w, const float *__restrict__ lambda,
+               const float *__restrict__ theta, const double *__restrict__ mbar_full,
+               double *__restrict__ part_b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int j = blockIdx.y, c = blockIdx.x;
+  const int pj = (int)min((unsigned)P, p[j]);
+  const int PX = (P + 3) / 4 * 4;
+  const int RS = (kSub * P + 3) / 4 * 4;  // one raw sub-chunk of theta
+  const int nb = (pj + 3) / 4, ntiles = nb * (nb + 1) / 2;
+  const int G = ntiles > 0 ? kVbThreads / ntiles : 0;
+  double *wbuf = reinterpret_cast<double *>(smem_raw);  // 2 x kSub
+  float *raw = reinterpret_cast<float *>(wbuf + 2 * kSub);  // 2 x RS
+  float *lbuf = raw + 2 * RS;                               // 2 x kSub
+  float *X = lbuf + 2 * kSub;                               // kSub x PX
+  float *mb = X + (size_t)kSub * PX;                        // PX
+  float *sc = mb + PX;                                      // kSub
+  float *red = sc + kSub;                                   // G * ntiles * 16
+  const int tid = threadIdx.x;
+  for (int k = tid; k < PX; k += blockDim.x) mb[k] = k < P ? (float)mbar_full[(size_t)j * P + k] : 0.f;
+  if (PX > P)
+    for (int e = tid; e < kSub * PX; e += blockDim.x)
+      if (e % PX >= P) X[e] = 0.f;
+  const int t = G > 0 ? tid % ntiles : 0;
+  const int g = G > 0 ? tid / ntiles : 1 << 30;
+  int by = 0;
+  while ((by + 1) * (by + 2) / 2 <= t) ++by;
+  const int bx = t - by * (by + 1) / 2;
+  float acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = 0.f;
+  const long i0 = (long)c * chunk;
+  const long i1 = min(n, i0 + chunk);
+  const int nsub = i1 > i0 ? (int)((i1 - i0 + kSub - 1) / kSub) : 0;
+  const float *lam_j = lambda + (size_t)j * n;
+  auto issue = [&](int sub) {
+    const int b = sub & 1;
+    const long s0 = i0 + (long)sub * kSub;
+    const int cnt = (int)min((long)kSub, i1 - s0);
+    const float *src = theta + ((size_t)j * n + s0) * P;
+    float *dst = raw + b * RS;
+    const int tot = cnt * P;
+    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+      for (int q = tid; q < tot / 4; q += blockDim.x) cpa16(dst + 4 * q, src + 4 * q);
+      for (int q = tot / 4 * 4 + tid; q < tot; q += blockDim.x) cpa4(dst + q, src + q);
+    } else {
+      for (int q = tid; q < tot; q += blockDim.x) cpa4(dst + q, src + q);
+    }
+    for (int q = tid; q < cnt; q += blockDim.x) {
+      cpa8(wbuf + b * kSub + q, w + s0 + q);
+      cpa4(lbuf + b * kSub + q, lam_j + s0 + q);
+    }
+    cpa_commit();
+  };
+  if (nsub > 0) issue(0);
+  if (nsub > 1) issue(1);
+  for (int sub = 0; sub < nsub; ++sub) {
+    const int b = sub & 1;
+    const long s0 = i0 + (long)sub * kSub;
+    const int cnt = (int)min((long)kSub, i1 - s0);
+    if (sub + 1 < nsub)
+      cpa_wait<1>();
+    else
+      cpa_wait<0>();
+    __syncthreads();
+    const float *cur = raw + b * RS;
+    for (int s = tid; s < cnt; s += blockDim.x)
+      sc[s] = sqrtf((float)wbuf[b * kSub + s] * lbuf[b * kSub + s]);
+    __syncthreads();
+    for (int e = tid; e < cnt * P; e += blockDim.x) {
+      const int s = e / P, k = e - s * P;
+      X[s * PX + k] = sc[s] * (cur[e] - mb[k]);
+    }
+    __syncthreads();
+    // buffer b is free: the sub-chunk after next goes into it
+    if (sub + 2 < nsub) issue(sub + 2);
+    if (g < G) {
+      for (int s = g; s < cnt; s += G) {
+        float xa[4], xb[4];
+        load4(X + s * PX + 4 * bx, xa);
+        load4(X + s * PX + 4 * by, xb);
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 4; ++bb) acc[4 * a + bb] += xa[a] * xb[bb];
+      }
+    }
+    __syncthreads();
+  }
+  if (g < G) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) red[((size_t)g * ntiles + t) * 16 + q] = acc[q];
+  }
+  __syncthreads();
+  double *out = part_b + ((size_t)c * m + j) * P * P;
+  for (int e = tid; e < ntiles * 16; e += blockDim.x) {
+    const int tt = e / 16, q = e % 16;
+    int yy = 0;
+    while ((yy + 1) * (yy + 2) / 2 <= tt) ++yy;
+    const int xx = tt - yy * (yy + 1) / 2;
+    const int x = 4 * xx + q / 4, y = 4 * yy + q % 4;
+    if (x <= y && y < pj) {
+      double vv = 0.0;
+      for (int gg = 0; gg < G; ++gg) vv += (double)red[((size_t)gg * ntiles + tt) * 16 + q];
+      out[x + P * y] = vv;
+    }
+  }
+}
+
 // The reference's digamma and trigamma (kernel_functions.cuh:1006-1022): the
 // asymptotic (Stirling) series truncated after the x^-14 and x^-9 terms, applied
 // at any x.  Reproduced as is, including its error at small x.
@@ -599,7 +733,24 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
 #define SGDLM_VB_B(PM)                                                                \
   k_vb_b<T, PM><<<grid, kVbThreads, smem_b, s>>>(m, P, n, chunk, p, w, lambda, theta, mbar_full, \
                                                  scr.part_b)
-  if (P <= 8)
+  bool done_b = false;
+  if constexpr (sizeof(T) == 4) {
+    const size_t RS = ((size_t)kSub * P + 3) / 4 * 4;
+    const size_t smem_a = 2 * kSub * sizeof(double) +
+                          (2 * RS + 2 * kSub + (size_t)kSub * PX + PX + kSub + (size_t)kVbThreads * 16) *
+                              sizeof(float);
+    if (smem_a <= 200 * 1024) {
+      if (smem_a > 48 * 1024)
+        cudaFuncSetAttribute(k_vb_b_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a);
+      k_vb_b_f32<<<grid, kVbThreads, smem_a, s>>>(m, P, n, chunk, p, w,
+                                                  reinterpret_cast<const float *>(lambda),
+                                                  reinterpret_cast<const float *>(theta), mbar_full,
+                                                  scr.part_b);
+      done_b = true;
+    }
+  }
+  if (done_b) {
+  } else if (P <= 8)
     SGDLM_VB_B(8);
   else if (P <= 16)
     SGDLM_VB_B(16);
