@@ -430,6 +430,10 @@ __global__ void __launch_bounds__(kVbThreads)
   const long i1 = min(n, i0 + chunk);
   const int nsub = i1 > i0 ? (int)((i1 - i0 + kSub - 1) / kSub) : 0;
   const float *lam_j = lambda + (size_t)j * n;
+  // the X-build layout: xstep rows at a time, one column per thread (P <= 256)
+  const int xstep = (int)blockDim.x / P, xr = tid / P, xk = tid - xr * P;
+  __syncthreads();  // mb is filled
+  const float mbk = mb[xk];
   auto issue = [&](int sub) {
     const int b = sub & 1;
     const long s0 = i0 + (long)sub * kSub;
@@ -464,10 +468,9 @@ __global__ void __launch_bounds__(kVbThreads)
     for (int s = tid; s < cnt; s += blockDim.x)
       sc[s] = sqrtf((float)wbuf[b * kSub + s] * lbuf[b * kSub + s]);
     __syncthreads();
-    for (int e = tid; e < cnt * P; e += blockDim.x) {
-      const int s = e / P, k = e - s * P;
-      X[s * PX + k] = sc[s] * (cur[e] - mb[k]);
-    }
+    // thread (xr, xk) fills column xk of rows xr, xr + xstep, ... (no division)
+    if (xr < xstep)
+      for (int s = xr; s < cnt; s += xstep) X[s * PX + xk] = sc[s] * (cur[s * P + xk] - mbk);
     __syncthreads();
     // buffer b is free: the sub-chunk after next goes into it
     if (sub + 2 < nsub) issue(sub + 2);
