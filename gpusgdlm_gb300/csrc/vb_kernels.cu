@@ -245,20 +245,22 @@ __global__ void k_vb_a_fin(int m, int P, int chunks, const double *__restrict__ 
                            double *__restrict__ mean_lambda,
                            double *__restrict__ mean_log_lambda,
                            double *__restrict__ mbar_full) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per series, lane k < P + 2 adds partial k over the chunks in order
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (j >= m) return;
-  double sl = 0.0, sll = 0.0;
-  for (int c = 0; c < chunks; ++c) {
-    const double *pa = part_a + ((size_t)c * m + j) * (P + 2);
-    sl += pa[0];
-    sll += pa[1];
-  }
-  mean_lambda[j] = sl;
-  mean_log_lambda[j] = sll;
-  for (int k = 0; k < P; ++k) {
-    double st = 0.0;
-    for (int c = 0; c < chunks; ++c) st += part_a[((size_t)c * m + j) * (P + 2) + 2 + k];
-    mbar_full[(size_t)j * P + k] = st / sl;
+  double sl = 0.0;  // E_w lambda: partial 0, lane 0 of the first round
+  for (int k0 = 0; k0 < P + 2; k0 += 32) {
+    const int k = k0 + lane;
+    double v = 0.0;
+    if (k < P + 2)
+      for (int c = 0; c < chunks; ++c) v += part_a[((size_t)c * m + j) * (P + 2) + k];
+    if (k0 == 0) {
+      sl = __shfl_sync(0xffffffffu, v, 0);
+      if (lane == 0) mean_lambda[j] = v;
+      if (lane == 1) mean_log_lambda[j] = v;
+    }
+    if (k >= 2 && k < P + 2) mbar_full[(size_t)j * P + (k - 2)] = v / sl;
   }
 }
 
@@ -720,8 +722,8 @@ void launch_vb(cudaStream_t s, int m, int P, long n, const unsigned *p, const do
   // mbar_full lives in mean_m's slot until the refit overwrites it with the cut mean;
   // a separate buffer keeps the kernels independent.
   double *mbar_full = scr.part_a + (size_t)chunks * m * (P + 2);
-  k_vb_a_fin<<<(m + 127) / 128, 128, 0, s>>>(m, P, chunks, scr.part_a, mean_lambda,
-                                             mean_log_lambda, mbar_full);
+  k_vb_a_fin<<<(m + 3) / 4, 128, 0, s>>>(m, P, chunks, scr.part_a, mean_lambda,
+                                         mean_log_lambda, mbar_full);
   const size_t PX = (size_t)(P + 3) / 4 * 4;
   const size_t smem_b = ((size_t)kSub * PX + PX + kSub + (size_t)kVbThreads * 16) * sizeof(T);
   const size_t smem_f = ((size_t)P * P * 3 + 3 * (size_t)P) * sizeof(double);
