@@ -489,7 +489,7 @@ void sample_draws(sgdlm_engine *h, const double *m_t, const double *C_t, const d
 }
 
 template <typename T>
-void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
+int lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   const long n = (long)h->nsim;
   const bool refine = (h->precision != SGDLM_PRECISION_FP64);
   const GammaRows rows{h->g_rowptr.ptr, h->g_ent.ptr, h->g_extptr.ptr, h->g_extk.ptr};
@@ -501,7 +501,7 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
     h->launches += 2;
   }
   // the fast pass appends the draws it flags to pivot_list; the redo visits those
-  cudaMemsetAsync(h->pivot_list.ptr, 0, sizeof(int), h->stream);
+  CK(cudaMemsetAsync(h->pivot_list.ptr, 0, sizeof(int), h->stream));
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
                as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
                refine, y, rows, x ? h->nu_fc.ptr : nullptr, h->pivot_list.ptr);
@@ -509,6 +509,7 @@ void lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
                         as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
                         as<T>(h->lambda), key, y, rows, h->pivot_list.ptr);
   h->launches += 2;
+  return SGDLM_OK;
 }
 
 template <typename T> void vb_moments(sgdlm_engine *h, double *w) {
@@ -555,20 +556,20 @@ int vb_posterior(sgdlm_engine *h, double *o_m, double *o_C, double *o_n, double 
                  double *o_w, double *o_sum) {
   const size_t m = h->m, P = h->P, n = h->nsim;
   cudaStream_t s = h->stream;
+  int st;
   const RngKey key = h->key((uint32_t)h->epoch);
   h->epoch += 1;
   CK(cudaEventRecord(h->ev[0], s));
   CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
   sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, key);
   CK(cudaEventRecord(h->ev[1], s));
-  lu_draws<T>(h, nullptr, key, nullptr);
+  if ((st = lu_draws<T>(h, nullptr, key, nullptr))) return st;
   CK(cudaEventRecord(h->ev[2], s));
   launch_weights(s, (long)n, h->logdet.ptr, h->w.ptr, h->stats6.ptr, h->wpart.ptr);
   h->launches += 3;
   CK(cudaEventRecord(h->ev[3], s));
   vb_moments<T>(h, h->w.ptr);
   CK(cudaEventRecord(h->ev[4], s));
-  int st;
   if (o_m && (st = d2h(h, o_m, h->mean_m.ptr, P * m * sizeof(double)))) return st;
   if (o_C && (st = d2h(h, o_C, h->mean_C.ptr, P * P * m * sizeof(double)))) return st;
   if (o_n && (st = d2h(h, o_n, h->mean_n.ptr, m * sizeof(double)))) return st;
@@ -614,7 +615,7 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
     else
       (void)cudaGetLastError();  // pageable memory is not an error here
   }
-  lu_draws<T>(h, h->x_t.ptr, key, ydst);
+  if ((st = lu_draws<T>(h, h->x_t.ptr, key, ydst))) return st;
   CK(cudaEventRecord(h->ev[2], s));
   if (o_y && ydst == h->y_fc.ptr && (st = d2h(h, o_y, h->y_fc.ptr, n * m * sizeof(double))))
     return st;
@@ -707,7 +708,8 @@ int filter_step(sgdlm_engine *h, const double *d_y, const double *d_F, const dou
   h->launches += 1;
   CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
   sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, key_vb);
-  lu_draws<T>(h, nullptr, key_vb, nullptr);
+  int st = lu_draws<T>(h, nullptr, key_vb, nullptr);
+  if (st) return st;
   launch_weights(s, n, h->logdet.ptr, w, h->stats6.ptr, h->wpart.ptr);
   vb_moments<T>(h, w);
   launch_gate(s, m, P, h->stats6.ptr, ess_threshold, h->mean_m.ptr, h->mean_C.ptr,
@@ -716,11 +718,11 @@ int filter_step(sgdlm_engine *h, const double *d_y, const double *d_F, const dou
   launch_prior(s, m, P, h->p.ptr, h->C_t.ptr, h->n_t.ptr, h->W_t.ptr, h->beta.ptr, h->delta.ptr);
   h->launches += 5;  // three for the weights, the gate, the prior
   if (d_x) {
-    int st = copy_forecast_priors(h);
+    st = copy_forecast_priors(h);
     if (st) return st;
     CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
     sample_draws<T>(h, h->fm_t.ptr, h->fC_t.ptr, h->fn_t.ptr, h->fs_t.ptr, key_fc);
-    lu_draws<T>(h, d_x, key_fc, yout);
+    if ((st = lu_draws<T>(h, d_x, key_fc, yout))) return st;
   }
   if (d_stats) {
     // {ESS, sum_det, accepted, max_log_det, n_finite, sum_w2}
