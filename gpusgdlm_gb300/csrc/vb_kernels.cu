@@ -9,10 +9,12 @@
 // whose only consumer is the weighted mean Q_bar_j (compute_mean_Q_t :1088-1100).
 //
 // Here:
-//  * weights are exp(logdet - max) / sum in FP64 (log-sum-exp), one block;
+//  * weights are exp(logdet - max) / sum in FP64 (log-sum-exp), three short
+//    multi-block launches (max, exponentials, normalisation);
 //  * pass A and pass B reduce over draws with one block per (series, chunk of
-//    2048 draws), coalesced over the series-major draw buffers, warp-shuffle
-//    block reductions, FP64 chunk partials;
+//    draws; the chunks are sized for the SM count), coalesced over the
+//    series-major draw buffers, FP64 chunk partials; pass B for FP32 draws keeps
+//    the next 128-draw sub-chunk in flight by cp.async;
 //  * Q_bar_j is evaluated as trace(V^-1 V): since V = sum_i w_i theta~_i theta~_i'
 //    with the same weights, sum_i w_i theta~_i' V^-1 theta~_i = tr(V^-1 V)
 //    exactly, so the m*n quadratic forms of the reference collapse to a p x p
