@@ -16,24 +16,28 @@
 //  2. Block elimination of the core with 32 x 32 blocks, no chains of
 //     dependent scalar solves:
 //     (a) one warp inverts the diagonal block D in registers by Gauss-Jordan
-//         elimination (its pivots are the LU pivots, so they give log|det|),
-//         while the other warps stage the column panel C and the row panel B
-//         in shared memory;
-//     (b) all warps form the multipliers C D^-1 (a 32-wide GEMM);
-//     (c) the trailing update E -= (C D^-1) B: a register-tiled FMA loop over
-//         (32W) x 128 tiles with 16-byte conflict-free shared and global loads.
+//         elimination with 4 x 4 pivot blocks (its pivots are the LU pivots,
+//         so they give log|det|), while the other warps stage the column panel
+//         C and the row panel B;
+//     (b) the multipliers C D^-1 and (c) the trailing update E -= (C D^-1) B:
+//         for FP32 draws and d_p <= 224 as tcgen05 MMAs (kind::f16 on a
+//         three-way bf16 split of every operand, FP32 accumulation in tensor
+//         memory, E's first 128-row tile preloaded while D is inverted, and
+//         warp 0 starting the next inversion as soon as the first tile is
+//         updated); otherwise register-tiled FMA loops over shared memory.
 //     The pass does not pivot: (I - Gamma) is diagonally dominant in the
 //     filtering regime.  Every multiplier (the levels', the diagonal blocks'
 //     and C D^-1) is checked against kPivotThreshold; a draw with a larger one,
-//     or a zero / non-finite pivot, is flagged and redone by k_lu_fallback with
-//     partial pivoting on the full matrix (getrf semantics).  |det| does not
-//     depend on the elimination order.
-//  3. Forecasts: the right-hand side goes through the levels' forward program,
-//     rides along the block elimination (b2 -= C D^-1 b1), and the back solve
-//     x1 = D^-1 (b1 - B x2) runs block by block with the stored D^-1, C D^-1 and
-//     B; then the levels' backward program.  An FP64 residual
-//     nu - (I - Gamma) y0 from the sparse parent rows drives one refinement
-//     solve with the same factors.
+//     or a zero / non-finite pivot, is appended to the redo list and redone by
+//     k_lu_fallback with partial pivoting on the full matrix (getrf
+//     semantics).  |det| does not depend on the elimination order.
+//  3. Forecasts: the right-hand sides (k_forecast_nu, all draws beforehand) go
+//     through the levels' forward program and ride along the block
+//     elimination (b2 -= C D^-1 b1); the back solve x1 = D^-1 (b1 - B x2) runs
+//     as a pipeline between warps with the stored D^-1, C D^-1 and B, then the
+//     levels' backward program (staged in shared memory).  The residual
+//     nu - (I - Gamma) y0 from the sparse parent rows (FP64, or double-float
+//     FP32 for FP32 draws) drives one refinement solve with the same factors.
 #include <algorithm>
 
 #include <cuda_bf16.h>
