@@ -44,6 +44,7 @@
 
 #include "elimination.hpp"
 #include "kernels.hpp"
+#include "mma_sync.hpp"
 #include "rng.cuh"
 
 namespace sgdlm {
@@ -539,19 +540,41 @@ __device__ __forceinline__ void write_split_chunk(unsigned char *tile, size_t pa
   *reinterpret_cast<uint4 *>(d + 2 * part_bytes) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// Bounded wait for the MMA completion barrier (a timeout sets bad, and the draw
-// is redone by the pivoting pass).
-__device__ __forceinline__ void mma_wait(uint64_t *mbar, uint32_t &mphase, bool &bad) {
+// The CTA's MMA completion barrier and its give-up flag (mma_sync.hpp).
+struct MmaSync {
+  uint64_t bar;
+  int dead;
+};
+
+__device__ __forceinline__ bool mma_poll(const MmaSync *ms, uint32_t phase, int polls) {
   uint32_t done = 0;
-  for (int it = 0; it < (1 << 22) && !done; ++it)
+  for (int it = 0; it < polls && !done; ++it)
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         "selp.u32 %0, 1, 0, p;\n}"
         : "=r"(done)
-        : "r"(smem_u32(mbar)), "r"(mphase));
-  if (!done) bad = true;
-  mphase ^= 1u;
+        : "r"(smem_u32(&ms->bar)), "r"(phase));
+  return done != 0;
+}
+
+// Bounded wait for the MMAs committed to ms->bar (the rules of mma_sync.hpp): a
+// late completion marks the draw bad and is drained so the phase stays in step;
+// a completion never seen makes the CTA give the barrier up (ms->dead).
+__device__ __forceinline__ void mma_wait(MmaSync *ms, uint32_t &mphase, bool &bad) {
+  const bool dead = *reinterpret_cast<volatile int *>(&ms->dead) != 0;
+  bool first = false, drained = false;
+  if (!dead) {
+    first = mma_poll(ms, mphase, kMmaPolls);
+    if (!first) drained = mma_poll(ms, mphase, kMmaDrainPolls);
+  }
+  if (mma_wait_rule(dead, first, drained, mphase, bad) == kMmaLost)
+    *reinterpret_cast<volatile int *>(&ms->dead) = 1;
   asm volatile("tcgen05.fence::after_thread_sync;");
+}
+
+// Whether the CTA still issues MMAs (it stops once it has given its barrier up).
+__device__ __forceinline__ bool mma_live(const MmaSync *ms) {
+  return *reinterpret_cast<const volatile int *>(&ms->dead) == 0;
 }
 
 // The six split products of one 128-row tile, K = 32 (two K-steps of 16):
@@ -585,16 +608,16 @@ __device__ __forceinline__ void umma_split_tile(uint32_t d_tmem, uint32_t la, si
 constexpr int kTmemL = 192;
 __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int r0, int R,
                                      unsigned char *Lt, size_t part_L, const unsigned char *Dt,
-                                     uint32_t tmem, uint64_t *mbar, uint32_t &mphase, float tau,
+                                     uint32_t tmem, MmaSync *mbar, uint32_t &mphase, float tau,
                                      float *z, bool solve, bool &bad) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (tid == 0) {
+  if (tid == 0 && mma_live(mbar)) {
     for (int mt = 0; mt < R; mt += 128)
       umma_split_tile(tmem + kTmemL + (uint32_t)(mt / 128) * kB, smem_u32(Lt) + (uint32_t)(mt / 8) * 512,
                       part_L, smem_u32(Dt), (size_t)kB * 64, umma_idesc(kB, false), false);
     asm volatile(
         "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(mbar)));
+            smem_u32(&mbar->bar)));
   }
   mma_wait(mbar, mphase, bad);
   const int tile = warp >> 2, quarter = warp & 3;
@@ -740,7 +763,7 @@ __device__ __forceinline__ void tc_preload_tile0(const float *A, int dp, int r0,
 // next diagonal block from the first tile, and the update ends on __syncthreads.
 __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
                                    const unsigned char *Lt, const unsigned char *Ut,
-                                   size_t part_L, size_t part_U, uint32_t tmem, uint64_t *mbar,
+                                   size_t part_L, size_t part_U, uint32_t tmem, MmaSync *mbar,
                                    uint32_t &mphase, bool &bad, float *dnext) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3;
@@ -753,12 +776,12 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
   // ---- tile 0: rows 0..127 (in tensor memory already)
   {
     const int row = quarter * 32 + lane;
-    if (tid == 0) {
+    if (tid == 0 && mma_live(mbar)) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       umma_split_tile(tmem, smem_u32(Lt), part_L, smem_u32(Ut), part_U, idesc, true);
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(mbar)));
+              smem_u32(&mbar->bar)));
     }
     mma_wait(mbar, mphase, bad);
     if (warp == 0) {
@@ -803,13 +826,13 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
     if (128 + quarter * 32 < R) e_to_tmem(E, dp, R, row, cb, ce, tlane);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (tid == 0) {
+    if (tid == 0 && mma_live(mbar)) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       umma_split_tile(tmem, smem_u32(Lt) + (uint32_t)(128 / 8) * 512, part_L, smem_u32(Ut), part_U,
                       idesc, true);
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-              smem_u32(mbar)));
+              smem_u32(&mbar->bar)));
     }
     mma_wait(mbar, mphase, bad);
     if (128 + quarter * 32 < R) tmem_to_e(E, dp, R, row, cb, ce, tlane);
@@ -1465,7 +1488,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   // tensor-core trailing updates (FP32 draws, d_p <= 224): 256 columns of tensor
   // memory for this CTA and the MMA completion barrier
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ __align__(8) MmaSync s_mbar;
   uint32_t mphase = 0;
   if constexpr (TC) {
     if (warp == 0) {
@@ -1473,7 +1496,10 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
           smem_u32(&s_tmem)));
       asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_mbar)));
+    if (tid == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s_mbar.bar)));
+      s_mbar.dead = 0;
+    }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");

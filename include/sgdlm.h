@@ -170,10 +170,11 @@ int sgdlm_filter_step_device(sgdlm_handle h, const double *d_y, const double *d_
  * engine stores them; d_sp the parental sets (max_p x m, as in
  * sgdlm_set_parental_sets); d_log_det (n doubles) and d_flags (n ints, per-draw
  * status bits) receive the results.  The LU working matrices live in a 16 MiB
- * static device array instead of allocated scratch, which limits m to 2048.
- * The first call on a device looks that array up (make it outside stream
- * capture); calls that overlap on the GPU share the array and race.  Runs on
- * `stream` (a cudaStream_t) and returns without synchronising. */
+ * static device array instead of allocated scratch.  m is at most 736 (the LU
+ * block's shared memory; larger m returns SGDLM_ERR_UNSUPPORTED) and max_p at
+ * most 64.  The first call in each CUDA context looks that array up (make it
+ * outside stream capture); calls that overlap on the GPU share the array and
+ * race.  Runs on `stream` (a cudaStream_t) and returns without synchronising. */
 int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const float *d_theta,
                           const unsigned *d_sp, double *d_log_det, int *d_flags, void *stream);
 /* The handle's CUDA stream (cudaStream_t), for events and graph capture. */

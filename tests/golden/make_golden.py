@@ -1,7 +1,7 @@
 """Generates tests/golden/*.npz from the reference's own kernels run on the CPU.
 
-Run here (needs the reference sources):  python tests/golden/make_golden.py
-It builds oracle/_ref/libref_kernels.so with oracle/build_ref.sh, feeds the
+Run with the reference checkout:  python tests/golden/make_golden.py <reference checkout>
+(or SGDLM_REFERENCE=<checkout>).  It builds oracle/_ref/libref_kernels.so with oracle/build_ref.sh, feeds the
 reference's kernels (rSGDLM/src/kernel_functions.cuh, launched with the
 shapes of rSGDLM/src/SGDLM/SGDLM.cu) seeded inputs, and stores inputs and outputs.
 Where the reference consumes cuRAND output, the inputs are the GB300 library's
@@ -28,8 +28,18 @@ NA = 2147483648  # R's NA_integer_ read as unsigned (memory_manager_RCPP.hpp:31-
 TAG_THETA, TAG_NU, TAG_OMEGA = 2, 3, 6
 
 
+def reference_checkout():
+    import os
+
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SGDLM_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> (or set SGDLM_REFERENCE)")
+    return ref
+
+
 def ref_lib():
-    subprocess.run([str(ROOT / "oracle" / "build_ref.sh")], check=True, capture_output=True)
+    subprocess.run([str(ROOT / "oracle" / "build_ref.sh"), reference_checkout()], check=True,
+                   capture_output=True)
     L = C.CDLL(str(ROOT / "oracle" / "_ref" / "libref_kernels.so"))
     d, i, l = C.c_double, C.c_int, C.c_long
     Pd, Pu = C.POINTER(C.c_double), C.POINTER(C.c_uint)
