@@ -14,9 +14,11 @@ beta = 0.97, Delta = 0.98.  Seeds are recorded in the output line.
   e2e   : the same steps through the C ABI with host buffers (pinned), H2D of
           y_t, F_t, F_t+1 and D2H of the VB results and the forecast draws inside
           the timed region.
+  fp64_gpu : the plain FP64 form (every kernel in FP64) on the same workload.
 --impl reference runs the FP64 CPU implementation of the same step (the oracle
 port: the reference has no CPU path and its CUDA build cannot be built on the
-Arm GPU host) on a bounded sample of draws, on all host cores.
+Arm GPU host) on all host cores: whole time steps at the full draw counts after
+a reduced-draw burn-in; the line reports the steps that ran.
 """
 from __future__ import annotations
 
@@ -151,7 +153,7 @@ def run_gpu(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    T_total = args.burn_in + args.warmup + args.steps + args.e2e_steps + 8
+    T_total = args.burn_in + args.warmup + args.steps + args.e2e_steps + args.fp64_steps + 12
     wl = make_workload(m=args.m, T=T_total, seed=args.seed + rank)
     m, P, n = wl["m"], wl["P"], args.nsim
     s = SGDLM(1, strict=True, precision=args.precision)
@@ -224,12 +226,62 @@ def run_gpu(args, rank, world):
     info = s.getEliminationInfo()
     dpad = (info["core_n"] + 31) // 32 * 32
     exec_flops = n * (2.0 / 3.0 * dpad ** 3)
-    return dict(ms=ms, launches=launches, clocks=clk, accepted=accepted, ess=ess_last,
+    fp64 = None
+    if args.precision == "mixed" and args.fp64_steps > 0:
+        t_next = nsteps + 1 + args.e2e_steps + 2 + 3
+        fp64 = run_fp64_form(args, s, wl, t_next, dev, rank)
+    return dict(ms=ms, launches=launches, clocks=clk, accepted=accepted, ess=ess_last, fp64=fp64,
                 exec_flops=exec_flops, core_n=info["core_n"], levels=info["levels"],
                 lu_ms=statistics.median(lu_ms), vb_ms=statistics.median(vb_ms),
                 sample_ms=statistics.median(sample_ms), fc_ms=statistics.median(fc_ms),
                 pivoted=int(max(pivoted)), e2e=e2e, m=m, P=P,
                 ess_per_s=statistics.median(ess_rate))
+
+
+def run_fp64_form(args, s_mixed, wl, t0, dev, rank):
+    """The plain FP64 form (every kernel in FP64, the reference's arithmetic) on
+    the same workload, continuing from the mixed engine's current prior state:
+    fused device steps with inputs staged in HBM, CUDA events on the engine's
+    stream."""
+    import torch
+
+    from gpusgdlm_gb300 import SGDLM
+
+    m, P, n = wl["m"], wl["P"], args.nsim
+    st = s_mixed.getParameters()
+    s = SGDLM(1, strict=True, precision="fp64")
+    s.setSimultaneousParents(wl["p"], np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float))
+    s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+    s.setPriorParameters(st["m"], st["C"], st["n"], st["s"])
+    s.setRngState(5678 + 100 * rank, 0)
+    s._ensure_sim(n, n)
+    stream = torch.cuda.ExternalStream(s.stream(), device=dev)
+    k_warm, k = 1, args.fp64_steps
+    ts = range(t0, t0 + k_warm + k)
+    ys = torch.tensor(np.stack([wl["y"][t] for t in ts]), dtype=torch.float64, device=dev)
+    Fs = torch.tensor(np.stack([wl["F_of"](t).ravel(order="F") for t in ts]), dtype=torch.float64,
+                      device=dev)
+    Xs = torch.tensor(np.stack([wl["F_of"](t + 1, False).ravel(order="F") for t in ts]),
+                      dtype=torch.float64, device=dev)
+    yout = torch.zeros(n * m, dtype=torch.float64, device=dev)
+    wout = torch.zeros(n, dtype=torch.float64, device=dev)
+
+    def step(i):
+        assert s.filterStepDevice(ys[i].data_ptr(), Fs[i].data_ptr(), Xs[i].data_ptr(), n / 2.0,
+                                  yout.data_ptr(), wout.data_ptr(), None)
+
+    for i in range(k_warm):
+        step(i)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for i in range(k_warm, k_warm + k):
+        step(i)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    s.close()
+    return dict(ms=ms, steps=k)
 
 
 def run_e2e(args, s, wl, rank, world, t0):
@@ -307,26 +359,46 @@ def job_value(ms_max, steps, world):
 
 
 # --------------------------------------------------------------- CPU arms
-def run_cpu(m, P_unused, nsim_sample, threads, seed):
-    import oracle
+def cpu_filter(m, nsim, threads, seed, burn_in, burn_in_draws, warmup, steps, single=None):
+    """The FP64 oracle (tests/oracle_model.py over oracle/) running the same README
+    time step on the host cores: burn_in untimed steps with burn_in_draws draws
+    (the filter past the diffuse-prior transient, as the GPU arm), then warmup
+    untimed and `steps` timed steps at the full nsim VB + nsim forecast draws.
+    Returns the seconds of each timed step."""
+    import oracle  # noqa: F401  (builds the oracle library if needed)
 
     sys.path.insert(0, str(ROOT / "tests"))
     from oracle_model import OracleSGDLM
 
-    wl = make_workload(m=m, T=6, seed=seed)
+    wl = make_workload(m=m, T=burn_in + warmup + steps + 4, seed=seed)
     P = wl["P"]
     o = OracleSGDLM(wl["p"], wl["sp"], np.full(m, 0.97), np.full((P, P, m), 0.98), seed=77, epoch=0,
                     nthreads=threads)
     a, R, r, c = prior_arrays(m, P)
     o.set_parameters(a, R, r, c)
-    t0 = time.perf_counter()
-    o.posterior(wl["y"][1], wl["F_of"](1))
-    vb = o.vb(nsim_sample)
-    if 1.0 / np.sum(vb["IS_weights"] ** 2) > nsim_sample / 2:
-        o.set_parameters(vb["m"], vb["C"], vb["n"], vb["s"])
-    o.prior()
-    o.forecast(nsim_sample, wl["F_of"](2, False))
-    return time.perf_counter() - t0
+
+    def step(t, n):
+        o.posterior(wl["y"][t], wl["F_of"](t))
+        vb = o.vb(n)
+        if 1.0 / np.sum(vb["IS_weights"] ** 2) > n / 2:
+            o.set_parameters(vb["m"], vb["C"], vb["n"], vb["s"])
+        o.prior()
+        o.forecast(n, wl["F_of"](t + 1, False))
+
+    t = 1
+    for _ in range(burn_in):
+        step(t, burn_in_draws)
+        t += 1
+    for _ in range(warmup):
+        step(t, nsim)
+        t += 1
+    secs = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        step(t, single or nsim)
+        secs.append(time.perf_counter() - t0)
+        t += 1
+    return secs
 
 
 def host_threads():
@@ -337,20 +409,58 @@ def host_threads():
 
 
 def cpu_baseline(args):
+    """One measured full-size step of the FP64 oracle on all host threads after a
+    reduced-draw burn-in (about 15 s of host work at m = 400), plus a one-thread
+    sample scaled to the workload."""
     threads = host_threads()
-    sample = args.cpu_sample
-    secs = run_cpu(args.m, None, sample, threads, args.seed)
-    per_step = secs * (args.nsim / sample)  # LU work and moments are linear in draws
-    # the same on one thread, on a tenth of the sample
-    sample1 = max(50, sample // 10)
-    secs1 = run_cpu(args.m, None, sample1, 1, args.seed)
-    return {"value": 1.0 / per_step, "unit": "time-steps/s", "cores": threads, "kind": "port",
-            "sample": f"one full step with {sample} VB + {sample} forecast draws at m={args.m} "
-                      f"in {secs:.2f} s on {threads} threads (FP64 oracle, OpenMP), "
-                      f"scaled linearly to {args.nsim} draws",
-            "single_thread": {"value": 1.0 / (secs1 * (args.nsim / sample1)), "unit": "time-steps/s",
-                              "sample": f"{sample1} VB + {sample1} forecast draws in {secs1:.2f} s "
-                                        f"on 1 thread, scaled linearly to {args.nsim} draws"}}
+    t0 = time.perf_counter()
+    secs = cpu_filter(args.m, args.nsim, threads, args.seed, args.burn_in, args.cpu_burn_in_draws,
+                      0, 1)
+    total = time.perf_counter() - t0
+    sample1 = max(50, args.cpu_sample // 10)
+    secs1 = cpu_filter(args.m, args.nsim, 1, args.seed, 0, 0, 0, 1, single=sample1)
+    return {"value": 1.0 / secs[0], "unit": "time-steps/s", "cores": threads, "kind": "port",
+            "precision": "fp64",
+            "sample": f"one full step ({args.nsim} VB + {args.nsim} forecast draws, m={args.m}) of "
+                      f"the FP64 oracle on {threads} threads (OpenMP), measured: {secs[0]:.2f} s, "
+                      f"after {args.burn_in} burn-in steps with {args.cpu_burn_in_draws} draws "
+                      f"({total:.1f} s in all)",
+            "single_thread": {"value": 1.0 / (secs1[0] * (args.nsim / sample1)), "unit": "time-steps/s",
+                              "sample": f"{sample1} VB + {sample1} forecast draws from the prior in "
+                                        f"{secs1[0]:.2f} s on 1 thread, scaled linearly to "
+                                        f"{args.nsim} draws"}}
+
+
+def run_reference_arm(args, config):
+    """The reference arm: the FP64 CPU implementation of the step (the oracle port,
+    the reference having no CPU path of its own), on all host threads, at the full
+    workload: every timed step is one whole time step with nsim VB + nsim forecast
+    draws.  A reduced-draw burn-in first takes the filter to the GPU arm's regime;
+    warm-up and timed steps are capped (1 and 8) so that the run stays within a few
+    minutes, and the line reports the counts that ran."""
+    threads = host_threads()
+    warm = min(args.warmup, 1)
+    k = max(1, min(args.steps, args.ref_max_steps))
+    t0 = time.perf_counter()
+    secs = cpu_filter(args.m, args.nsim, threads, args.seed, args.burn_in, args.cpu_burn_in_draws,
+                      warm, k)
+    wall = time.perf_counter() - t0
+    ms = 1000.0 * sum(secs)
+    value = k / (ms / 1000.0)
+    cfg = dict(config, precision="fp64")
+    cb = {"value": value, "unit": "time-steps/s", "cores": threads, "kind": "port",
+          "sample": f"{k} full time steps ({args.nsim} VB + {args.nsim} forecast draws, m={args.m}) "
+                    f"of the FP64 oracle on {threads} threads, after {args.burn_in} untimed burn-in "
+                    f"steps with {args.cpu_burn_in_draws} draws and {warm} untimed full step; "
+                    f"{wall:.1f} s wall in all"}
+    return {"metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": args.gpus,
+            "steps": k, "warmup": warm, "ms_per_step": ms / k, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (true-SGDLM simulation)", "config": cfg, "impl": "reference",
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": "time-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "requested": {"steps": args.steps, "warmup": args.warmup}}
 
 
 # --------------------------------------------------------------------- main
@@ -366,7 +476,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--burn-in", type=int, default=30,
                     help="untimed filter steps run first to reach the steady state")
-    ap.add_argument("--cpu-sample", type=int, default=1000)
+    ap.add_argument("--cpu-sample", type=int, default=1000,
+                    help="draws of the one-thread CPU sample (a tenth of this)")
+    ap.add_argument("--cpu-burn-in-draws", type=int, default=1000,
+                    help="draws per burn-in step of the CPU arms")
+    ap.add_argument("--ref-max-steps", type=int, default=8,
+                    help="cap on the reference arm's timed full-size steps")
+    ap.add_argument("--fp64-steps", type=int, default=3,
+                    help="timed steps of the plain FP64 form (0: skip)")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -384,15 +501,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline(args)
-        line = {"metric": METRIC, "value": cb["value"], "unit": "time-steps/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (true-SGDLM simulation)", "config": config, "impl": "reference",
-                "cpu_baseline": cb,
-                "e2e": {"value": cb["value"], "unit": "time-steps/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(run_reference_arm(args, config)))
         return
 
     if world > 1:
@@ -436,6 +545,12 @@ def main():
         "draws_pivoted_max": r["pivoted"],
         "elimination": {"levels": r["levels"], "dense_core": r["core_n"]},
         "is_draws_per_s": value * args.nsim,
+        "fp64_gpu": None if r["fp64"] is None else {
+            "value": r["fp64"]["steps"] / (r["fp64"]["ms"] / 1000.0), "unit": "time-steps/s",
+            "steps": r["fp64"]["steps"], "ms_per_step": r["fp64"]["ms"] / r["fp64"]["steps"],
+            "speedup_of_value": value / (r["fp64"]["steps"] / (r["fp64"]["ms"] / 1000.0)),
+            "note": "plain FP64 form: every kernel in FP64 (draws, LU, solves, moments), "
+                    "same workload and fused device step, continuing from the mixed run's state"},
         "ess_last": r["ess"], "accepted_last": r["accepted"],
         "ess_per_s": {"plain": r["ess_per_s"], "learned": None,
                       "note": "ESS of the decoupled (plain) proposal per second of "

@@ -50,7 +50,8 @@ def test_replicas_max_over_ranks_gloo(tmp_path):
 
 def test_reference_arm_runs_on_rank0_only():
     base = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2",
-            "--m", "40", "--nsim", "200", "--cpu-sample", "50", "--steps", "1", "--warmup", "1"]
+            "--m", "40", "--nsim", "200", "--cpu-sample", "50", "--steps", "2", "--warmup", "3",
+            "--burn-in", "3", "--cpu-burn-in-draws", "50"]
     env = dict(os.environ, WORLD_SIZE="2", MASTER_ADDR="127.0.0.1")
     r1 = subprocess.run(base, env=dict(env, RANK="1"), capture_output=True, text=True, timeout=300)
     assert r1.returncode == 0 and r1.stdout.strip() == ""
@@ -60,3 +61,7 @@ def test_reference_arm_runs_on_rank0_only():
     assert line["impl"] == "reference" and line["n_gpus"] == 2
     assert line["cpu_baseline"]["kind"] == "port" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    # whole steps at the declared draw count; the line reports what ran
+    assert line["steps"] == 2 and line["warmup"] == 1
+    assert line["config"]["precision"] == "fp64" and line["config"]["nsim"] == 200
+    assert abs(line["ms_per_step"] * line["steps"] / 1000.0 * line["value"] - line["steps"]) < 1e-9
