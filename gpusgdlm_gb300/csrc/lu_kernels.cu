@@ -89,6 +89,29 @@ __device__ double block_sum_det(double v, double *red) {
   for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
   return t;
 }
+// Block-wide maxima of two non-negative values (a NaN in either counts as
+// infinity), over red (at least 2 * warps doubles).
+__device__ void block_max2(double &a, double &b, double *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  a = (a == a) ? a : INFINITY;
+  b = (b == b) ? b : INFINITY;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  __syncthreads();
+  if (lane == 0) {
+    red[2 * warp] = a;
+    red[2 * warp + 1] = b;
+  }
+  __syncthreads();
+  a = b = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    a = fmax(a, red[2 * w]);
+    b = fmax(b, red[2 * w + 1]);
+  }
+}
 
 // Shared-memory carve-up (byte offsets, 16-byte aligned).  dp is the padded
 // dense size, m the number of nodes (forecast vectors are node-indexed).  The
@@ -143,6 +166,10 @@ struct Smem {
 // correction, the row permutation, one diagonal block and the FP64 forecast
 // vectors.
 constexpr int kFbChunk = 128;
+constexpr int kFbRefine = 3;  // refinement steps of the pivoting pass's forecast solves
+// the fast pass's forecast of a draw is kept when its refinement correction is at
+// most this fraction of the solution (the error left is about its square)
+constexpr double kRefineTol = 1e-3;
 struct FallbackSmem {
   size_t off_pan, off_U, off_piv, off_pivabs, off_cand, off_D, off_z, off_d, off_perm, off_nu,
       off_res, off_red, total;
@@ -668,6 +695,7 @@ __device__ void tc_block_multipliers(float *__restrict__ A, int dp, int k0, int 
 // Named barriers of the tensor-core path (barrier 0 is __syncthreads; 1..8 are
 // the Gauss-Jordan super-steps of the FFMA path).
 constexpr int kBarRest = 9;       // warps 1..7 (224 threads)
+constexpr int kBarQuarter0 = 10;  // warps 0 and 4 (64 threads): tensor-memory lanes 0..31
 constexpr int kBarDt = 11;        // warp 0 and warps 1, 2, 3, 5 (160 threads): D^-1 -> Dt
 __device__ __forceinline__ void named_arrive_n(int id, int n) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
@@ -676,24 +704,19 @@ __device__ __forceinline__ void named_sync_n(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
-// The trailing update's product -L B of rows [row0, row0 + 32) (this warp's
-// lanes of tensor memory) is added to E in FP32 with round-to-nearest: the
-// tensor cores accumulate only the product, from zero, so their rounding of the
-// accumulation (toward zero, as the tensor cores' adder aligns and truncates)
-// acts on the small product instead of on E itself, which would shrink every
-// entry of E by about half an ulp per MMA and bias log|det| (by about -8e-5 at
-// m = 400).  Columns [cb, ce) in 8-column chunks; the E values of the next chunk
+// The two-tile update's product -L U (this warp's lanes, columns [cb, ce)) is
+// added to E in global memory in 8-column chunks: the E values of the next chunk
 // are loaded while the current one is added (the first chunk is loaded before
-// the MMA wait); the routine is not inlined, which keeps its registers out of
-// the kernel's peak.  Rows at or beyond R are padding: loaded as 0, never stored.
-constexpr int kEc = 8;  // columns per chunk of tmem_add_e
+// the MMA wait).  Not inlined: its registers stay out of the kernel's peak.  Rows
+// at or beyond R are padding: loaded as 0, never stored.
+constexpr int kEc = 8;
 __device__ __forceinline__ void e_chunk_load(const float *E, int dp, int R, int row, int c0,
                                              float (&e)[kEc]) {
 #pragma unroll
   for (int j = 0; j < kEc; ++j) e[j] = row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f;
 }
 __device__ __noinline__ void tmem_add_e(float *E, int dp, int R, int row, int cb, int ce,
-                                           uint32_t tlane, float (&e0)[kEc]) {
+                                        uint32_t tlane, float (&e0)[kEc]) {
   for (int c0 = cb; c0 < ce; c0 += kEc) {
     float e1[kEc];
     if (c0 + kEc < ce) e_chunk_load(E, dp, R, row, c0 + kEc, e1);
@@ -716,6 +739,55 @@ __device__ __noinline__ void tmem_add_e(float *E, int dp, int R, int row, int cb
   }
 }
 
+// Single-tile updates (R <= 128) keep E's tile in tensor memory: warps 1..7
+// load it into columns 0 .. R-1 while warp 0 inverts the diagonal block
+// (tc_preload_tile0), the MMAs put -L U into columns kTmemU .. kTmemU + R - 1
+// (free then: the block multipliers there have been read out), and the sum is
+// formed from the two in FP32 with round-to-nearest.
+constexpr int kTmemU = 128;
+__device__ __forceinline__ void e_to_tmem(const float *E, int dp, int R, int row, int cb, int ce,
+                                          uint32_t tlane) {
+  for (int c0 = cb; c0 < ce; c0 += 16) {
+    uint32_t v[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      v[j] = __float_as_uint(row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f);
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(tlane + (uint32_t)c0),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+        "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+        "r"(v[15]));
+  }
+  asm volatile("tcgen05.wait::st.sync.aligned;");
+}
+// 16 columns of tensor memory at taddr into v.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+}
+// E = E + (-L U), both in tensor memory, columns [cb, ce) of this warp's lanes,
+// stored to global (rows at or beyond R are not stored).
+__device__ __noinline__ void tmem_sum_to_e(float *E, int dp, int R, int row, int cb, int ce,
+                                           uint32_t tlane) {
+  for (int c0 = cb; c0 < ce; c0 += 16) {
+    uint32_t e[16], u[16];
+    tmem_ld16(tlane + (uint32_t)c0, e);
+    tmem_ld16(tlane + (uint32_t)(kTmemU + c0), u);
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
+    if (row < R) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        E[(size_t)row + (size_t)dp * (c0 + j)] = __fadd_rn(__uint_as_float(e[j]), __uint_as_float(u[j]));
+    }
+  }
+}
+
 // This warp's columns of a 128-row tile of E: lanes 32..127 split the columns in
 // halves between warps q and q + 4; lanes 0..31 (the next diagonal block's rows)
 // give warp 0 the first 32 columns and warp 4 the rest (in halves when the
@@ -732,20 +804,46 @@ __device__ __forceinline__ void e_columns(int warp, int R, bool with_warp0, int 
   }
 }
 
+// The first 128-row tile of E[r0:, r0:] into tensor memory (columns 0 .. R-1,
+// R <= 128), by warps 1..7 while warp 0 inverts the diagonal block.  after_d:
+// warp 4 first waits for warp 0 to have read the diagonal block out of lanes
+// 0..31 (the previous trailing update had one tile too; after two tiles the
+// update ended on __syncthreads).
+__device__ __forceinline__ void tc_preload_tile0(const float *A, int dp, int r0, int R,
+                                                 uint32_t tmem, bool after_d) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, quarter = warp & 3;
+  const float *E = A + (size_t)r0 + (size_t)dp * r0;
+  int cb, ce;
+  e_columns(warp, R, false, cb, ce);
+  if (warp == 4 && after_d) {
+    named_sync_n(kBarQuarter0, 64);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+  }
+  if (quarter * 32 < R)
+    e_to_tmem(E, dp, R, quarter * 32 + lane, cb, ce, tmem + ((uint32_t)(quarter * 32) << 16));
+}
+
 // E[r0:, r0:] (R x R, leading dimension dp, R <= 192) -= L U on the tensor cores,
 // 128-row tiles (rows beyond R are padding: loaded as 0, never stored).  One
-// thread issues the 12 MMAs of a tile (-L U accumulated from zero in tensor
-// memory columns 0 .. R-1) and commits them to mbar; the waiting threads spin
-// with a bound (mma_sync.hpp) and then add the product to E in FP32
-// (tmem_add_e).  Warp w moves lanes 32 (w % 4) .. (columns: e_columns).
-// Look-ahead (R <= 128, one tile): warp 0 adds the next diagonal block (rows and
-// columns r0 .. r0 + 31 of the updated matrix) into dnext (shared, row-major,
-// stride kDs) instead of storing it and returns, so that the next panel's
-// Gauss-Jordan overlaps the rest of this update and the other warps' splits of
-// the next panel; warps 1..7 meet on a named barrier at the end.  With two tiles
-// (R > 128) warp 4 would carry lanes 0..31 alone through both the work (lanes
-// 0..31 in halves, as the other quarters), warp 0 stashes the next diagonal block
-// from the first tile, and the update ends on __syncthreads.
+// thread issues the 12 MMAs of a tile, -L U accumulated from zero in tensor
+// memory, and commits them to mbar; the waiting threads spin with a bound
+// (mma_sync.hpp) and then form E + (-L U) in FP32 with round-to-nearest.  The
+// tensor cores' own accumulation rounds toward zero (their adder aligns and
+// truncates); accumulating onto E itself would shrink every entry of E by about
+// half an ulp per MMA and bias log|det| (about -8e-5 at m = 400), while on the
+// product alone that rounding is as small as the product.  Warp w moves lanes
+// 32 (w % 4) .. (columns: e_columns).
+// One tile (R <= 128): E was preloaded into columns 0 .. R-1, the product goes to
+// columns kTmemU ..; warp 0 forms the next diagonal block (rows and columns
+// r0 .. r0 + 31 of the updated matrix) into dnext (shared, row-major, stride
+// kDs) instead of storing it and returns, so that the next panel's Gauss-Jordan
+// overlaps the rest of this update and the other warps' splits and preload of the
+// next panel; warps 1..7 meet on a named barrier at the end.
+// Two tiles (R > 128): the product of each tile goes to columns 0 .. R-1 and E
+// comes from global memory (tmem_add_e); warp 4 would carry lanes 0..31 alone
+// through both tiles, so lanes 0..31 are split in halves as the other quarters,
+// warp 0 stashes the next diagonal block from the first tile, and the update ends
+// on __syncthreads.
 __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
                                    const unsigned char *Lt, const unsigned char *Ut,
                                    size_t part_L, size_t part_U, uint32_t tmem, MmaSync *mbar,
@@ -758,7 +856,45 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
   const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
   int cb, ce;
   e_columns(warp, R, true, cb, ce, two);
-  // ---- tile 0: rows 0..127
+  if (!two) {
+    const int row = quarter * 32 + lane;
+    if (tid == 0 && mma_live(mbar)) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      umma_split_tile(tmem + kTmemU, smem_u32(Lt), part_L, smem_u32(Ut), part_U, idesc, false);
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&mbar->bar)));
+    }
+    mma_wait(mbar, mphase, bad);
+    if (warp == 0) {
+#pragma unroll
+      for (int h = 0; h < kB; h += 16) {
+        uint32_t e[16], u[16];
+        tmem_ld16(tlane + (uint32_t)h, e);
+        tmem_ld16(tlane + (uint32_t)(kTmemU + h), u);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int q = 0; q < 16; q += 4)
+          *reinterpret_cast<float4 *>(dnext + lane * kDs + h + q) = make_float4(
+              __fadd_rn(__uint_as_float(e[q]), __uint_as_float(u[q])),
+              __fadd_rn(__uint_as_float(e[q + 1]), __uint_as_float(u[q + 1])),
+              __fadd_rn(__uint_as_float(e[q + 2]), __uint_as_float(u[q + 2])),
+              __fadd_rn(__uint_as_float(e[q + 3]), __uint_as_float(u[q + 3])));
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      // warp 4 may overwrite lanes 0..31 now, in the next panel's preload (there
+      // is one when R > 32)
+      if (R > kB) named_arrive_n(kBarQuarter0, 64);
+      __syncwarp();
+      return;
+    }
+    if (quarter * 32 < R) tmem_sum_to_e(E, dp, R, row, cb, ce, tlane);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    named_sync_n(kBarRest, kThreads - 32);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    return;
+  }
+  // ---- two tiles: tile 0, rows 0..127
   {
     const int row = quarter * 32 + lane;
     if (tid == 0 && mma_live(mbar)) {
@@ -777,13 +913,7 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
 #pragma unroll
       for (int h = 0; h < kB; h += 16) {
         uint32_t v[16];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-              "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-            : "r"(tlane + (uint32_t)h));
+        tmem_ld16(tlane + (uint32_t)h, v);
         asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
         for (int q = 0; q < 16; q += 4) {
@@ -796,11 +926,6 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
           *dst = d;
         }
       }
-      if (!two) {
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncwarp();
-        return;
-      }
       if (kB < ce) {  // the rest of warp 0's half
         float e0[kEc];
         e_chunk_load(E, dp, R, row, kB, e0);
@@ -808,21 +933,17 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
       }
     } else {
       float e0[kEc];
-      // (warp 4 has no columns when R = 32: E ends at column R)
       const bool mine = quarter * 32 < R && cb < ce;
       if (mine) e_chunk_load(E, dp, R, row, cb, e0);
       mma_wait(mbar, mphase, bad);
       if (mine) tmem_add_e(E, dp, R, row, cb, ce, tlane, e0);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
-    if (two)
-      __syncthreads();
-    else
-      named_sync_n(kBarRest, kThreads - 32);
+    __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
   }
   // ---- tile 1: rows 128..R-1, all eight warps
-  if (two) {
+  {
     const int row = 128 + quarter * 32 + lane;
     if (tid == 0 && mma_live(mbar)) {
       asm volatile("tcgen05.fence::after_thread_sync;");
@@ -1687,9 +1808,13 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
               named_arrive_n(kBarDt, 160);
             }
           } else {
-            // while warp 0 inverts D: the row panel B (rows k0.., columns r0..) and
-            // the rows of C, split, one column of B and one row of C per thread of
-            // warps 1..3, 5..7
+            // while warp 0 inverts D: the first tile of a single-tile trailing
+            // update into tensor memory, and the row panel B (rows k0.., columns
+            // r0..) and the rows of C, split, one column of B and one row of C per
+            // thread of warps 1..3, 5..7 (warp 4 loads all columns of lanes 0..31)
+            if (R > 0 && R <= 128)
+              tc_preload_tile0(reinterpret_cast<const float *>(A), dp, r0, R, tmem,
+                               kb > 0 && R + kB <= 128);
             if (warp != 4) {
               const int s0 = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane;
               for (int t = s0; t < R; t += kThreads - 64) {
@@ -1891,8 +2016,28 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
         for (int r = tid; r < ep.core_n; r += blockDim.x) yd[planned ? ep.core_node[r] : r] = z[r];
         __syncthreads();
         levels_backward<T>(eps, vals, zf, yd);
-        for (int r = tid; r < m; r += blockDim.x)
-          y[(size_t)i * m + r] = (double)yf[r] + (double)yd[r];
+        // one refinement step leaves an error of about (correction / solution)^2:
+        // a draw whose correction exceeds kRefineTol of its solution (an
+        // ill-conditioned (I - Gamma_i), cond * eps not small) goes to the
+        // pivoting pass, which refines until it converges
+        double dmax = 0.0, ymax = 0.0;
+        for (int r = tid; r < m; r += blockDim.x) {
+          dmax = fmax(dmax, fabs((double)yd[r]));
+          ymax = fmax(ymax, fabs((double)yf[r]));
+        }
+        block_max2(dmax, ymax, red);
+        if (!(dmax <= kRefineTol * ymax)) {
+          if (tid == 0) {
+            atomicOr(&draw_flags[i], DRAW_FLAG_PIVOT);
+            if (pivot_list) {
+              const int q = atomicAdd(pivot_list, 1);
+              if (q < n) pivot_list[1 + q] = (int)i;
+            }
+          }
+        } else {
+          for (int r = tid; r < m; r += blockDim.x)
+            y[(size_t)i * m + r] = (double)yf[r] + (double)yd[r];
+        }
       } else {
         for (int r = tid; r < m; r += blockDim.x) y[(size_t)i * m + r] = (double)yf[r];
       }
@@ -2107,11 +2252,20 @@ __global__ void __launch_bounds__(kThreads)
       } else {
         block_forward_solve<T>(A, mp, z, D);
         block_back_solve<T>(A, mp, z, D);
-        residual<T>(m, P, n, i, rows, theta, nu, z, res);
-        for (int r = tid; r < mp; r += blockDim.x) d[r] = (perm[r] < m) ? (T)res[perm[r]] : T(0);
-        __syncthreads();
-        block_forward_solve<T>(A, mp, d, D);
-        block_back_solve<T>(A, mp, d, D);
+        // the draws that reach this pass are the ill-conditioned ones: refine
+        // kFbRefine times (FP64 residual of the working-precision solution),
+        // which recovers working-precision accuracy while cond * eps < 1
+        for (int it = 0; it < kFbRefine; ++it) {
+          if (it > 0) {
+            for (int r = tid; r < m; r += blockDim.x) z[r] += d[r];
+            __syncthreads();
+          }
+          residual<T>(m, P, n, i, rows, theta, nu, z, res);
+          for (int r = tid; r < mp; r += blockDim.x) d[r] = (perm[r] < m) ? (T)res[perm[r]] : T(0);
+          __syncthreads();
+          block_forward_solve<T>(A, mp, d, D);
+          block_back_solve<T>(A, mp, d, D);
+        }
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)z[r] + (double)d[r];
       }

@@ -281,10 +281,16 @@ def test_readme_scenario_exact_fp64_vs_oracle(built_lib):
 
 def test_readme_scenario_exact_mixed_vs_oracle_on_device_draws(built_lib):
     """The same 500 steps in the mixed form; every 25th step the VB posterior and
-    the forecasts are checked against the oracle run on the device's own draws."""
+    the forecasts are checked against the oracle run on the device's own draws.
+    Forecast errors are normwise per draw (max_r |dy_r| / max_r |y_r|): a draw
+    with a tiny lambda_j has a huge nu_j, and components of y that cancel it carry
+    the FP32 normals' own rounding (1e-6 of z / sqrt(lambda)), which only a
+    normwise measure puts on the draw's scale.  Steps whose forecast draws include
+    ill-conditioned ones (the partial-pivoting pass, FP32 with three refinement
+    steps) are gated separately."""
     T, n = 500, 10000
     s, o, d, spu = readme_setup("mixed", 20261203)
-    worst = dict(ld=0.0, m=0.0, C=0.0, n=0.0, s=0.0, y=0.0, ld_pivoted=0.0)
+    worst = dict(ld=0.0, m=0.0, C=0.0, n=0.0, s=0.0, y=0.0, ld_pivoted=0.0, y_pivoted=0.0)
     for t in range(1, T):
         F = d["predictors"](t, d["y"][t])
         s.computePosterior(d["y"][t], F)
@@ -315,17 +321,23 @@ def test_readme_scenario_exact_mixed_vs_oracle_on_device_draws(built_lib):
             th = np.asfortranarray(out["thetas"].transpose(0, 2, 1))
             seed, epoch = s.getRngState()
             y, _ = oracle.forecast(spu, lam, th, Fn, seed, epoch - 1)
-            worst["y"] = max(worst["y"], float(np.max(np.abs(out["y"] - y) / (np.abs(y) + 1e-2))))
+            key = "y_pivoted" if s.getStats()["draws_pivoted"] else "y"
+            # normwise per draw: max_r |dy_ir| / max_r |y_ir|
+            err = np.max(np.abs(out["y"] - y), axis=0) / np.max(np.abs(y), axis=0)
+            worst[key] = max(worst[key], float(np.max(err)))
         else:
             s.computeForecast(n, n, Fn)
     s.close()
     record("readme_T500_mixed_vs_oracle_on_device_draws", steps=T - 1, draws=n, checked_every=25,
            logdet_max_abs_err=worst["ld"], logdet_max_abs_err_steps_with_pivoting=worst["ld_pivoted"],
            mean_sd_units=worst["m"], cov_rel=worst["C"],
-           n_rel=worst["n"], s_rel=worst["s"], forecast_max_rel_err=worst["y"])
+           n_rel=worst["n"], s_rel=worst["s"], forecast_max_rel_err=worst["y"],
+           forecast_max_rel_err_steps_with_pivoting=worst["y_pivoted"])
     assert worst["ld"] <= LOGDET_GATE_MIXED
     assert max(worst["m"], worst["C"], worst["n"], worst["s"]) <= 1e-4
     assert worst["y"] <= 1e-4
+    # ill-conditioned draws (the pivoting pass) after its three refinement steps
+    assert worst["y_pivoted"] <= 1e-3
 
 
 def test_m100_fp32_vs_fp64_T1000(built_lib):
