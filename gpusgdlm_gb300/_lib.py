@@ -25,6 +25,7 @@ STATUS = {
     7: "SGDLM_ERR_NO_DEVICE",
     8: "SGDLM_ERR_OUT_OF_MEMORY",
     9: "SGDLM_ERR_UNSUPPORTED",
+    10: "SGDLM_ERR_EVO_DISABLED",
 }
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -85,6 +86,10 @@ SIGNATURES = {
     "sgdlm_compute_prior": [_H, _i],
     "sgdlm_init_forecast_priors": [_H],
     "sgdlm_evolve_forecast_samples": [_H],
+    "sgdlm_get_evolution_matrix_configuration": [_H, _Pi],
+    "sgdlm_manage_evo_memory": [_H, _i],
+    "sgdlm_get_evolution_matrix": [_H, _Pd],
+    "sgdlm_set_evolution_matrix": [_H, _Pd],
     "sgdlm_compute_evo_prior": [_H, _Pd, _i],
     "sgdlm_evolve_forecast_samples_evo": [_H, _Pd],
     "sgdlm_compute_forecast": [_H, _Pd, _Pd, _Pd, _Pd, _i],

@@ -17,6 +17,10 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libsgdlm_gb300.so"
+# the reference's C++ engine interface (SGDLM::HostWrapper<double> and its
+# factory) on top of LIB: plain C++, no CUDA headers
+HW_SRC = CSRC / "host_wrapper.cpp"
+HW_LIB = HERE / "libsgdlm_hostwrapper.so"
 SOURCES = [
     "state_kernels.cu",
     "sample_kernels.cu",
@@ -75,7 +79,24 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
+    build_host_wrapper(verbose, force)
     return LIB
+
+
+def build_host_wrapper(verbose: bool = False, force: bool = False) -> Path:
+    """libsgdlm_hostwrapper.so: g++ on host_wrapper.cpp, linked against LIB and
+    finding it next to itself at run time."""
+    deps = [HW_SRC, LIB, HERE.parent / "include" / "sgdlm.h",
+            HERE.parent / "include" / "sgdlm_hostwrapper.hpp"]
+    if force or _stale(HW_LIB, deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", str(HW_SRC), "-o", str(HW_LIB),
+               "-L", str(HERE), "-lsgdlm_gb300", "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed on host_wrapper.cpp:\n{r.stdout}\n{r.stderr}")
+    return HW_LIB
 
 
 if __name__ == "__main__":

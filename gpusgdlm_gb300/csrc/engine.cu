@@ -71,6 +71,7 @@ struct sgdlm_engine {
   size_t no_gpus = 1;
   size_t m = 0, P = 0;
   bool mem_init = false, sim_init = false, is_prior = false;
+  bool use_evo = false;  // state evolution matrices enabled (manageEvoMemory)
   size_t nsim = 0, nsim_batch = 0;
   int precision = SGDLM_PRECISION_MIXED;
   unsigned compat = SGDLM_COMPAT_REFERENCE;
@@ -146,6 +147,14 @@ struct sgdlm_engine {
   bool check_sim_initialized() {
     if (!sim_init) {
       log(LOG_ERROR, "The simulation device memory is not initialized.");
+      return false;
+    }
+    return true;
+  }
+  // HostWrapperImpl.cu:1258-1265
+  bool check_use_evo() {
+    if (!use_evo) {
+      log(LOG_ERROR, "The use of state evolution matrices is disabled.");
       return false;
     }
     return true;
@@ -644,14 +653,25 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
   return collect_flags(h, false);
 }
 
-// Copies the evolution matrices (P x P x m, column-major per series) to the device
-// (setEvolutionMatrix, HostWrapperImpl.cu:737-754), with an FP32 copy.
-int upload_evolution_matrix(sgdlm_engine *h, const double *G) {
+// Device memory of the evolution matrices (P x P x m, FP64 and FP32), zeroed
+// (manageEvoMemory, HostWrapperImpl.cu:231-279).
+int alloc_evolution_matrix(sgdlm_engine *h) {
   const size_t n = h->P * h->P * h->m;
   if (h->G_t.count != n) {
     CK(h->G_t.alloc(n));
     CK(h->G32.alloc(n));
+    CK(cudaMemsetAsync(h->G_t.ptr, 0, n * sizeof(double), h->stream));
+    CK(cudaMemsetAsync(h->G32.ptr, 0, n * sizeof(float), h->stream));
   }
+  return SGDLM_OK;
+}
+
+// Copies the evolution matrices (P x P x m, column-major per series) to the device
+// (setEvolutionMatrix, HostWrapperImpl.cu:737-754), with an FP32 copy.
+int upload_evolution_matrix(sgdlm_engine *h, const double *G) {
+  const size_t n = h->P * h->P * h->m;
+  int st = alloc_evolution_matrix(h);
+  if (st) return st;
   CK(cudaMemcpyAsync(h->G_t.ptr, G, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   launch_to_float(h->stream, n, h->G_t.ptr, h->G32.ptr);
   h->launches += 1;
@@ -823,6 +843,7 @@ int sgdlm_init_memory(sgdlm_handle h, size_t m, size_t max_p) {
   h->m = m;
   h->P = max_p;
   int st = alloc_state(h);
+  if (!st && h->use_evo) st = alloc_evolution_matrix(h);  // HostWrapperImpl.cu:225
   if (st) {
     release_all(h);
     return st;
@@ -1031,9 +1052,55 @@ int sgdlm_compute_prior(sgdlm_handle h, int evolve_forecast_variables) {
   return SGDLM_OK;
 }
 
+int sgdlm_get_evolution_matrix_configuration(sgdlm_handle h, int *use) {
+  HCHECK(h);
+  if (!use) return SGDLM_ERR_BAD_ARG;
+  *use = h->use_evo ? 1 : 0;
+  return SGDLM_OK;
+}
+
+int sgdlm_manage_evo_memory(sgdlm_handle h, int use) {
+  HCHECK(h);
+  if (use) {
+    if (h->mem_init) {
+      int st = alloc_evolution_matrix(h);
+      if (st) return st;
+      if ((st = sync(h))) return st;
+    }
+  } else {
+    cudaStreamSynchronize(h->stream);
+    h->G_t.release();
+    h->G32.release();
+  }
+  h->use_evo = use != 0;
+  return SGDLM_OK;
+}
+
+int sgdlm_get_evolution_matrix(sgdlm_handle h, double *G_t) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_use_evo()) return SGDLM_ERR_EVO_DISABLED;
+  if (!G_t) return SGDLM_OK;  // a NULL destination copies nothing (HostWrapperImpl.cu:727)
+  int st = alloc_evolution_matrix(h);
+  if (st) return st;
+  if ((st = d2h(h, G_t, h->G_t.ptr, h->P * h->P * h->m * sizeof(double)))) return st;
+  return sync(h);
+}
+
+int sgdlm_set_evolution_matrix(sgdlm_handle h, const double *G_t) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_use_evo()) return SGDLM_ERR_EVO_DISABLED;
+  if (!G_t) return SGDLM_OK;
+  int st = upload_evolution_matrix(h, G_t);
+  if (st) return st;
+  return sync(h);
+}
+
 int sgdlm_compute_evo_prior(sgdlm_handle h, const double *G_tp1, int evolve_forecast_variables) {
   HCHECK(h);
   if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_use_evo()) return SGDLM_ERR_EVO_DISABLED;
   if (!G_tp1) return h->fail(SGDLM_ERR_BAD_ARG, "null evolution matrix");
   if (!evolve_forecast_variables && !h->check_prior(false)) return SGDLM_ERR_WRONG_STATE;
   int st = upload_evolution_matrix(h, G_tp1);
@@ -1054,6 +1121,7 @@ int sgdlm_compute_evo_prior(sgdlm_handle h, const double *G_tp1, int evolve_fore
 int sgdlm_evolve_forecast_samples_evo(sgdlm_handle h, const double *G_tp1) {
   HCHECK(h);
   if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_use_evo()) return SGDLM_ERR_EVO_DISABLED;
   if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
   if (!G_tp1) return h->fail(SGDLM_ERR_BAD_ARG, "null evolution matrix");
   int st = upload_evolution_matrix(h, G_tp1);

@@ -261,7 +261,37 @@ class SGDLM:
         if G.shape != (P, P, m):
             return self._bad_dim("Dimensions of input arguments are incompatible")
         G = np.asfortranarray(G)
+        if not self._check(self._lib.sgdlm_manage_evo_memory(self._h, 1)):  # RcppWrapper.cpp:406
+            return None
         self._check(self._lib.sgdlm_compute_evo_prior(self._h, _pd(G), 0))
+        return None
+
+    def getEvolutionMatrixConfiguration(self) -> bool:
+        """HostWrapper.hpp:19: whether evolution matrices are enabled."""
+        v = C.c_int()
+        self._lib.sgdlm_get_evolution_matrix_configuration(self._h, C.byref(v))
+        return bool(v.value)
+
+    def manageEvoMemory(self, use_state_evolution_matrix: bool):
+        """HostWrapper.hpp:31: enable or disable the evolution matrices."""
+        self._check(self._lib.sgdlm_manage_evo_memory(self._h, 1 if use_state_evolution_matrix else 0))
+
+    def getEvolutionMatrix(self):
+        """HostWrapper.hpp:57: the current evolution matrices (max_p x max_p x m)."""
+        m, P = self.m, self.max_p
+        G = np.zeros((P, P, m), order="F")
+        if not self._check(self._lib.sgdlm_get_evolution_matrix(self._h, _pd(G))):
+            return None
+        return G
+
+    def setEvolutionMatrix(self, G_t):
+        """HostWrapper.hpp:59: sets the evolution matrices (max_p x max_p x m)."""
+        m, P = self.m, self.max_p
+        G = np.asarray(G_t, dtype=np.float64)
+        if G.shape != (P, P, m):
+            return self._bad_dim("Dimensions of input arguments are incompatible")
+        G = np.asfortranarray(G)
+        self._check(self._lib.sgdlm_set_evolution_matrix(self._h, _pd(G)))
         return None
 
     def computeEvoForecast(self, nsim: int, nsim_batch: int, F_tp1, G_tp1):
@@ -303,6 +333,8 @@ class SGDLM:
         y = np.zeros((m, n, K), order="F")
         lam = np.zeros((m, n, K), order="F") if debug else None
         th = np.zeros((P, m, n, K), order="F") if debug else None
+        if G4 is not None and not self._check(self._lib.sgdlm_manage_evo_memory(self._h, 1)):
+            return None  # RcppWrapper.cpp:649
         if not self._check(self._lib.sgdlm_init_forecast_priors(self._h)):
             return None
         for k in range(K):

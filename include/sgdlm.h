@@ -39,7 +39,8 @@ typedef enum {
   SGDLM_ERR_BAD_ARG = 6,        /* null pointer, nsim = 0, invalid parental set */
   SGDLM_ERR_NO_DEVICE = 7,      /* no CUDA device (HostWrapperImpl.cu:22-25) */
   SGDLM_ERR_OUT_OF_MEMORY = 8,
-  SGDLM_ERR_UNSUPPORTED = 9     /* size beyond this build's limits (max_p > 64, m > 800) */
+  SGDLM_ERR_UNSUPPORTED = 9,    /* size beyond this build's limits (max_p > 64, m > 800) */
+  SGDLM_ERR_EVO_DISABLED = 10   /* evolution matrices not enabled (HostWrapperImpl.cu:1258-1265) */
 } sgdlm_status;
 
 typedef enum {
@@ -114,6 +115,18 @@ int sgdlm_evolve_forecast_samples(sgdlm_handle h);                              
  * max_p x max_p x m, column-major per series (R's array(…, c(max_p, max_p, m))).
  * evolveForecastSamples(const DOUBLE *G) (HostWrapperImpl.cu:904-946) -- the
  * evolution of forecast draws with theta = G theta before adding chol(W)' omega. */
+/* getEvolutionMatrixConfiguration (HostWrapper.hpp:19, HostWrapperImpl.cu:122-127):
+ * whether evolution matrices are enabled. */
+int sgdlm_get_evolution_matrix_configuration(sgdlm_handle h, int *use);
+/* manageEvoMemory (HostWrapper.hpp:31, HostWrapperImpl.cu:231-279): enable (device
+ * memory for G, zeroed) or disable (memory released) the evolution matrices; the
+ * setting survives sgdlm_init_memory.  The four G functions below return
+ * SGDLM_ERR_EVO_DISABLED unless enabled, as the reference logs and returns. */
+int sgdlm_manage_evo_memory(sgdlm_handle h, int use);
+/* getEvolutionMatrix / setEvolutionMatrix (HostWrapper.hpp:57-59,
+ * HostWrapperImpl.cu:717-755): G_t is max_p x max_p x m; NULL copies nothing. */
+int sgdlm_get_evolution_matrix(sgdlm_handle h, double *G_t);
+int sgdlm_set_evolution_matrix(sgdlm_handle h, const double *G_t);
 int sgdlm_compute_evo_prior(sgdlm_handle h, const double *G_tp1, int evolve_forecast_variables);
 int sgdlm_evolve_forecast_samples_evo(sgdlm_handle h, const double *G_tp1);
 /* y_tp1 (m x nsim, draw-major) in page-locked, device-mapped host memory (e.g.
