@@ -56,6 +56,42 @@ class Stats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ProposalConfig(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int),
+        ("train_steps", C.c_int),
+        ("iters_per_step", C.c_int),
+        ("batch", C.c_int),
+        ("lr", C.c_double),
+        ("ess_fraction", C.c_double),
+        ("seed", C.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ProposalInfo(C.Structure):
+    _fields_ = [
+        ("training_calls", C.c_uint64),
+        ("samples", C.c_uint64),
+        ("adam_steps", C.c_uint64),
+        ("learned_calls", C.c_uint64),
+        ("fallbacks", C.c_uint64),
+        ("last_loss", C.c_double),
+        ("ess_learned", C.c_double),
+        ("ess_plain", C.c_double),
+        ("deployed", C.c_int),
+        ("used_learned", C.c_int),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+PROPOSAL_PLAIN = 0
+PROPOSAL_LEARNED = 1
+
 _H = C.c_void_p
 _sz, _i, _u, _u64, _d = C.c_size_t, C.c_int, C.c_uint, C.c_uint64, C.c_double
 _Pd, _Pu, _Psz, _Pi, _Pu64 = (C.POINTER(C.c_double), C.POINTER(C.c_uint), C.POINTER(C.c_size_t),
@@ -106,6 +142,15 @@ SIGNATURES = {
     "sgdlm_set_log_level": [_H, _i],
     "sgdlm_get_log_level": [_H, _Pi],
     "sgdlm_last_error": [_H],
+    "sgdlm_set_proposal": [_H, C.POINTER(ProposalConfig)],
+    "sgdlm_get_proposal": [_H, C.POINTER(ProposalConfig)],
+    "sgdlm_get_proposal_info": [_H, C.POINTER(ProposalInfo)],
+    "sgdlm_proposal_sizes": [_H, _Psz, _Pi, _Pi],
+    "sgdlm_proposal_get_params": [_H, C.c_void_p],
+    "sgdlm_proposal_set_params": [_H, C.c_void_p],
+    "sgdlm_proposal_loss_and_gradient": [_H, _sz, C.c_void_p, C.c_void_p, C.c_void_p, _Pd,
+                                         C.c_void_p],
+    "sgdlm_get_proposal_state": [_H, _Pd, _Pd, _Pd, _Pd, _Pd],
     "sgdlm_filter_step_device": [_H, C.c_void_p, C.c_void_p, C.c_void_p, _d, C.c_void_p,
                                  C.c_void_p, C.c_void_p],
     "sgdlm_get_stream": [_H, C.POINTER(C.c_void_p)],

@@ -29,6 +29,8 @@ SOURCES = [
     "engine.cu",
     "elimination.cu",
     "noalloc.cu",
+    "mlp_kernels.cu",
+    "proposal_kernels.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]

@@ -23,9 +23,14 @@
 #include <type_traits>
 #include <vector>
 
+#include <cmath>
+
+#include <cuda_bf16.h>
+
 #include "../../include/sgdlm.h"
 #include "elimination.hpp"
 #include "kernels.hpp"
+#include "proposal.hpp"
 
 using namespace sgdlm;
 
@@ -61,6 +66,38 @@ template <typename T> struct DevBuf {
 };
 
 constexpr size_t kMaxP = 64;
+
+// The learned importance proposal's configuration, network, replay buffer and
+// per-call buffers (proposal.hpp).
+struct ProposalState {
+  sgdlm_proposal_config cfg{SGDLM_PROPOSAL_PLAIN, 500, 4, 4096, 1e-3, 0.5, 20261204u};
+  size_t m = 0, P = 0;  // dimensions the buffers were made for
+  MlpLayout L{};
+  long cap = 0, count = 0, pos = 0;
+  sgdlm_proposal_info info{};
+  DevBuf<float> w, grad, m1, m2;
+  DevBuf<__nv_bfloat16> w16;
+  DevBuf<float> X, Y, M;                 // m rows: features (normalised in X), targets, mask
+  DevBuf<float> bX, bY, bM;              // replay ring, cap rows
+  DevBuf<float> Xb, Yb, Mb;              // training batch
+  DevBuf<float> Z1, A1, Z2, A2, Out, dOut, dA, dA2;  // activations, max(batch, m) rows
+  DevBuf<double> fsum, loss;
+  DevBuf<double> mq, nq, sq, Uq64, cst, lr, logw;
+  DevBuf<float> Uq32;
+  MlpActs acts() {
+    return MlpActs{Z1.ptr, A1.ptr, Z2.ptr, A2.ptr, Out.ptr, dOut.ptr, dA.ptr, dA2.ptr};
+  }
+  void release() {
+    for (auto *b : {&w, &grad, &m1, &m2, &X, &Y, &M, &bX, &bY, &bM, &Xb, &Yb, &Mb, &Z1, &A1, &Z2,
+                    &A2, &Out, &dOut, &dA, &dA2, &Uq32})
+      b->release();
+    for (auto *b : {&fsum, &loss, &mq, &nq, &sq, &Uq64, &cst, &lr, &logw}) b->release();
+    w16.release();
+    m = P = 0;
+    cap = count = pos = 0;
+    info = sgdlm_proposal_info{};
+  }
+};
 
 }  // namespace
 
@@ -110,6 +147,7 @@ struct sgdlm_engine {
   DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
   DevBuf<uint32_t> dev_epoch;
   LuPlan plan{};
+  ProposalState prop;
   int chunks = 0;          // VB draw chunks and draws per chunk (vb_chunking)
   long chunk_draws = 0;
   cudaEvent_t ev[8] = {};
@@ -532,6 +570,155 @@ template <typename T> void vb_moments(sgdlm_engine *h, double *w) {
   h->launches += 4;
 }
 
+// ---- learned importance proposal ------------------------------------------------
+
+// splitmix64 (Steele, Lea & Flood 2014) and Box-Muller normals for the initial
+// weights: the same values on every host.
+uint64_t splitmix64(uint64_t &x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+double host_normal(uint64_t &st) {
+  const double u1 = ((splitmix64(st) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  const double u2 = ((splitmix64(st) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+}
+
+// Buffers and fresh weights for the current (m, max_p): W1 ~ N(0, 1/F),
+// W2 ~ N(0, 1/H), W3 = 0 and zero biases, so that an untrained network leaves
+// the naive posterior unchanged.
+int proposal_ensure(sgdlm_engine *h) {
+  ProposalState &q = h->prop;
+  if (q.w.ptr && q.m == h->m && q.P == h->P) return SGDLM_OK;
+  if (h->P > (size_t)kProposalMaxP)
+    return h->fail(SGDLM_ERR_UNSUPPORTED, "the learned proposal serves max_p <= 24");
+  cudaStreamSynchronize(h->stream);
+  const sgdlm_proposal_config cfg = q.cfg;
+  q.release();
+  const int m = (int)h->m, P = (int)h->P, F = proposal_features(P), O = proposal_outputs(P);
+  q.L = mlp_layout(F, O);
+  const long H = q.L.H;
+  q.cap = (long)std::max(1, cfg.train_steps) * m;
+  const long rows = std::max<long>(cfg.batch, m);
+  CK(q.w.alloc(q.L.total));
+  CK(q.grad.alloc(q.L.total));
+  CK(q.m1.alloc(q.L.total));
+  CK(q.m2.alloc(q.L.total));
+  CK(q.w16.alloc(q.L.total));
+  CK(q.X.alloc((size_t)m * F));
+  CK(q.Y.alloc((size_t)m * O));
+  CK(q.M.alloc((size_t)m * O));
+  CK(q.bX.alloc((size_t)q.cap * F));
+  CK(q.bY.alloc((size_t)q.cap * O));
+  CK(q.bM.alloc((size_t)q.cap * O));
+  CK(q.Xb.alloc((size_t)cfg.batch * F));
+  CK(q.Yb.alloc((size_t)cfg.batch * O));
+  CK(q.Mb.alloc((size_t)cfg.batch * O));
+  for (auto *b : {&q.Z1, &q.A1, &q.Z2, &q.A2, &q.dA, &q.dA2}) CK(b->alloc((size_t)rows * H));
+  CK(q.Out.alloc((size_t)rows * O));
+  CK(q.dOut.alloc((size_t)rows * O));
+  CK(q.fsum.alloc(2 * (size_t)F + 1));
+  CK(q.loss.alloc(1));
+  CK(q.mq.alloc((size_t)m * P));
+  CK(q.nq.alloc(m));
+  CK(q.sq.alloc(m));
+  CK(q.cst.alloc(m));
+  CK(q.Uq64.alloc((size_t)m * P * P));
+  CK(q.Uq32.alloc((size_t)m * P * P));
+  std::vector<float> w(q.L.total, 0.f);
+  uint64_t st = cfg.seed;
+  const double s1 = 1.0 / std::sqrt((double)F), s2 = 1.0 / std::sqrt((double)H);
+  for (long e = 0; e < H * F; ++e) w[q.L.w1 + e] = (float)(s1 * host_normal(st));
+  for (long e = 0; e < H * H; ++e) w[q.L.w2 + e] = (float)(s2 * host_normal(st));
+  CK(cudaMemcpyAsync(q.w.ptr, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+  mlp_refresh_bf16(h->stream, q.L, q.w.ptr, q.w16.ptr);
+  h->launches += 1;
+  q.cfg = cfg;
+  q.m = h->m;
+  q.P = h->P;
+  q.info.deployed = cfg.train_steps <= 0 ? 1 : 0;
+  return sync(h);
+}
+
+// The pairs of this call (naive posterior in m_t.., VB refit in mean_..) into
+// the replay buffer, then iters_per_step Adam iterations on random batches.
+int proposal_train(sgdlm_engine *h) {
+  ProposalState &q = h->prop;
+  cudaStream_t s = h->stream;
+  const int m = (int)h->m, P = (int)h->P, F = q.L.F, O = q.L.O;
+  launch_proposal_features(s, m, P, h->p.ptr, h->sp.ptr, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr,
+                           h->s_t.ptr, q.X.ptr);
+  launch_proposal_targets(s, m, P, h->p.ptr, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr,
+                          h->mean_m.ptr, h->mean_C.ptr, h->mean_n.ptr, h->mean_s.ptr, q.Y.ptr,
+                          q.M.ptr);
+  launch_replay_append(s, m, F, O, q.pos, q.cap, q.X.ptr, q.Y.ptr, q.M.ptr, q.bX.ptr, q.bY.ptr,
+                       q.bM.ptr, q.fsum.ptr);
+  h->launches += 3;
+  q.pos = (q.pos + m) % q.cap;
+  q.count = std::min(q.count + m, q.cap);
+  const int B = q.cfg.batch;
+  for (int it = 0; it < q.cfg.iters_per_step; ++it) {
+    const uint64_t step = ++q.info.adam_steps;
+    launch_replay_gather(s, B, F, O, q.count, q.cfg.seed, step, q.bX.ptr, q.bY.ptr, q.bM.ptr,
+                         q.fsum.ptr, q.Xb.ptr, q.Yb.ptr, q.Mb.ptr);
+    mlp_forward(s, q.L, B, q.Xb.ptr, q.w.ptr, q.w16.ptr, q.acts());
+    mlp_loss_backward(s, q.L, B, q.Xb.ptr, q.Yb.ptr, q.Mb.ptr, q.w16.ptr, q.acts(), q.grad.ptr,
+                      q.loss.ptr);
+    mlp_adam(s, q.L, q.w.ptr, q.w16.ptr, q.grad.ptr, q.m1.ptr, q.m2.ptr, (float)q.cfg.lr,
+             (long)step);
+    h->launches += 16;
+  }
+  q.info.training_calls += 1;
+  q.info.samples = (uint64_t)q.count;
+  if ((long)q.info.training_calls >= q.cfg.train_steps) q.info.deployed = 1;
+  double loss = NAN;
+  int st = d2h(h, &loss, q.loss.ptr, sizeof(double));
+  if (st) return st;
+  if ((st = sync(h))) return st;
+  q.info.last_loss = loss;
+  return SGDLM_OK;
+}
+
+// Draws from the learned proposal and their exact log weights (in q.logw), then
+// the normalised weights.  Precondition: the proposal's buffers exist.
+template <typename T>
+int learned_draws(sgdlm_engine *h, RngKey key) {
+  ProposalState &q = h->prop;
+  cudaStream_t s = h->stream;
+  const int m = (int)h->m, P = (int)h->P, F = q.L.F;
+  const long n = (long)h->nsim;
+  if (q.lr.count != (size_t)m * n) {
+    CK(q.lr.alloc((size_t)m * n));
+    CK(q.logw.alloc(n));
+  }
+  launch_cholesky(s, m, P, h->p.ptr, h->C_t.ptr, h->U64.ptr, h->U32.ptr);
+  launch_proposal_features(s, m, P, h->p.ptr, h->sp.ptr, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr,
+                           h->s_t.ptr, q.X.ptr);
+  launch_normalise(s, m, F, q.fsum.ptr, q.X.ptr);
+  mlp_forward(s, q.L, m, q.X.ptr, q.w.ptr, q.w16.ptr, q.acts());
+  T *Uq = std::is_same<T, float>::value ? reinterpret_cast<T *>(q.Uq32.ptr)
+                                        : reinterpret_cast<T *>(q.Uq64.ptr);
+  launch_proposal_params<T>(s, m, P, h->p.ptr, q.Out.ptr, h->m_t.ptr, h->n_t.ptr, h->s_t.ptr,
+                            h->U64.ptr, q.mq.ptr, q.nq.ptr, q.sq.ptr, q.Uq64.ptr, Uq, q.cst.ptr);
+  launch_sample<T>(s, m, P, n, q.mq.ptr, q.nq.ptr, q.sq.ptr, Uq, key, as<T>(h->lambda),
+                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr);
+  h->launches += 8;
+  CK(cudaEventRecord(h->ev[1], s));
+  int st = lu_draws<T>(h, nullptr, key, nullptr);
+  if (st) return st;
+  CK(cudaEventRecord(h->ev[2], s));
+  const T *U = std::is_same<T, float>::value ? reinterpret_cast<const T *>(h->U32.ptr)
+                                              : reinterpret_cast<const T *>(h->U64.ptr);
+  launch_log_ratio<T>(s, m, P, n, h->p.ptr, as<T>(h->theta), as<T>(h->lambda), h->m_t.ptr,
+                      h->n_t.ptr, h->s_t.ptr, U, q.mq.ptr, q.nq.ptr, q.sq.ptr, Uq, q.cst.ptr,
+                      h->logdet.ptr, q.lr.ptr, q.logw.ptr);
+  launch_weights(s, n, q.logw.ptr, h->w.ptr, h->stats6.ptr, h->wpart.ptr);
+  h->launches += 5;
+  return SGDLM_OK;
+}
+
 // Reads back the per-draw and per-series status words into the stats block.
 int collect_flags(sgdlm_engine *h, bool with_series) {
   std::vector<int> f(h->nsim);
@@ -566,17 +753,46 @@ int vb_posterior(sgdlm_engine *h, double *o_m, double *o_C, double *o_n, double 
   const size_t m = h->m, P = h->P, n = h->nsim;
   cudaStream_t s = h->stream;
   int st;
+  ProposalState &q = h->prop;
+  const bool use_learned = q.cfg.mode == SGDLM_PROPOSAL_LEARNED;
+  if (use_learned && (st = proposal_ensure(h))) return st;
+  const bool learned = use_learned && q.info.deployed;
   const RngKey key = h->key((uint32_t)h->epoch);
   h->epoch += 1;
+  q.info.ess_learned = q.info.ess_plain = 0.0;
+  q.info.used_learned = 0;
   CK(cudaEventRecord(h->ev[0], s));
   CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
-  sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, key);
-  CK(cudaEventRecord(h->ev[1], s));
-  if ((st = lu_draws<T>(h, nullptr, key, nullptr))) return st;
-  CK(cudaEventRecord(h->ev[2], s));
-  launch_weights(s, (long)n, h->logdet.ptr, h->w.ptr, h->stats6.ptr, h->wpart.ptr);
-  h->launches += 3;
-  CK(cudaEventRecord(h->ev[3], s));
+  bool plain = !learned;
+  if (learned) {
+    if ((st = learned_draws<T>(h, key))) return st;
+    CK(cudaEventRecord(h->ev[3], s));
+    double st6[6];
+    if ((st = d2h(h, st6, h->stats6.ptr, 6 * sizeof(double)))) return st;
+    if ((st = sync(h))) return st;
+    q.info.learned_calls += 1;
+    q.info.ess_learned = st6[1];
+    if (!(st6[1] >= q.cfg.ess_fraction * (double)n)) {
+      // fallback: the plain proposal on an independent stream (the key's high
+      // word flipped), as the caller would run it
+      q.info.fallbacks += 1;
+      plain = true;
+      CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
+    } else {
+      q.info.used_learned = 1;
+    }
+  }
+  if (plain) {
+    RngKey kp = key;
+    if (learned) kp.k1 ^= 0x80000000u;
+    sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, kp);
+    CK(cudaEventRecord(h->ev[1], s));
+    if ((st = lu_draws<T>(h, nullptr, kp, nullptr))) return st;
+    CK(cudaEventRecord(h->ev[2], s));
+    launch_weights(s, (long)n, h->logdet.ptr, h->w.ptr, h->stats6.ptr, h->wpart.ptr);
+    h->launches += 3;
+    CK(cudaEventRecord(h->ev[3], s));
+  }
   vb_moments<T>(h, h->w.ptr);
   CK(cudaEventRecord(h->ev[4], s));
   if (o_m && (st = d2h(h, o_m, h->mean_m.ptr, P * m * sizeof(double)))) return st;
@@ -591,12 +807,16 @@ int vb_posterior(sgdlm_engine *h, double *o_m, double *o_C, double *o_n, double 
   h->stats.sum_det_weights = st6[0];
   h->stats.ess = st6[1];
   h->stats.max_log_det = st6[2];
+  if (plain) q.info.ess_plain = st6[1];
   h->stats.ms_sample = elapsed(h->ev[0], h->ev[1]);
   h->stats.ms_lu = elapsed(h->ev[1], h->ev[2]);
   h->stats.ms_weights = elapsed(h->ev[2], h->ev[3]);
   h->stats.ms_vb = elapsed(h->ev[3], h->ev[4]);
   h->stats.ms_total = elapsed(h->ev[0], h->ev[4]);
-  return collect_flags(h, true);
+  if ((st = collect_flags(h, true))) return st;
+  // training pairs: calls before deployment whose ESS passes the README's gate
+  if (use_learned && !q.info.deployed && st6[1] > 0.5 * (double)n) return proposal_train(h);
+  return SGDLM_OK;
 }
 
 template <typename T>
@@ -1267,6 +1487,128 @@ int sgdlm_get_log_level(sgdlm_handle h, int *level) {
   return SGDLM_OK;
 }
 const char *sgdlm_last_error(sgdlm_handle h) { return h ? h->last_error.c_str() : ""; }
+
+int sgdlm_set_proposal(sgdlm_handle h, const sgdlm_proposal_config *cfg) {
+  HCHECK(h);
+  sgdlm_proposal_config c{SGDLM_PROPOSAL_PLAIN, 500, 4, 4096, 1e-3, 0.5, 20261204u};
+  if (cfg) c = *cfg;
+  if ((c.mode != SGDLM_PROPOSAL_PLAIN && c.mode != SGDLM_PROPOSAL_LEARNED) || c.train_steps < 0 ||
+      c.iters_per_step < 0 || c.batch < 1 || !(c.lr > 0.0) ||
+      !(c.ess_fraction >= 0.0 && c.ess_fraction <= 1.0))
+    return h->fail(SGDLM_ERR_BAD_ARG, "invalid proposal configuration");
+  cudaStreamSynchronize(h->stream);
+  h->prop.release();
+  h->prop.cfg = c;
+  if (c.mode == SGDLM_PROPOSAL_LEARNED && h->mem_init) return proposal_ensure(h);
+  return SGDLM_OK;
+}
+
+int sgdlm_get_proposal(sgdlm_handle h, sgdlm_proposal_config *cfg) {
+  HCHECK(h);
+  if (!cfg) return SGDLM_ERR_BAD_ARG;
+  *cfg = h->prop.cfg;
+  return SGDLM_OK;
+}
+
+int sgdlm_get_proposal_info(sgdlm_handle h, sgdlm_proposal_info *info) {
+  HCHECK(h);
+  if (!info) return SGDLM_ERR_BAD_ARG;
+  *info = h->prop.info;
+  return SGDLM_OK;
+}
+
+int sgdlm_proposal_sizes(sgdlm_handle h, size_t *n_params, int *n_features, int *n_outputs) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  const int F = proposal_features((int)h->P), O = proposal_outputs((int)h->P);
+  if (n_params) *n_params = (size_t)mlp_layout(F, O).total;
+  if (n_features) *n_features = F;
+  if (n_outputs) *n_outputs = O;
+  return SGDLM_OK;
+}
+
+int sgdlm_proposal_get_params(sgdlm_handle h, float *params) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!params) return h->fail(SGDLM_ERR_BAD_ARG, "null parameter array");
+  int st = proposal_ensure(h);
+  if (st) return st;
+  if ((st = d2h(h, params, h->prop.w.ptr, h->prop.L.total * sizeof(float)))) return st;
+  return sync(h);
+}
+
+int sgdlm_proposal_set_params(sgdlm_handle h, const float *params) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!params) return h->fail(SGDLM_ERR_BAD_ARG, "null parameter array");
+  int st = proposal_ensure(h);
+  if (st) return st;
+  ProposalState &q = h->prop;
+  if ((st = h2d(h, q.w.ptr, params, q.L.total * sizeof(float)))) return st;
+  mlp_refresh_bf16(h->stream, q.L, q.w.ptr, q.w16.ptr);
+  h->launches += 1;
+  return sync(h);
+}
+
+int sgdlm_proposal_loss_and_gradient(sgdlm_handle h, size_t batch, const float *X, const float *Y,
+                                     const float *mask, double *loss, float *grad) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!X || !Y || !mask || batch < 1 || batch > (1u << 24))
+    return h->fail(SGDLM_ERR_BAD_ARG, "invalid batch");
+  int st = proposal_ensure(h);
+  if (st) return st;
+  ProposalState &q = h->prop;
+  const MlpLayout &L = q.L;
+  const size_t B = batch;
+  DevBuf<float> x, y, mk, g, z1, a1, z2, a2, out, dout, da, da2;
+  DevBuf<double> l;
+  CK(x.alloc(B * L.F));
+  CK(y.alloc(B * L.O));
+  CK(mk.alloc(B * L.O));
+  CK(g.alloc(L.total));
+  for (auto *b : {&z1, &a1, &z2, &a2, &da, &da2}) CK(b->alloc(B * L.H));
+  CK(out.alloc(B * L.O));
+  CK(dout.alloc(B * L.O));
+  CK(l.alloc(1));
+  if ((st = h2d(h, x.ptr, X, B * L.F * sizeof(float)))) return st;
+  if ((st = h2d(h, y.ptr, Y, B * L.O * sizeof(float)))) return st;
+  if ((st = h2d(h, mk.ptr, mask, B * L.O * sizeof(float)))) return st;
+  const MlpActs a{z1.ptr, a1.ptr, z2.ptr, a2.ptr, out.ptr, dout.ptr, da.ptr, da2.ptr};
+  mlp_forward(h->stream, L, (int)B, x.ptr, q.w.ptr, q.w16.ptr, a);
+  mlp_loss_backward(h->stream, L, (int)B, x.ptr, y.ptr, mk.ptr, q.w16.ptr, a, g.ptr, l.ptr);
+  h->launches += 13;
+  if (loss && (st = d2h(h, loss, l.ptr, sizeof(double)))) return st;
+  if (grad && (st = d2h(h, grad, g.ptr, L.total * sizeof(float)))) return st;
+  return sync(h);
+}
+
+int sgdlm_get_proposal_state(sgdlm_handle h, double *m_q, double *C_q, double *n_q, double *s_q,
+                             double *log_weights) {
+  HCHECK(h);
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  ProposalState &q = h->prop;
+  if (!q.mq.ptr || !q.logw.ptr)
+    return h->fail(SGDLM_ERR_WRONG_STATE, "no learned proposal has been drawn from");
+  const size_t m = h->m, P = h->P;
+  int st;
+  std::vector<double> U(P * P * m);
+  if (m_q && (st = d2h(h, m_q, q.mq.ptr, P * m * sizeof(double)))) return st;
+  if (n_q && (st = d2h(h, n_q, q.nq.ptr, m * sizeof(double)))) return st;
+  if (s_q && (st = d2h(h, s_q, q.sq.ptr, m * sizeof(double)))) return st;
+  if (C_q && (st = d2h(h, U.data(), q.Uq64.ptr, U.size() * sizeof(double)))) return st;
+  if (log_weights && (st = d2h(h, log_weights, q.logw.ptr, h->nsim * sizeof(double)))) return st;
+  if ((st = sync(h))) return st;
+  if (C_q)  // C~ = U~' U~ per series
+    for (size_t j = 0; j < m; ++j)
+      for (size_t c = 0; c < P; ++c)
+        for (size_t r = 0; r < P; ++r) {
+          double acc = 0.0;
+          for (size_t l = 0; l < P; ++l) acc += U[j * P * P + l + P * r] * U[j * P * P + l + P * c];
+          C_q[j * P * P + r + P * c] = acc;
+        }
+  return SGDLM_OK;
+}
 
 int sgdlm_filter_step_device(sgdlm_handle h, const double *d_y, const double *d_F,
                              const double *d_x, double ess_threshold, double *d_forecast,

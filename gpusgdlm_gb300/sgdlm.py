@@ -427,6 +427,71 @@ class SGDLM:
             return None
         return {"lambdas": lam, "thetas": th, "log_dets": ld}
 
+    # ------------------------------------------------ learned importance proposal
+    def setProposal(self, mode: str = "plain", train_steps: int = 500, iters_per_step: int = 4,
+                    batch: int = 4096, lr: float = 1e-3, ess_fraction: float = 0.5,
+                    seed: int = 20261204):
+        """The importance proposal of computeVBPosterior: "plain" (the reference's
+        decoupled naive posterior) or "learned" (include/sgdlm.h)."""
+        cfg = L.ProposalConfig(L.PROPOSAL_LEARNED if mode == "learned" else L.PROPOSAL_PLAIN,
+                               int(train_steps), int(iters_per_step), int(batch), float(lr),
+                               float(ess_fraction), int(seed))
+        self._check(self._lib.sgdlm_set_proposal(self._h, C.byref(cfg)))
+
+    def getProposal(self) -> dict:
+        cfg = L.ProposalConfig()
+        self._lib.sgdlm_get_proposal(self._h, C.byref(cfg))
+        d = cfg.as_dict()
+        d["mode"] = "learned" if d["mode"] == L.PROPOSAL_LEARNED else "plain"
+        return d
+
+    def getProposalInfo(self) -> dict:
+        info = L.ProposalInfo()
+        self._lib.sgdlm_get_proposal_info(self._h, C.byref(info))
+        return info.as_dict()
+
+    def proposalSizes(self):
+        n, f, o = C.c_size_t(), C.c_int(), C.c_int()
+        if not self._check(self._lib.sgdlm_proposal_sizes(self._h, C.byref(n), C.byref(f), C.byref(o))):
+            return None
+        return int(n.value), int(f.value), int(o.value)
+
+    def getProposalParams(self) -> np.ndarray:
+        n, _, _ = self.proposalSizes()
+        w = np.zeros(n, dtype=np.float32)
+        if not self._check(self._lib.sgdlm_proposal_get_params(self._h, w.ctypes.data)):
+            return None
+        return w
+
+    def setProposalParams(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._check(self._lib.sgdlm_proposal_set_params(self._h, w.ctypes.data))
+
+    def proposalLossAndGradient(self, X, Y, mask):
+        """Masked MSE and its gradient (flat parameter layout) on a batch of
+        normalised features X (B x F), targets Y and mask (B x O)."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        M = np.ascontiguousarray(mask, dtype=np.float32)
+        n, _, _ = self.proposalSizes()
+        g = np.zeros(n, dtype=np.float32)
+        loss = C.c_double()
+        if not self._check(self._lib.sgdlm_proposal_loss_and_gradient(
+                self._h, X.shape[0], X.ctypes.data, Y.ctypes.data, M.ctypes.data, C.byref(loss),
+                g.ctypes.data)):
+            return None
+        return float(loss.value), g
+
+    def getProposalState(self):
+        """The last learned call's proposal (m, C, n, s) and the draws' log weights."""
+        m, P, n = self.m, self.max_p, self.nsim
+        mq = np.zeros((P, m), order="F"); Cq = np.zeros((P, P, m), order="F")
+        nq = np.zeros(m); sq = np.zeros(m); lw = np.zeros(n)
+        if not self._check(self._lib.sgdlm_get_proposal_state(self._h, _pd(mq), _pd(Cq), _pd(nq),
+                                                              _pd(sq), _pd(lw))):
+            return None
+        return {"m": mq, "C": Cq, "n": nq, "s": sq, "log_weights": lw}
+
     def launchCount(self) -> int:
         v = C.c_uint64()
         self._lib.sgdlm_get_launch_count(self._h, C.byref(v))

@@ -164,6 +164,62 @@ int sgdlm_get_log_level(sgdlm_handle h, int *level);  /* RcppWrapper.cpp:827-832
 /* Last error message of this handle (empty string if none). */
 const char *sgdlm_last_error(sgdlm_handle h);
 
+/* ---- learned importance proposal (no counterpart in the reference) ----
+ * The reference samples the VB importance draws from the decoupled naive
+ * posterior (SGDLM.cu:623-677).  With SGDLM_PROPOSAL_LEARNED a per-series network
+ * (features of the naive posterior and of the series' simultaneous parents ->
+ * 128 -> GELU -> 128 -> GELU -> location shift and log-scales of theta_j and
+ * log-corrections of (n_j, s_j); BF16 weights, FP32 accumulation) is trained
+ * online by Adam on (naive posterior -> VB-refitted posterior) pairs of the
+ * first train_steps computeVBPosterior calls whose ESS exceeds nsim/2, then
+ * deployed: later calls draw from the corrected normal-gamma proposal, with
+ * importance weights that stay exact density ratios
+ * (log w = log|det(I - Gamma)| + sum_j [log p_j - log q_j]), and fall back to the
+ * plain proposal when the learned weights' ESS is below ess_fraction * nsim.
+ * computeVBPosterior only (the fused device step keeps the plain proposal);
+ * max_p <= 24. */
+enum { SGDLM_PROPOSAL_PLAIN = 0, SGDLM_PROPOSAL_LEARNED = 1 };
+typedef struct {
+  int mode;             /* SGDLM_PROPOSAL_PLAIN or SGDLM_PROPOSAL_LEARNED */
+  int train_steps;      /* training calls before deployment (500) */
+  int iters_per_step;   /* Adam iterations after each training call (4) */
+  int batch;            /* samples per Adam iteration (4096) */
+  double lr;            /* Adam step size (1e-3) */
+  double ess_fraction;  /* fall back to the plain proposal below this ESS / nsim (0.5) */
+  uint64_t seed;        /* initial weights and training batches */
+} sgdlm_proposal_config;
+typedef struct {
+  uint64_t training_calls;  /* calls whose pairs trained the network */
+  uint64_t samples;         /* (series, call) pairs in the replay buffer */
+  uint64_t adam_steps;
+  uint64_t learned_calls;   /* calls that drew from the learned proposal */
+  uint64_t fallbacks;       /* of those, calls redone with the plain proposal */
+  double last_loss;         /* masked MSE of the last Adam iteration */
+  double ess_learned;       /* last call: ESS of the learned proposal's weights (0: not run) */
+  double ess_plain;         /* last call: ESS of the plain proposal's weights (0: not run) */
+  int deployed;             /* training finished, the learned proposal is in use */
+  int used_learned;         /* the last call's moments came from the learned proposal */
+} sgdlm_proposal_info;
+/* Configures the proposal (a NULL cfg restores the plain defaults); a new
+ * configuration restarts training from freshly initialised weights. */
+int sgdlm_set_proposal(sgdlm_handle h, const sgdlm_proposal_config *cfg);
+int sgdlm_get_proposal(sgdlm_handle h, sgdlm_proposal_config *cfg);
+int sgdlm_get_proposal_info(sgdlm_handle h, sgdlm_proposal_info *info);
+/* The network's sizes: parameters (flat FP32 layout W1 (128 x F), b1, W2 (128 x
+ * 128), b2, W3 (O x 128), b3), features F = 2 max_p + 5, outputs O = 2 max_p + 2. */
+int sgdlm_proposal_sizes(sgdlm_handle h, size_t *n_params, int *n_features, int *n_outputs);
+int sgdlm_proposal_get_params(sgdlm_handle h, float *params);
+int sgdlm_proposal_set_params(sgdlm_handle h, const float *params);
+/* One forward and backward pass on host data (batch rows of normalised features
+ * X (F), targets Y (O) and mask (O)): the masked MSE and the gradient of every
+ * parameter (flat layout); the parameters are left unchanged. */
+int sgdlm_proposal_loss_and_gradient(sgdlm_handle h, size_t batch, const float *X, const float *Y,
+                                     const float *mask, double *loss, float *grad);
+/* The last learned call's proposal q (m_q P x m, C_q P x P x m, n_q, s_q m) and
+ * the draws' log weights (nsim); any pointer may be NULL. */
+int sgdlm_get_proposal_state(sgdlm_handle h, double *m_q, double *C_q, double *n_q, double *s_q,
+                             double *log_weights);
+
 /* ---- fused device-resident filter step (GB300 path; asynchronous) ----
  * One README time step (README.md:103-154) on the handle's stream with no host
  * synchronisation: computePosterior(y, F) -> computeVBPosterior(nsim) ->
