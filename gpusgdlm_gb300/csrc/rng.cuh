@@ -68,7 +68,11 @@ __host__ __device__ __forceinline__ uint32_t tag_sub(uint32_t tag, uint32_t sub)
 
 // Uniform on the open interval (0, 1).
 //   double: (x + 1/2) 2^-32, exact.
-//   float : (x>>9 + 1/2) 2^-23, exact (24 significant bits).
+//   float : the same value rounded to float (within 2^-23 relative of it), so the
+//           lower tail keeps its resolution: Box-Muller's log(u) and the gamma
+//           boost's u^(1/a) then follow the FP64 stream draw by draw even for the
+//           smallest u (a grid of 2^-23 absolute would move those tails by
+//           percents).  Values that round up to 1 become the largest float below 1.
 template <typename T> struct Uniform;
 template <> struct Uniform<double> {
   __host__ __device__ static __forceinline__ double of(uint32_t x) {
@@ -77,7 +81,8 @@ template <> struct Uniform<double> {
 };
 template <> struct Uniform<float> {
   __host__ __device__ static __forceinline__ float of(uint32_t x) {
-    return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-07f;  // 2^-23
+    const float u = ((float)x + 0.5f) * 2.3283064365386963e-10f;  // 2^-32
+    return u < 1.0f ? u : 0.99999994f;
   }
 };
 
