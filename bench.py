@@ -284,6 +284,107 @@ def run_fp64_form(args, s_mixed, wl, t0, dev, rank):
     return dict(ms=ms, steps=k)
 
 
+def run_c3(args):
+    """The batched form: 64 independent instances with m_i ~ Uniform{20..400}
+    (p_j <= 20, the true-SGDLM data with per-instance seeds), 10k IS draws and a
+    10k-draw one-step forecast per instance per step, mixed precision.  After a
+    few burn-in steps, timed time steps of (a) every instance one at a time
+    (its fused device step, synchronised before the next instance), (b) the
+    batch: one CUDA-graph launch per time step whose branches run concurrently,
+    (c) the batch after the autotuner (LU plan per m bucket, LU grid
+    concurrency).  Inputs of each step are staged in HBM beforehand and copied
+    into the recorded buffers with one device copy per step."""
+    import torch
+
+    from gpusgdlm_gb300 import Batch, SGDLM
+
+    K, n = args.c3_instances, args.nsim
+    rng = np.random.default_rng(args.seed + 3)
+    ms = rng.integers(20, 401, size=K)
+    T = args.c3_burn_in + 3 * args.c3_steps + 2
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    engines, wls = [], []
+    for k, m in enumerate(ms):
+        m = int(m)
+        wl = make_workload(m=m, kmax=17, T=T + 1, seed=args.seed + 1000 + k)
+        P = wl["P"]
+        s = SGDLM(1, strict=True, precision="mixed")
+        s.setSimultaneousParents(wl["p"], np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float))
+        s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+        a, R, r, c = prior_arrays(m, P)
+        s.setPriorParameters(a, R, r, c)
+        s.setRngState(5000 + k, 0)
+        s._ensure_sim(n, n)
+        engines.append(s)
+        wls.append(wl)
+    # packed per-step inputs: for instance k, y (m), F (P m), x (P m)
+    sizes = [wl["m"] * (1 + 2 * wl["P"]) for wl in wls]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    staged = np.zeros((T, offs[-1]))
+    for t in range(1, T):
+        for k, wl in enumerate(wls):
+            m, P = wl["m"], wl["P"]
+            o = offs[k]
+            staged[t, o:o + m] = wl["y"][t]
+            staged[t, o + m:o + m + P * m] = wl["F_of"](t).ravel(order="F")
+            staged[t, o + m + P * m:o + m + 2 * P * m] = wl["F_of"](t + 1, False).ravel(order="F")
+    staged = torch.tensor(staged, dtype=torch.float64, device=dev)
+    cur = torch.zeros(offs[-1], dtype=torch.float64, device=dev)
+    fcs = [torch.zeros(n * wl["m"], dtype=torch.float64, device=dev) for wl in wls]
+    base = cur.data_ptr()
+    yp = [base + 8 * int(offs[k]) for k in range(K)]
+    Fp = [base + 8 * int(offs[k] + wls[k]["m"]) for k in range(K)]
+    xp = [base + 8 * int(offs[k] + wls[k]["m"] * (1 + wls[k]["P"])) for k in range(K)]
+    b = Batch(engines)
+    b.record(yp, Fp, xp, n / 2.0, [f.data_ptr() for f in fcs], None, None)
+
+    def load(t):
+        cur.copy_(staged[t])
+        torch.cuda.synchronize()
+
+    def batched(t0, t1):
+        for t in range(t0, t1):
+            load(t)
+            b.step()
+        for s in engines:
+            s.synchronize()
+
+    def one_at_a_time(t0, t1):
+        for t in range(t0, t1):
+            load(t)
+            for k, s in enumerate(engines):
+                assert s.filterStepDevice(yp[k], Fp[k], xp[k], n / 2.0, fcs[k].data_ptr(), None, None)
+                s.synchronize()
+
+    t = 1
+    batched(t, t + args.c3_burn_in)
+    t += args.c3_burn_in
+    res = {}
+    for name, fn in (("one_at_a_time", one_at_a_time), ("batched", batched)):
+        fn(t, t + 1)  # warm-up
+        t += 1
+        t0 = time.perf_counter()
+        fn(t, t + args.c3_steps - 1)
+        res[name] = (args.c3_steps - 1) / (time.perf_counter() - t0)
+        t += args.c3_steps - 1
+    tune = b.autotune(replays=3)
+    batched(t, t + 1)
+    t += 1
+    t0 = time.perf_counter()
+    batched(t, t + args.c3_steps - 1)
+    res["batched_autotuned"] = (args.c3_steps - 1) / (time.perf_counter() - t0)
+    b.close()
+    for s in engines:
+        s.close()
+    return {"workload": f"{K} instances, m in [{int(ms.min())}, {int(ms.max())}] (Uniform{{20..400}}), "
+                        f"p_j<=20, {n} IS + {n} forecast draws per instance per step, mixed",
+            "time_steps_per_s": res,
+            "instance_steps_per_s": {k: v * K for k, v in res.items()},
+            "speedup_batched_autotuned_vs_one_at_a_time": res["batched_autotuned"] / res["one_at_a_time"],
+            "autotune": tune, "timed_steps": args.c3_steps - 1, "burn_in_steps": args.c3_burn_in,
+            "note": "wall clock per time step (a host synchronisation per step for the input copy)"}
+
+
 def run_c4(args):
     """The learned-proposal configuration: m = 200, p_j <= 15 (3 external +
     Uniform{0..12} simultaneous parents), the true-SGDLM data, T = 2000 steps of
@@ -564,6 +665,10 @@ def main():
                     help="cap on the reference arm's timed full-size steps")
     ap.add_argument("--fp64-steps", type=int, default=3,
                     help="timed steps of the plain FP64 form (0: skip)")
+    ap.add_argument("--c3-instances", type=int, default=64,
+                    help="instances of the batched-form comparison (0: skip)")
+    ap.add_argument("--c3-steps", type=int, default=12)
+    ap.add_argument("--c3-burn-in", type=int, default=5)
     ap.add_argument("--c4-steps", type=int, default=2000,
                     help="time steps of the learned-proposal comparison (0: skip)")
     ap.add_argument("--seed", type=int, default=20261203)
@@ -640,6 +745,8 @@ def main():
     }
     if args.c4_steps > 0:
         line["ess_per_s"] = run_c4(args)
+    if args.c3_instances > 0:
+        line["batched_instances"] = run_c3(args)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     print(json.dumps(line))

@@ -4,7 +4,7 @@
 in-tree CUDA library ``libsgdlm_gb300.so`` (hand-written sm_103a kernels behind
 the C ABI of include/sgdlm.h).  There is no CPU fallback.
 """
-from .sgdlm import SGDLM, SGDLMError, encode_sp, NA_UNSIGNED  # noqa: F401
+from .sgdlm import SGDLM, Batch, SGDLMError, encode_sp, NA_UNSIGNED  # noqa: F401
 from . import _lib  # noqa: F401
 
-__all__ = ["SGDLM", "SGDLMError", "encode_sp", "NA_UNSIGNED"]
+__all__ = ["SGDLM", "Batch", "SGDLMError", "encode_sp", "NA_UNSIGNED"]

@@ -89,6 +89,35 @@ class ProposalInfo(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class LuTuning(C.Structure):
+    _fields_ = [
+        ("levels", C.c_int),
+        ("tensor_cores", C.c_int),
+        ("core_n", C.c_int),
+        ("ms", C.c_double),
+        ("ms_candidates", C.c_double * 8),
+    ]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["ms_candidates"] = list(self.ms_candidates)
+        return d
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [
+        ("buckets", C.c_int),
+        ("concurrency", C.c_int),
+        ("ms_per_step", C.c_double),
+        ("ms_candidates", C.c_double * 4),
+    ]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["ms_candidates"] = list(self.ms_candidates)
+        return d
+
+
 PROPOSAL_PLAIN = 0
 PROPOSAL_LEARNED = 1
 
@@ -153,6 +182,16 @@ SIGNATURES = {
     "sgdlm_get_proposal_state": [_H, _Pd, _Pd, _Pd, _Pd, _Pd],
     "sgdlm_filter_step_device": [_H, C.c_void_p, C.c_void_p, C.c_void_p, _d, C.c_void_p,
                                  C.c_void_p, C.c_void_p],
+    "sgdlm_set_lu_options": [_H, _i, _i],
+    "sgdlm_get_lu_options": [_H, _Pi, _Pi],
+    "sgdlm_tune_lu": [_H, C.POINTER(LuTuning)],
+    "sgdlm_batch_create": [C.POINTER(_H), _sz, C.POINTER(C.c_void_p)],
+    "sgdlm_batch_destroy": [C.c_void_p],
+    "sgdlm_batch_record": [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                           C.POINTER(C.c_void_p), _d, C.POINTER(C.c_void_p),
+                           C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)],
+    "sgdlm_batch_step": [C.c_void_p],
+    "sgdlm_batch_autotune": [C.c_void_p, _i, C.POINTER(BatchTuning)],
     "sgdlm_get_stream": [_H, C.POINTER(C.c_void_p)],
     "sgdlm_synchronize": [_H],
     "sgdlm_get_launch_count": [_H, _Pu64],

@@ -147,6 +147,7 @@ struct sgdlm_engine {
   DevBuf<double> mean_m, mean_C, mean_n, mean_s, mean_lambda, mean_log_lambda, mean_Q;
   DevBuf<uint32_t> dev_epoch;
   LuPlan plan{};
+  LuOptions lu_opt{};
   ProposalState prop;
   int chunks = 0;          // VB draw chunks and draws per chunk (vb_chunking)
   long chunk_draws = 0;
@@ -442,9 +443,9 @@ int plan_sim(sgdlm_engine *h, long n, LuPlan *out) {
   const int nv = h->elim_dev.nv;
   LuPlan pl = (h->precision == SGDLM_PRECISION_FP64)
                   ? plan_lu<double>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv,
-                                    h->elim_dev.n_solve, h->elim_dev.prog_len)
+                                    h->elim_dev.n_solve, h->elim_dev.prog_len, h->lu_opt)
                   : plan_lu<float>((int)h->m, (int)h->P, n, h->num_sms, core_n, nv,
-                                   h->elim_dev.n_solve, h->elim_dev.prog_len);
+                                   h->elim_dev.n_solve, h->elim_dev.prog_len, h->lu_opt);
   if (pl.smem > 227 * 1024 - 64 || pl.smem_fallback > 227 * 1024 - 64) {
     char buf[200];
     snprintf(buf, sizeof buf,
@@ -519,6 +520,15 @@ int validate_parents(sgdlm_engine *h, const unsigned *p, const unsigned *sp) {
 }
 
 template <typename T> T *as(DevBuf<unsigned char> &b) { return reinterpret_cast<T *>(b.ptr); }
+
+// The device-side epoch counter (read by the fused step) follows the host's, so
+// that API calls and fused steps never reuse an epoch.
+void advance_device_epoch(sgdlm_engine *h, uint32_t delta) {
+  if (h->dev_epoch.ptr) {
+    launch_advance_epoch(h->stream, h->dev_epoch.ptr, delta);
+    h->launches += 1;
+  }
+}
 
 // sample -> LU -> fallback, from the given normal-gamma parameters (posterior
 // for VB, forecasting prior for forecasts).
@@ -759,6 +769,7 @@ int vb_posterior(sgdlm_engine *h, double *o_m, double *o_C, double *o_n, double 
   const bool learned = use_learned && q.info.deployed;
   const RngKey key = h->key((uint32_t)h->epoch);
   h->epoch += 1;
+  advance_device_epoch(h, 1);
   q.info.ess_learned = q.info.ess_plain = 0.0;
   q.info.used_learned = 0;
   CK(cudaEventRecord(h->ev[0], s));
@@ -828,6 +839,7 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
   if ((st = h2d(h, h->x_t.ptr, x, P * m * sizeof(double)))) return st;
   const RngKey key = h->key((uint32_t)h->epoch);
   h->epoch += 1;
+  advance_device_epoch(h, 1);
   CK(cudaEventRecord(h->ev[0], s));
   CK(cudaMemsetAsync(h->draw_flags.ptr, 0, n * sizeof(int), s));
   if (!use_existing)
@@ -903,6 +915,7 @@ template <typename T> int evolve(sgdlm_engine *h, bool with_G = false) {
   const long n = (long)h->nsim;
   const RngKey key = h->key((uint32_t)h->epoch);
   h->epoch += 1;
+  advance_device_epoch(h, 1);
   // chol(W) of the forecasting copy (SGDLM.cu:742-747); the forecasting r, c and
   // W are not re-discounted between steps (HostWrapperImpl.cu:891-900)
   launch_cholesky(h->stream, m, P, h->p.ptr, h->fW_t.ptr, h->U64.ptr, h->U32.ptr);
@@ -1626,6 +1639,356 @@ int sgdlm_filter_step_device(sgdlm_handle h, const double *d_y, const double *d_
   if (st) return st;
   h->is_prior = true;
   return SGDLM_OK;
+}
+
+int sgdlm_set_lu_options(sgdlm_handle h, int allow_tensor_cores, int max_ctas) {
+  HCHECK(h);
+  if (max_ctas < 0) return h->fail(SGDLM_ERR_BAD_ARG, "max_ctas must not be negative");
+  h->lu_opt.allow_tc = allow_tensor_cores ? 1 : 0;
+  h->lu_opt.max_grid = max_ctas;
+  if (!h->mem_init) return SGDLM_OK;
+  cudaStreamSynchronize(h->stream);
+  return replan_sim(h);
+}
+
+int sgdlm_get_lu_options(sgdlm_handle h, int *allow_tensor_cores, int *max_ctas) {
+  HCHECK(h);
+  if (allow_tensor_cores) *allow_tensor_cores = h->lu_opt.allow_tc;
+  if (max_ctas) *max_ctas = h->lu_opt.max_grid;
+  return SGDLM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+template <typename T> int tune_lu(sgdlm_engine *h, sgdlm_lu_tuning *out) {
+  const int levels0 = h->elim_levels;
+  const LuOptions opt0 = h->lu_opt;
+  CK(cudaMemsetAsync(h->draw_flags.ptr, 0, h->nsim * sizeof(int), h->stream));
+  sample_draws<T>(h, h->m_t.ptr, h->C_t.ptr, h->n_t.ptr, h->s_t.ptr, h->key((uint32_t)h->epoch));
+  const int cand_levels[4] = {0, 2, 4, 6};
+  double best = 1e300;
+  int best_l = levels0, best_tc = opt0.allow_tc;
+  for (int q = 0; q < 8; ++q) out->ms_candidates[q] = -1.0;
+  for (int li = 0; li < 4; ++li)
+    for (int tc = 1; tc >= 0; --tc) {
+      if (tc == 0 && std::is_same<T, double>::value) continue;  // FP64 has no tensor-core path
+      h->lu_opt.allow_tc = tc;
+      int st = sgdlm_set_elimination_levels(h, cand_levels[li]);
+      if (st) return st;
+      if (tc == 1 && !h->plan.tc && !std::is_same<T, double>::value) {
+        // no tensor-core plan for this core: the FFMA candidate covers it
+        continue;
+      }
+      std::vector<float> ms;
+      for (int rep = 0; rep < 4; ++rep) {
+        CK(cudaEventRecord(h->ev[5], h->stream));
+        if ((st = lu_draws<T>(h, nullptr, h->key((uint32_t)h->epoch), nullptr))) return st;
+        CK(cudaEventRecord(h->ev[6], h->stream));
+        if ((st = sync(h))) return st;
+        if (rep > 0) ms.push_back(elapsed(h->ev[5], h->ev[6]));
+      }
+      std::sort(ms.begin(), ms.end());
+      const double t = ms[ms.size() / 2];
+      out->ms_candidates[2 * li + (1 - tc)] = t;
+      if (t < best) {
+        best = t;
+        best_l = cand_levels[li];
+        best_tc = h->plan.tc;
+      }
+    }
+  h->lu_opt.allow_tc = best_tc;
+  int st = sgdlm_set_elimination_levels(h, best_l);
+  if (st) return st;
+  out->levels = h->eplan.nlev;
+  out->tensor_cores = h->plan.tc;
+  out->core_n = h->eplan.core_n;
+  out->ms = best;
+  return SGDLM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int sgdlm_tune_lu(sgdlm_handle h, sgdlm_lu_tuning *out) {
+  HCHECK(h);
+  if (!out) return SGDLM_ERR_BAD_ARG;
+  if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+  if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+  *out = sgdlm_lu_tuning{};
+  return h->precision == SGDLM_PRECISION_FP64 ? tune_lu<double>(h, out) : tune_lu<float>(h, out);
+}
+
+}  // extern "C"
+
+struct sgdlm_batch {
+  std::vector<sgdlm_engine *> eng;
+  cudaStream_t origin = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> launches_per_step;
+  // the recording's arguments (re-recorded by the autotuner)
+  std::vector<const double *> y, F, x;
+  std::vector<double *> fc, w, st;
+  double ess = 0.0;
+  bool recorded = false;
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    recorded = false;
+  }
+};
+
+namespace {
+
+// Captures every engine's fused step into b->graph: the origin stream forks to
+// the engines' streams, each runs its step, and they join back.
+int batch_capture(sgdlm_batch *b) {
+  b->drop_graph();
+  const size_t k = b->eng.size();
+  cudaError_t e = cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return SGDLM_ERR_DEVICE;
+  int status = SGDLM_OK;
+  e = cudaEventRecord(b->fork, b->origin);
+  for (size_t i = 0; i < k && e == cudaSuccess && status == SGDLM_OK; ++i) {
+    sgdlm_engine *h = b->eng[i];
+    e = cudaStreamWaitEvent(h->stream, b->fork, 0);
+    if (e != cudaSuccess) break;
+    const uint64_t l0 = h->launches, ep0 = h->epoch;
+    status = h->precision == SGDLM_PRECISION_FP64
+                 ? filter_step<double>(h, b->y[i], b->F[i], b->x[i], b->ess, b->fc[i], b->w[i],
+                                       b->st[i])
+                 : filter_step<float>(h, b->y[i], b->F[i], b->x[i], b->ess, b->fc[i], b->w[i],
+                                      b->st[i]);
+    b->launches_per_step[i] = h->launches - l0;
+    h->launches = l0;   // counted when the graph runs
+    h->epoch = ep0;     // advanced when the graph runs
+    if (status == SGDLM_OK) e = cudaEventRecord(b->join[i], h->stream);
+    if (e == cudaSuccess && status == SGDLM_OK) e = cudaStreamWaitEvent(b->origin, b->join[i], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(b->origin, &g);
+  if (status != SGDLM_OK || e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+    return status != SGDLM_OK ? status : SGDLM_ERR_DEVICE;
+  }
+  b->graph = g;
+  if (cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
+    b->drop_graph();
+    return SGDLM_ERR_DEVICE;
+  }
+  b->recorded = true;
+  return SGDLM_OK;
+}
+
+int batch_launch(sgdlm_batch *b) {
+  for (size_t i = 0; i < b->eng.size(); ++i) {
+    if (cudaEventRecord(b->join[i], b->eng[i]->stream) != cudaSuccess ||
+        cudaStreamWaitEvent(b->origin, b->join[i], 0) != cudaSuccess)
+      return SGDLM_ERR_DEVICE;
+  }
+  if (cudaGraphLaunch(b->exec, b->origin) != cudaSuccess) return SGDLM_ERR_DEVICE;
+  if (cudaEventRecord(b->done, b->origin) != cudaSuccess) return SGDLM_ERR_DEVICE;
+  for (size_t i = 0; i < b->eng.size(); ++i) {
+    sgdlm_engine *h = b->eng[i];
+    if (cudaStreamWaitEvent(h->stream, b->done, 0) != cudaSuccess) return SGDLM_ERR_DEVICE;
+    h->epoch += 2;
+    h->launches += b->launches_per_step[i];
+    h->is_prior = true;
+  }
+  return SGDLM_OK;
+}
+
+// Parameters and RNG states of every engine, for the autotuner's trial steps.
+struct BatchSnapshot {
+  std::vector<std::vector<double>> m, C, n, s;
+  std::vector<uint64_t> seed, epoch;
+};
+int batch_save(sgdlm_batch *b, BatchSnapshot &snap) {
+  const size_t k = b->eng.size();
+  snap.m.resize(k); snap.C.resize(k); snap.n.resize(k); snap.s.resize(k);
+  snap.seed.resize(k); snap.epoch.resize(k);
+  for (size_t i = 0; i < k; ++i) {
+    sgdlm_engine *h = b->eng[i];
+    snap.m[i].resize(h->P * h->m);
+    snap.C[i].resize(h->P * h->P * h->m);
+    snap.n[i].resize(h->m);
+    snap.s[i].resize(h->m);
+    int st = sgdlm_get_parameters(h, snap.m[i].data(), snap.C[i].data(), snap.n[i].data(),
+                                  snap.s[i].data());
+    if (st) return st;
+    snap.seed[i] = h->seed;
+    snap.epoch[i] = h->epoch;
+  }
+  return SGDLM_OK;
+}
+int batch_restore(sgdlm_batch *b, const BatchSnapshot &snap) {
+  for (size_t i = 0; i < b->eng.size(); ++i) {
+    sgdlm_engine *h = b->eng[i];
+    int st = sgdlm_set_parameters(h, snap.m[i].data(), snap.C[i].data(), snap.n[i].data(),
+                                  snap.s[i].data());
+    if (!st) st = sgdlm_set_is_prior(h, 1);
+    if (!st) st = sgdlm_set_rng_state(h, snap.seed[i], snap.epoch[i]);
+    if (st) return st;
+  }
+  return SGDLM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgdlm_batch_create(const sgdlm_handle *handles, size_t count, sgdlm_batch_handle *out) {
+  if (!out || !handles || count < 1) return SGDLM_ERR_BAD_ARG;
+  *out = nullptr;
+  std::unique_ptr<sgdlm_batch> b(new sgdlm_batch());
+  for (size_t i = 0; i < count; ++i) {
+    if (!handles[i]) return SGDLM_ERR_BAD_ARG;
+    if (handles[i]->device != handles[0]->device)
+      return handles[i]->fail(SGDLM_ERR_BAD_ARG, "the engines of a batch share one device");
+    for (size_t q = 0; q < i; ++q)
+      if (handles[q] == handles[i])
+        return handles[i]->fail(SGDLM_ERR_BAD_ARG, "an engine appears twice in the batch");
+    b->eng.push_back(handles[i]);
+  }
+  cudaSetDevice(handles[0]->device);
+  if (cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess)
+    return SGDLM_ERR_DEVICE;
+  b->join.assign(count, nullptr);
+  for (auto &e : b->join)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return SGDLM_ERR_DEVICE;
+  b->launches_per_step.assign(count, 0);
+  *out = b.release();
+  return SGDLM_OK;
+}
+
+int sgdlm_batch_destroy(sgdlm_batch_handle b) {
+  if (!b) return SGDLM_OK;
+  if (b->origin) cudaStreamSynchronize(b->origin);
+  b->drop_graph();
+  for (auto e : b->join)
+    if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->origin) cudaStreamDestroy(b->origin);
+  delete b;
+  return SGDLM_OK;
+}
+
+int sgdlm_batch_record(sgdlm_batch_handle b, const double *const *d_y, const double *const *d_F,
+                       const double *const *d_x, double ess_threshold,
+                       double *const *d_forecast, double *const *d_is_weights,
+                       double *const *d_step_stats) {
+  if (!b || !d_y || !d_F) return SGDLM_ERR_BAD_ARG;
+  const size_t k = b->eng.size();
+  for (size_t i = 0; i < k; ++i) {
+    sgdlm_engine *h = b->eng[i];
+    cudaSetDevice(h->device);
+    if (!h->check_initialized()) return SGDLM_ERR_NOT_INIT;
+    if (!h->check_sim_initialized()) return SGDLM_ERR_SIM_NOT_INIT;
+    if (!h->check_prior(true)) return SGDLM_ERR_WRONG_STATE;
+    if (!d_y[i] || !d_F[i]) return h->fail(SGDLM_ERR_BAD_ARG, "null input");
+  }
+  b->y.assign(d_y, d_y + k);
+  b->F.assign(d_F, d_F + k);
+  b->x.assign(k, nullptr);
+  b->fc.assign(k, nullptr);
+  b->w.assign(k, nullptr);
+  b->st.assign(k, nullptr);
+  for (size_t i = 0; i < k; ++i) {
+    if (d_x) b->x[i] = d_x[i];
+    if (d_forecast) b->fc[i] = d_forecast[i];
+    if (d_is_weights) b->w[i] = d_is_weights[i];
+    if (d_step_stats) b->st[i] = d_step_stats[i];
+  }
+  b->ess = ess_threshold;
+  for (auto *h : b->eng) cudaStreamSynchronize(h->stream);
+  return batch_capture(b);
+}
+
+int sgdlm_batch_step(sgdlm_batch_handle b) {
+  if (!b) return SGDLM_ERR_BAD_ARG;
+  if (!b->recorded) return SGDLM_ERR_WRONG_STATE;
+  cudaSetDevice(b->eng[0]->device);
+  return batch_launch(b);
+}
+
+int sgdlm_batch_autotune(sgdlm_batch_handle b, int replays, sgdlm_batch_tuning *out) {
+  if (!b || !out || replays < 1) return SGDLM_ERR_BAD_ARG;
+  if (!b->recorded) return SGDLM_ERR_WRONG_STATE;
+  cudaSetDevice(b->eng[0]->device);
+  *out = sgdlm_batch_tuning{};
+  for (auto *h : b->eng) cudaStreamSynchronize(h->stream);
+  // (1) per m bucket (m rounded up to 32): tune the LU on one engine, apply to the rest
+  std::vector<int> bucket_done;
+  for (size_t i = 0; i < b->eng.size(); ++i) {
+    sgdlm_engine *h = b->eng[i];
+    const int bucket = (int)((h->m + 31) / 32);
+    bool seen = false;
+    for (int q : bucket_done) seen |= (q == bucket);
+    if (seen) continue;
+    bucket_done.push_back(bucket);
+    sgdlm_lu_tuning t{};
+    int st = sgdlm_tune_lu(h, &t);
+    if (st) return st;
+    for (size_t j = 0; j < b->eng.size(); ++j) {
+      sgdlm_engine *g = b->eng[j];
+      if (j == i || (int)((g->m + 31) / 32) != bucket) continue;
+      g->lu_opt.allow_tc = h->lu_opt.allow_tc;
+      if ((st = sgdlm_set_elimination_levels(g, h->elim_levels))) return st;
+    }
+  }
+  out->buckets = (int)bucket_done.size();
+  // (2) concurrency: each engine's LU grid capped at 2 x SMs / c, timed on the graph
+  BatchSnapshot snap;
+  int st = batch_save(b, snap);
+  if (st) return st;
+  const int cs[4] = {1, 2, 4, 8};
+  double best = 1e300;
+  int best_c = 1;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int ci = 0; ci < 4; ++ci) {
+    for (auto *h : b->eng)
+      if ((st = sgdlm_set_lu_options(h, h->lu_opt.allow_tc, cs[ci] == 1 ? 0 : 2 * h->num_sms / cs[ci])))
+        break;
+    if (!st) st = batch_capture(b);
+    if (!st) st = batch_launch(b);  // warm-up
+    if (!st) {
+      cudaEventRecord(e0, b->origin);
+      for (int r = 0; r < replays && !st; ++r) st = batch_launch(b);
+      cudaEventRecord(e1, b->origin);
+      cudaEventSynchronize(e1);
+    }
+    for (auto *h : b->eng) cudaStreamSynchronize(h->stream);
+    if (st) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    out->ms_candidates[ci] = ms / replays;
+    if (ms / replays < best) {
+      best = ms / replays;
+      best_c = cs[ci];
+    }
+    if ((st = batch_restore(b, snap))) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  for (auto *h : b->eng)
+    if ((st = sgdlm_set_lu_options(h, h->lu_opt.allow_tc, best_c == 1 ? 0 : 2 * h->num_sms / best_c)))
+      return st;
+  if ((st = batch_restore(b, snap))) return st;
+  out->concurrency = best_c;
+  out->ms_per_step = best;
+  return batch_capture(b);
 }
 
 int sgdlm_get_stream(sgdlm_handle h, void **stream) {

@@ -88,11 +88,18 @@ struct LuPlan {
   size_t scratch_elems_per_cta;  // dense core + per-draw values of the sparse levels
   size_t scratch_elems_total;    // covers both passes
 };
+// Tuning knobs of the fast pass: allow_tc = 0 keeps the FFMA instantiation where
+// the tensor-core one would apply; max_grid > 0 caps the persistent grid (fewer
+// CTAs, more draws each: room for other work on the GPU at the same time).
+struct LuOptions {
+  int allow_tc = 1;
+  int max_grid = 0;
+};
 // core_n / nv / n_solve / prog_len come from the elimination plan (core_n = m and
 // the others 0 without one).
 template <typename T>
 LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solve = 0,
-               int prog_len = 0);
+               int prog_len = 0, LuOptions opt = LuOptions{});
 // Row-wise list of the Gamma entries of (I - Gamma): for row r, entries
 // rowptr[r] .. rowptr[r+1]-1 are (e = j*P + k, column).  Built on the host from
 // the parental sets; gives the forecast residual a fixed summation order.

@@ -2284,7 +2284,8 @@ size_t smem_budget(int per_sm) {
 }  // namespace
 
 template <typename T>
-LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solve, int prog_len) {
+LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solve, int prog_len,
+               LuOptions opt) {
   LuPlan pl{};
   pl.m = m;
   pl.P = P;
@@ -2297,7 +2298,7 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solv
   // tensor-core path for FP32 draws while the trailing update's first tile (R <= 192
   // columns) and the block multipliers (64 columns) fit the CTA's 256 columns of
   // tensor memory together: d_p <= 224
-  pl.tc = (sizeof(T) == 4 && pl.dp <= 224) ? 1 : 0;
+  pl.tc = (sizeof(T) == 4 && pl.dp <= 224 && opt.allow_tc) ? 1 : 0;
   const size_t with_vals = Smem(pl.dp, m, sizeof(T), nv, pl.tc != 0).total;
   pl.vals_smem = (nv > 0 && with_vals <= smem_budget(target)) ? 1 : 0;
   pl.smem = Smem(pl.dp, m, sizeof(T), pl.vals_smem ? nv : 0, pl.tc != 0).total;
@@ -2312,6 +2313,7 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solv
   int ctas_per_sm = pl.smem <= smem_budget(2) ? 2 : 1;
   if (sizeof(T) == 8) ctas_per_sm = 1;
   long grid = (long)num_sms * ctas_per_sm;
+  if (opt.max_grid > 0 && grid > opt.max_grid) grid = opt.max_grid;
   if (grid > n) grid = n;
   if (grid < 1) grid = 1;
   pl.grid = (int)grid;
@@ -2379,8 +2381,8 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const unsigned
       rows, pivot_list);
 }
 
-template LuPlan plan_lu<float>(int, int, long, int, int, int, int, int);
-template LuPlan plan_lu<double>(int, int, long, int, int, int, int, int);
+template LuPlan plan_lu<float>(int, int, long, int, int, int, int, int, LuOptions);
+template LuPlan plan_lu<double>(int, int, long, int, int, int, int, int, LuOptions);
 template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
                                const unsigned *, const float *, const float *, float *,
                                double *, int *,

@@ -492,6 +492,24 @@ class SGDLM:
             return None
         return {"m": mq, "C": Cq, "n": nq, "s": sq, "log_weights": lw}
 
+    # ------------------------------------------------------------ LU tuning
+    def setLuOptions(self, allow_tensor_cores: bool = True, max_ctas: int = 0):
+        self._check(self._lib.sgdlm_set_lu_options(self._h, 1 if allow_tensor_cores else 0,
+                                                   int(max_ctas)))
+
+    def getLuOptions(self):
+        tc, mx = C.c_int(), C.c_int()
+        self._lib.sgdlm_get_lu_options(self._h, C.byref(tc), C.byref(mx))
+        return {"allow_tensor_cores": bool(tc.value), "max_ctas": int(mx.value)}
+
+    def tuneLu(self):
+        """Times the batched LU over elimination levels and the tensor-core switch
+        and keeps the fastest (include/sgdlm.h, sgdlm_tune_lu)."""
+        t = L.LuTuning()
+        if not self._check(self._lib.sgdlm_tune_lu(self._h, C.byref(t))):
+            return None
+        return t.as_dict()
+
     def launchCount(self) -> int:
         v = C.c_uint64()
         self._lib.sgdlm_get_launch_count(self._h, C.byref(v))
@@ -513,3 +531,57 @@ class SGDLM:
             self._h, C.c_void_p(d_y), C.c_void_p(d_F), C.c_void_p(d_x) if d_x else None,
             float(ess_threshold), C.c_void_p(d_forecast) if d_forecast else None,
             C.c_void_p(d_weights) if d_weights else None, C.c_void_p(d_stats) if d_stats else None))
+
+
+class Batch:
+    """Several engines advanced together: one CUDA-graph launch per time step
+    whose branches (one fused step per engine) run concurrently
+    (include/sgdlm.h, sgdlm_batch_*).  The engines stay owned by the caller."""
+
+    def __init__(self, engines):
+        self._lib = L.lib()
+        self.engines = list(engines)
+        hs = (L._H * len(self.engines))(*[e._h for e in self.engines])
+        self._b = C.c_void_p()
+        st = self._lib.sgdlm_batch_create(hs, len(self.engines), C.byref(self._b))
+        if st != L.OK:
+            raise SGDLMError(f"sgdlm_batch_create failed: {L.STATUS.get(st, st)}")
+
+    def close(self):
+        if self._b:
+            self._lib.sgdlm_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _ptrs(values):
+        if values is None:
+            return None
+        return (C.c_void_p * len(values))(*[C.c_void_p(v) if v else None for v in values])
+
+    def record(self, d_y, d_F, d_x=None, ess_threshold=0.0, d_forecast=None, d_weights=None,
+               d_stats=None):
+        """Records one fused step per engine (device pointers as integers, one per engine)."""
+        st = self._lib.sgdlm_batch_record(self._b, self._ptrs(d_y), self._ptrs(d_F),
+                                          self._ptrs(d_x), float(ess_threshold),
+                                          self._ptrs(d_forecast), self._ptrs(d_weights),
+                                          self._ptrs(d_stats))
+        if st != L.OK:
+            raise SGDLMError(f"sgdlm_batch_record failed: {L.STATUS.get(st, st)}")
+
+    def step(self):
+        st = self._lib.sgdlm_batch_step(self._b)
+        if st != L.OK:
+            raise SGDLMError(f"sgdlm_batch_step failed: {L.STATUS.get(st, st)}")
+
+    def autotune(self, replays: int = 3) -> dict:
+        t = L.BatchTuning()
+        st = self._lib.sgdlm_batch_autotune(self._b, int(replays), C.byref(t))
+        if st != L.OK:
+            raise SGDLMError(f"sgdlm_batch_autotune failed: {L.STATUS.get(st, st)}")
+        return t.as_dict()

@@ -246,6 +246,58 @@ int sgdlm_filter_step_device(sgdlm_handle h, const double *d_y, const double *d_
  * race.  Runs on `stream` (a cudaStream_t) and returns without synchronising. */
 int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const float *d_theta,
                           const unsigned *d_sp, double *d_log_det, int *d_flags, void *stream);
+/* ---- LU tuning and the batched multi-instance step (no counterpart in the
+ * reference, which runs one engine per handle and per stream,
+ * HostWrapperImpl.cu:47-61) ---- */
+/* Fast-pass options of the batched LU: allow_tensor_cores = 0 keeps the FFMA
+ * path where the tensor-core one applies (d_p <= 224, mixed precision);
+ * max_ctas > 0 caps its persistent grid (more draws per CTA, fewer CTAs: room
+ * for other instances on the GPU).  Results equal up to rounding. */
+int sgdlm_set_lu_options(sgdlm_handle h, int allow_tensor_cores, int max_ctas);
+int sgdlm_get_lu_options(sgdlm_handle h, int *allow_tensor_cores, int *max_ctas);
+typedef struct {
+  int levels;           /* chosen sparse elimination levels */
+  int tensor_cores;     /* chosen: 1 tensor-core fast pass, 0 FFMA */
+  int core_n;           /* dense core of the chosen plan */
+  double ms;            /* its LU time for nsim draws (median of 3) */
+  double ms_candidates[8]; /* levels {0, 2, 4, 6} x tensor cores {1, 0} (-1: not run) */
+} sgdlm_lu_tuning;
+/* Times the batched LU of the current draws' distribution (draws sampled once
+ * from the current parameters, the RNG epoch left unchanged) over the
+ * candidates and keeps the fastest; overwrites the draw buffers.  Needs
+ * initialised simulation memory. */
+int sgdlm_tune_lu(sgdlm_handle h, sgdlm_lu_tuning *out);
+
+typedef struct sgdlm_batch *sgdlm_batch_handle;
+/* A batch over `count` engines (each in the prior state with simulation memory)
+ * that advance together.  The engines stay owned by the caller and must outlive
+ * the batch. */
+int sgdlm_batch_create(const sgdlm_handle *handles, size_t count, sgdlm_batch_handle *out);
+int sgdlm_batch_destroy(sgdlm_batch_handle b);
+/* Records one fused time step of every engine (sgdlm_filter_step_device with
+ * instance i's device pointers, arrays of `count`; d_x, d_forecast, d_is_weights,
+ * d_step_stats may be NULL arrays or hold NULLs) into one CUDA graph whose
+ * branches, one per engine, run concurrently.  Re-recording replaces it. */
+int sgdlm_batch_record(sgdlm_batch_handle b, const double *const *d_y, const double *const *d_F,
+                       const double *const *d_x, double ess_threshold,
+                       double *const *d_forecast, double *const *d_is_weights,
+                       double *const *d_step_stats);
+/* One time step of every engine: one graph launch, ordered after the engines'
+ * earlier work and before their later work; returns without synchronising.
+ * The inputs are read from the recorded pointers (refresh them before). */
+int sgdlm_batch_step(sgdlm_batch_handle b);
+typedef struct {
+  int buckets;                 /* m buckets (m rounded up to 32) tuned */
+  int concurrency;             /* chosen c: each engine's LU grid capped at (2 x SMs) / c */
+  double ms_per_step;          /* batch step time with the chosen c */
+  double ms_candidates[4];     /* c = 1, 2, 4, 8 */
+} sgdlm_batch_tuning;
+/* Autotuner: per m bucket, sgdlm_tune_lu on one engine and its choice applied
+ * to the bucket; then the concurrency c by timing `replays` recorded steps per
+ * candidate (the engines' parameters and RNG states are restored afterwards)
+ * and re-records with the best.  Needs a recording. */
+int sgdlm_batch_autotune(sgdlm_batch_handle b, int replays, sgdlm_batch_tuning *out);
+
 /* The handle's CUDA stream (cudaStream_t), for events and graph capture. */
 int sgdlm_get_stream(sgdlm_handle h, void **stream);
 /* Blocks until the handle's stream is idle. */
