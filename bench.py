@@ -668,7 +668,7 @@ def main():
     ap.add_argument("--c3-instances", type=int, default=64,
                     help="instances of the batched-form comparison (0: skip)")
     ap.add_argument("--c3-steps", type=int, default=12)
-    ap.add_argument("--c3-burn-in", type=int, default=5)
+    ap.add_argument("--c3-burn-in", type=int, default=10)
     ap.add_argument("--c4-steps", type=int, default=2000,
                     help="time steps of the learned-proposal comparison (0: skip)")
     ap.add_argument("--seed", type=int, default=20261203)

@@ -31,6 +31,7 @@ SOURCES = [
     "noalloc.cu",
     "mlp_kernels.cu",
     "proposal_kernels.cu",
+    "forecast_kernels.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]

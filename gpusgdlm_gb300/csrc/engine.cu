@@ -148,6 +148,9 @@ struct sgdlm_engine {
   DevBuf<uint32_t> dev_epoch;
   LuPlan plan{};
   LuOptions lu_opt{};
+  JacobiPlan jac{};        // iterative forecast solves of FP32 draws
+  int forecast_iterative = 1;
+  DevBuf<int> jac_list;    // nsim + 1: count, then the forecast draws left to factor
   ProposalState prop;
   int chunks = 0;          // VB draw chunks and draws per chunk (vb_chunking)
   long chunk_draws = 0;
@@ -272,6 +275,7 @@ int upload_gamma_rows(sgdlm_engine *h) {
   CK(h->g_extk.alloc(extk.size()));
   CK(cudaMemcpy(h->g_extptr.ptr, extptr.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->g_extk.ptr, extk.data(), extk.size() * sizeof(int), cudaMemcpyHostToDevice));
+  h->jac = plan_jacobi((int)m, rowptr[m], h->num_sms);
   return SGDLM_OK;
 }
 
@@ -476,6 +480,7 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   CK(h->nu_fc.alloc(nsim * m));
   CK(h->draw_flags.alloc(nsim));
   CK(h->pivot_list.alloc(nsim + 1));
+  CK(h->jac_list.alloc(nsim + 1));
   CK(h->part_a.alloc((size_t)h->chunks * m * (P + 2) + m * P));
   CK(h->part_b.alloc((size_t)h->chunks * m * P * P));
   h->nsim = nsim;
@@ -557,11 +562,22 @@ int lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
                           h->x32.ptr, as<T>(h->lambda), key, h->nu_fc.ptr);
     h->launches += 2;
   }
+  // forecasts of FP32 draws: the iterative solve first; the LU kernels then
+  // factor only the draws it leaves in jac_list
+  const bool iterative = x && std::is_same<T, float>::value && h->forecast_iterative && h->jac.ok;
+  if (iterative) {
+    CK(cudaMemsetAsync(h->jac_list.ptr, 0, sizeof(int), h->stream));
+    launch_forecast_jacobi(h->stream, h->jac, (int)h->m, (int)h->P, n, rows,
+                           reinterpret_cast<const float *>(h->theta_dm.ptr), h->nu_fc.ptr, y,
+                           h->logdet.ptr, h->jac_list.ptr);
+    h->launches += 1;
+  }
   // the fast pass appends the draws it flags to pivot_list; the redo visits those
   CK(cudaMemsetAsync(h->pivot_list.ptr, 0, sizeof(int), h->stream));
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
                as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
-               refine, y, rows, x ? h->nu_fc.ptr : nullptr, h->pivot_list.ptr);
+               refine, y, rows, x ? h->nu_fc.ptr : nullptr, h->pivot_list.ptr,
+               iterative ? h->jac_list.ptr : nullptr);
   launch_lu_fallback<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta),
                         as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
                         as<T>(h->lambda), key, y, rows, h->pivot_list.ptr);
@@ -858,6 +874,10 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
   }
   if ((st = lu_draws<T>(h, h->x_t.ptr, key, ydst))) return st;
   CK(cudaEventRecord(h->ev[2], s));
+  int factored = (int)n;
+  if (std::is_same<T, float>::value && h->forecast_iterative && h->jac.ok &&
+      (st = d2h(h, &factored, h->jac_list.ptr, sizeof(int))))
+    return st;
   if (o_y && ydst == h->y_fc.ptr && (st = d2h(h, o_y, h->y_fc.ptr, n * m * sizeof(double))))
     return st;
   std::vector<T> lam, th;
@@ -881,6 +901,7 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
         for (size_t k = 0; k < P; ++k) o_theta[(i * m + j) * P + k] = (double)th[(j * n + i) * P + k];
   h->stats.ms_sample = elapsed(h->ev[0], h->ev[1]);
   h->stats.ms_lu_forecast = elapsed(h->ev[1], h->ev[2]);
+  h->stats.forecast_draws_factored = (uint64_t)factored;
   h->stats.ms_total = elapsed(h->ev[0], h->ev[2]);
   return collect_flags(h, false);
 }
@@ -1649,6 +1670,12 @@ int sgdlm_set_lu_options(sgdlm_handle h, int allow_tensor_cores, int max_ctas) {
   if (!h->mem_init) return SGDLM_OK;
   cudaStreamSynchronize(h->stream);
   return replan_sim(h);
+}
+
+int sgdlm_set_forecast_solver(sgdlm_handle h, int iterative) {
+  HCHECK(h);
+  h->forecast_iterative = iterative ? 1 : 0;
+  return SGDLM_OK;
 }
 
 int sgdlm_get_lu_options(sgdlm_handle h, int *allow_tensor_cores, int *max_ctas) {

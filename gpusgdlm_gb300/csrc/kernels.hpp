@@ -125,7 +125,23 @@ void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan
                const double *nu_in = nullptr,
                // n + 1 ints, [0] zero on entry: the draws flagged for the pivoted redo
                // are appended ([0] their count, [1..] their indices), or nullptr
-               int *pivot_list = nullptr);
+               int *pivot_list = nullptr,
+               // the same form: only the listed draws are factored, or nullptr: all
+               const int *draw_list = nullptr);
+// Forecast solves of FP32 draws by fixed-point iteration on the sparse Gamma_i
+// (forecast_kernels.cu).  ok = 0: the shared-memory working set of a draw does
+// not fit, every draw keeps the factorising path.
+struct JacobiPlan {
+  int ok, grid, nnz;
+  size_t smem;
+};
+JacobiPlan plan_jacobi(int m, int nnz, int num_sms);
+// y (draw-major) of every draw whose iteration converges (logdet[i] set to NaN:
+// not factored); the others are appended to list (n + 1 ints, [0] zero on entry).
+// theta_dm: the draws' draw-major copy; nu: series-major right-hand sides.
+void launch_forecast_jacobi(cudaStream_t s, const JacobiPlan &jp, int m, int P, long n,
+                            GammaRows rows, const float *theta_dm, const double *nu, double *y,
+                            double *logdet, int *list);
 // The forecast right-hand sides nu_ij = z_ij / sqrt(lambda_ij) + x_j' phi_ij of all
 // draws (series-major, nu[j*n + i]); theta series-major; x32: an FP32 copy of x
 // (used for FP32 draws).  SGDLM.cu:574-590 (batchedComputeNuPlusMu,

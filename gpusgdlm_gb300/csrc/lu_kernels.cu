@@ -1578,7 +1578,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
          double *__restrict__ logdet, int *__restrict__ draw_flags,
          const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
          double *__restrict__ y, GammaRows rows, const double *__restrict__ nu_in,
-         int *__restrict__ pivot_list) {
+         int *__restrict__ pivot_list, const int *__restrict__ draw_list) {
   static_assert(!TC || sizeof(T) == 4, "tensor-core path: FP32 draws");
   using V = Vec<T>;
   constexpr int W = V::W;
@@ -1628,7 +1628,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   }
   const uint32_t tmem = TC ? s_tmem : 0u;
 
-  for (long i = blockIdx.x; i < n; i += gridDim.x) {
+  const long n_todo = draw_list ? min((long)draw_list[0], n) : n;
+  for (long it = blockIdx.x; it < n_todo; it += gridDim.x) {
+    const long i = draw_list ? (long)draw_list[1 + it] : it;
     if (tid == 0) sflag = 0;
     bool bad = false;
     double ld_part = 0.0;  // this thread's share of sum log|pivot| (levels and core)
@@ -2338,7 +2340,7 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
                const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
                double *logdet, int *draw_flags,
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
-               GammaRows rows, const double *nu_in, int *pivot_list) {
+               GammaRows rows, const double *nu_in, int *pivot_list, const int *draw_list) {
   // opt in to exactly the shared memory this plan needs (a failure here shows up
   // as a launch error that the engine reports)
   auto run = [&](auto kernel) {
@@ -2348,7 +2350,7 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
                                               pl.vals_smem, pl.prog_smem, n, ep, sp, theta,
                                               theta_dm, scratch,
                                               logdet, draw_flags, x, lambda, key, refine, y, rows,
-                                              nu_in, pivot_list);
+                                              nu_in, pivot_list, draw_list);
   };
   if constexpr (sizeof(T) == 4) {
     if (pl.tc) {
@@ -2387,12 +2389,12 @@ template void launch_lu<float>(cudaStream_t, const LuPlan &, long, const Elimina
                                const unsigned *, const float *, const float *, float *,
                                double *, int *,
                                const double *, const float *, RngKey, bool, double *, GammaRows,
-                               const double *, int *);
+                               const double *, int *, const int *);
 template void launch_lu<double>(cudaStream_t, const LuPlan &, long, const EliminationPlan &,
                                 const unsigned *, const double *, const double *, double *,
                                 double *, int *,
                                 const double *, const double *, RngKey, bool, double *,
-                                GammaRows, const double *, int *);
+                                GammaRows, const double *, int *, const int *);
 template void launch_forecast_nu<float>(cudaStream_t, int, int, long, GammaRows, const float *,
                                         const double *, const float *, const float *, RngKey,
                                         double *);

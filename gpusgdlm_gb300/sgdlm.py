@@ -497,6 +497,9 @@ class SGDLM:
         self._check(self._lib.sgdlm_set_lu_options(self._h, 1 if allow_tensor_cores else 0,
                                                    int(max_ctas)))
 
+    def setForecastSolver(self, iterative: bool = True):
+        self._check(self._lib.sgdlm_set_forecast_solver(self._h, 1 if iterative else 0))
+
     def getLuOptions(self):
         tc, mx = C.c_int(), C.c_int()
         self._lib.sgdlm_get_lu_options(self._h, C.byref(tc), C.byref(mx))

@@ -75,6 +75,9 @@ typedef struct {
   /* CUDA-event timings of the last call's phases, milliseconds */
   double ms_sample, ms_lu, ms_weights, ms_vb, ms_total;
   double ms_lu_forecast;
+  /* last computeForecast: draws whose solve needed the LU factorisation (the rest
+   * converged in the iterative solve of FP32 draws; all draws in FP64) */
+  uint64_t forecast_draws_factored;
 } sgdlm_stats;
 
 /* ---- lifetime (HostWrapperFactory.cu:5-35, HostWrapperImpl.cu:12-105) ---- */
@@ -254,6 +257,10 @@ int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const float *d_theta
  * max_ctas > 0 caps its persistent grid (more draws per CTA, fewer CTAs: room
  * for other instances on the GPU).  Results equal up to rounding. */
 int sgdlm_set_lu_options(sgdlm_handle h, int allow_tensor_cores, int max_ctas);
+/* Forecast solves of FP32 draws: 1 (default) the fixed-point iteration on the
+ * sparse Gamma_i first (draws that do not converge are factored), 0 every draw
+ * factored.  Results equal to the refinement tolerance. */
+int sgdlm_set_forecast_solver(sgdlm_handle h, int iterative);
 int sgdlm_get_lu_options(sgdlm_handle h, int *allow_tensor_cores, int *max_ctas);
 typedef struct {
   int levels;           /* chosen sparse elimination levels */
