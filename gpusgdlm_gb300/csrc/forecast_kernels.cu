@@ -7,7 +7,7 @@
 // filtering regime the spectral radius of Gamma_i is well below one, so the
 // iteration converges geometrically at O(nnz) per sweep -- a few ten thousand
 // flop per draw at m = 400 instead of 10^8.  A draw is solved here when
-//   (1) the sweeps from y = nu reach max|dy| <= 2^-21 max|y| within kMaxSweeps
+//   (1) the sweeps from y = nu reach max|dy| <= 2^-20 max|y| within kMaxSweeps
 //       (FP32, the draw's Gamma entries and the iterate in shared memory),
 //   (2) the FP64 residual r = nu - (I - Gamma_i) y, solved by the same
 //       iteration, gives a correction d with max|d| <= 1e-3 max|y| (the rule
@@ -24,7 +24,11 @@ namespace {
 
 constexpr int kJacThreads = 256;
 constexpr int kMaxSweeps = 128;
-constexpr float kSweepTol = 4.76837158203125e-07f;  // 2^-21
+// The first solve stops at max|dy| <= 2^-20 max|y|; the correction, whose size
+// is that of y's error, needs only 2^-10 of its own size: y + d is then within
+// about 2^-30 of the solution (FP32 sweeps reach a few ulps, not further).
+constexpr float kSweepTol = 9.5367431640625e-07f;   // 2^-20
+constexpr float kCorrSweepTol = 9.765625e-04f;      // 2^-10
 constexpr double kCorrTol = 1e-3;
 
 struct JacSmem {
@@ -72,6 +76,23 @@ __device__ __forceinline__ void block_max2f(float &a, float &b, float *red) {
   }
 }
 
+// One row of a sweep: c_r + sum_e val[e] x[col[e]] over the row's entries.  The
+// first kUnroll entries are unrolled with predication, so that all their shared
+// loads are independent and in flight together; two accumulators halve the FMA
+// chain.  Rows with more entries finish in a plain loop.
+constexpr int kUnroll = 24;
+__device__ __forceinline__ float sweep_row(float c, int e0, int e1, const unsigned short *col,
+                                           const float *val, const float *x) {
+  float a0 = c, a1 = 0.f;
+#pragma unroll
+  for (int q = 0; q < kUnroll; q += 2) {
+    if (e0 + q < e1) a0 = fmaf(val[e0 + q], x[col[e0 + q]], a0);
+    if (e0 + q + 1 < e1) a1 = fmaf(val[e0 + q + 1], x[col[e0 + q + 1]], a1);
+  }
+  for (int e = e0 + kUnroll; e < e1; ++e) a0 = fmaf(val[e], x[col[e]], a0);
+  return a0 + a1;
+}
+
 // Sweeps x <- c + Gamma x from x = c.  Returns whether they converged
 // (max|dx| <= tol max|x|, everything finite); *out is the last iterate.
 __device__ bool jacobi(int m, const int *rowptr, const unsigned short *col, const float *val,
@@ -82,9 +103,7 @@ __device__ bool jacobi(int m, const int *rowptr, const unsigned short *col, cons
   for (int it = 1; it <= kMaxSweeps; ++it) {
     float dmax = 0.f, xmax = 0.f;
     for (int r = threadIdx.x; r < m; r += blockDim.x) {
-      float v = c[r];
-      const int e1 = rowptr[r + 1];
-      for (int e = rowptr[r]; e < e1; ++e) v = fmaf(val[e], cur[col[e]], v);
+      const float v = sweep_row(c[r], rowptr[r], rowptr[r + 1], col, val, cur);
       nxt[r] = v;
       dmax = fmaxf(dmax, fabsf(v - cur[r]));
       xmax = fmaxf(xmax, fabsf(v));
@@ -151,7 +170,7 @@ __global__ void __launch_bounds__(kJacThreads)
       // the correction's iterates go to `other` and nuf (nu's FP32 copy is no
       // longer needed); yv keeps y
       float *dv = nullptr;
-      ok = jacobi(m, rowptr, col, val, res, other, nuf, red, kSweepTol, &dv);
+      ok = jacobi(m, rowptr, col, val, res, other, nuf, red, kCorrSweepTol, &dv);
       float dmax = 0.f, ymax = 0.f;
       for (int r = tid; r < m; r += blockDim.x) {
         dmax = fmaxf(dmax, fabsf(dv[r]));
