@@ -275,7 +275,9 @@ int upload_gamma_rows(sgdlm_engine *h) {
   CK(h->g_extk.alloc(extk.size()));
   CK(cudaMemcpy(h->g_extptr.ptr, extptr.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->g_extk.ptr, extk.data(), extk.size() * sizeof(int), cudaMemcpyHostToDevice));
-  h->jac = plan_jacobi((int)m, rowptr[m], h->num_sms);
+  int max_row = 0;
+  for (size_t r = 0; r < m; ++r) max_row = std::max(max_row, rowptr[r + 1] - rowptr[r]);
+  h->jac = plan_jacobi((int)m, max_row, h->num_sms);
   return SGDLM_OK;
 }
 

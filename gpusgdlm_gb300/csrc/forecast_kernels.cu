@@ -8,7 +8,8 @@
 // iteration converges geometrically at O(nnz) per sweep -- a few ten thousand
 // flop per draw at m = 400 instead of 10^8.  A draw is solved here when
 //   (1) the sweeps from y = nu reach max|dy| <= 2^-20 max|y| within kMaxSweeps
-//       (FP32, the draw's Gamma entries and the iterate in shared memory),
+//       (FP32; each thread holds its rows' Gamma entries in registers in ELL
+//       form, the iterate is in shared memory),
 //   (2) the FP64 residual r = nu - (I - Gamma_i) y, solved by the same
 //       iteration, gives a correction d with max|d| <= 1e-3 max|y| (the rule
 //       the factorising path applies to its refinement step); y + d is written.
@@ -23,6 +24,7 @@ namespace sgdlm {
 namespace {
 
 constexpr int kJacThreads = 256;
+constexpr int kRowsPerThread = 2;  // m <= 512
 constexpr int kMaxSweeps = 128;
 // The first solve stops at max|dy| <= 2^-20 max|y|; the correction, whose size
 // is that of y's error, needs only 2^-10 of its own size: y + d is then within
@@ -32,8 +34,8 @@ constexpr float kCorrSweepTol = 9.765625e-04f;      // 2^-10
 constexpr double kCorrTol = 1e-3;
 
 struct JacSmem {
-  size_t nud, nuf, ya, yb, res, red, rowptr, col, val, total;
-  __host__ __device__ JacSmem(int m, int nnz) {
+  size_t nud, nuf, ya, yb, res, red, total;
+  __host__ __device__ JacSmem(int m) {
     size_t o = 0;
     auto take = [&](size_t bytes) {
       const size_t at = o;
@@ -46,9 +48,6 @@ struct JacSmem {
     yb = take((size_t)m * sizeof(float));
     res = take((size_t)m * sizeof(float));
     red = take(2 * (kJacThreads / 32) * sizeof(float));
-    rowptr = take((size_t)(m + 1) * sizeof(int));
-    val = take((size_t)nnz * sizeof(float));
-    col = take((size_t)nnz * sizeof(unsigned short));
     total = o;
   }
 };
@@ -76,37 +75,43 @@ __device__ __forceinline__ void block_max2f(float &a, float &b, float *red) {
   }
 }
 
-// One row of a sweep: c_r + sum_e val[e] x[col[e]] over the row's entries.  The
-// first kUnroll entries are unrolled with predication, so that all their shared
-// loads are independent and in flight together; two accumulators halve the FMA
-// chain.  Rows with more entries finish in a plain loop.
-constexpr int kUnroll = 24;
-__device__ __forceinline__ float sweep_row(float c, int e0, int e1, const unsigned short *col,
-                                           const float *val, const float *x) {
-  float a0 = c, a1 = 0.f;
-#pragma unroll
-  for (int q = 0; q < kUnroll; q += 2) {
-    if (e0 + q < e1) a0 = fmaf(val[e0 + q], x[col[e0 + q]], a0);
-    if (e0 + q + 1 < e1) a1 = fmaf(val[e0 + q + 1], x[col[e0 + q + 1]], a1);
+// A thread's rows r = threadIdx.x + 256 rr, in ELL form held in registers: K
+// slots per row (entries beyond the row's length have value 0 and point at the
+// row itself), the column indices packed two to a register.
+template <int K> struct Rows {
+  int r[kRowsPerThread];
+  uint32_t col[kRowsPerThread][K / 2];
+  float val[kRowsPerThread][K];
+  __device__ __forceinline__ int c(int rr, int q) const {
+    return (int)((col[rr][q >> 1] >> (16 * (q & 1))) & 0xFFFFu);
   }
-  for (int e = e0 + kUnroll; e < e1; ++e) a0 = fmaf(val[e], x[col[e]], a0);
-  return a0 + a1;
-}
+};
 
 // Sweeps x <- c + Gamma x from x = c.  Returns whether they converged
 // (max|dx| <= tol max|x|, everything finite); *out is the last iterate.
-__device__ bool jacobi(int m, const int *rowptr, const unsigned short *col, const float *val,
-                       const float *c, float *xa, float *xb, float *red, float tol, float **out) {
+template <int K>
+__device__ bool jacobi(int m, const Rows<K> &R, const float *c, float *xa, float *xb, float *red,
+                       float tol, float **out) {
   for (int r = threadIdx.x; r < m; r += blockDim.x) xa[r] = c[r];
   __syncthreads();
   float *cur = xa, *nxt = xb;
   for (int it = 1; it <= kMaxSweeps; ++it) {
     float dmax = 0.f, xmax = 0.f;
-    for (int r = threadIdx.x; r < m; r += blockDim.x) {
-      const float v = sweep_row(c[r], rowptr[r], rowptr[r + 1], col, val, cur);
-      nxt[r] = v;
-      dmax = fmaxf(dmax, fabsf(v - cur[r]));
-      xmax = fmaxf(xmax, fabsf(v));
+#pragma unroll
+    for (int rr = 0; rr < kRowsPerThread; ++rr) {
+      const int r = R.r[rr];
+      if (r < m) {
+        float a0 = c[r], a1 = 0.f;
+#pragma unroll
+        for (int q = 0; q < K; q += 2) {
+          a0 = fmaf(R.val[rr][q], cur[R.c(rr, q)], a0);
+          a1 = fmaf(R.val[rr][q + 1], cur[R.c(rr, q + 1)], a1);
+        }
+        const float v = a0 + a1;
+        nxt[r] = v;
+        dmax = fmaxf(dmax, fabsf(v - cur[r]));
+        xmax = fmaxf(xmax, fabsf(v));
+      }
     }
     float *t = cur;
     cur = nxt;
@@ -126,29 +131,45 @@ __device__ bool jacobi(int m, const int *rowptr, const unsigned short *col, cons
   return false;
 }
 
+template <int K>
 __global__ void __launch_bounds__(kJacThreads)
-    k_forecast_jacobi(int m, int P, long n, int nnz, GammaRows rows,
-                      const float *__restrict__ theta_dm, const double *__restrict__ nu,
-                      double *__restrict__ y, double *__restrict__ logdet, int *__restrict__ list) {
+    k_forecast_jacobi(int m, int P, long n, GammaRows rows, const float *__restrict__ theta_dm,
+                      const double *__restrict__ nu, double *__restrict__ y,
+                      double *__restrict__ logdet, int *__restrict__ list) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const JacSmem L(m, nnz);
+  const JacSmem L(m);
   double *nud = reinterpret_cast<double *>(smem_raw + L.nud);
   float *nuf = reinterpret_cast<float *>(smem_raw + L.nuf);
   float *ya = reinterpret_cast<float *>(smem_raw + L.ya);
   float *yb = reinterpret_cast<float *>(smem_raw + L.yb);
   float *res = reinterpret_cast<float *>(smem_raw + L.res);
   float *red = reinterpret_cast<float *>(smem_raw + L.red);
-  int *rowptr = reinterpret_cast<int *>(smem_raw + L.rowptr);
-  float *val = reinterpret_cast<float *>(smem_raw + L.val);
-  unsigned short *col = reinterpret_cast<unsigned short *>(smem_raw + L.col);
   const int tid = threadIdx.x;
-  for (int r = tid; r <= m; r += blockDim.x) rowptr[r] = rows.rowptr[r];
-  for (int e = tid; e < nnz; e += blockDim.x) col[e] = (unsigned short)rows.ent[e].y;
+  Rows<K> R;
+  int e0[kRowsPerThread], len[kRowsPerThread];
+#pragma unroll
+  for (int rr = 0; rr < kRowsPerThread; ++rr) {
+    const int r = tid + kJacThreads * rr;
+    R.r[rr] = r;
+    e0[rr] = r < m ? rows.rowptr[r] : 0;
+    len[rr] = r < m ? rows.rowptr[r + 1] - e0[rr] : 0;
+#pragma unroll
+    for (int q = 0; q < K; q += 2) {
+      const uint32_t c0 = q < len[rr] ? (uint32_t)rows.ent[e0[rr] + q].y : (uint32_t)(r < m ? r : 0);
+      const uint32_t c1 =
+          q + 1 < len[rr] ? (uint32_t)rows.ent[e0[rr] + q + 1].y : (uint32_t)(r < m ? r : 0);
+      R.col[rr][q >> 1] = c0 | (c1 << 16);
+    }
+  }
   const size_t row_len = (size_t)m * P;
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
     // this draw's Gamma entries (from its draw-major theta row) and nu
     const float *th = theta_dm + (size_t)i * row_len;
-    for (int e = tid; e < nnz; e += blockDim.x) val[e] = th[__ldg(&rows.ent[e].x)];
+#pragma unroll
+    for (int rr = 0; rr < kRowsPerThread; ++rr)
+#pragma unroll
+      for (int q = 0; q < K; ++q)
+        R.val[rr][q] = q < len[rr] ? th[__ldg(&rows.ent[e0[rr] + q].x)] : 0.f;
     for (int r = tid; r < m; r += blockDim.x) {
       const double v = nu[(size_t)r * n + i];
       nud[r] = v;
@@ -156,21 +177,25 @@ __global__ void __launch_bounds__(kJacThreads)
     }
     __syncthreads();
     float *yv = nullptr;
-    bool ok = jacobi(m, rowptr, col, val, nuf, ya, yb, red, kSweepTol, &yv);
+    bool ok = jacobi<K>(m, R, nuf, ya, yb, red, kSweepTol, &yv);
     if (ok) {
       // residual in FP64 and its correction by the same iteration
       float *other = (yv == ya) ? yb : ya;
-      for (int r = tid; r < m; r += blockDim.x) {
-        double v = nud[r] - (double)yv[r];
-        const int e1 = rowptr[r + 1];
-        for (int e = rowptr[r]; e < e1; ++e) v += (double)val[e] * (double)yv[col[e]];
-        res[r] = (float)v;
+#pragma unroll
+      for (int rr = 0; rr < kRowsPerThread; ++rr) {
+        const int r = R.r[rr];
+        if (r < m) {
+          double v = nud[r] - (double)yv[r];
+#pragma unroll
+          for (int q = 0; q < K; ++q) v += (double)R.val[rr][q] * (double)yv[R.c(rr, q)];
+          res[r] = (float)v;
+        }
       }
       __syncthreads();
       // the correction's iterates go to `other` and nuf (nu's FP32 copy is no
       // longer needed); yv keeps y
       float *dv = nullptr;
-      ok = jacobi(m, rowptr, col, val, res, other, nuf, red, kCorrSweepTol, &dv);
+      ok = jacobi<K>(m, R, res, other, nuf, red, kCorrSweepTol, &dv);
       float dmax = 0.f, ymax = 0.f;
       for (int r = tid; r < m; r += blockDim.x) {
         dmax = fmaxf(dmax, fabsf(dv[r]));
@@ -194,23 +219,27 @@ __global__ void __launch_bounds__(kJacThreads)
   }
 }
 
+template <int K> void *jacobi_kernel() { return reinterpret_cast<void *>(k_forecast_jacobi<K>); }
+
 }  // namespace
 
-JacobiPlan plan_jacobi(int m, int nnz, int num_sms) {
+JacobiPlan plan_jacobi(int m, int max_row, int num_sms) {
   JacobiPlan jp{};
-  if (m < 1 || m > 65535) return jp;
-  jp.smem = JacSmem(m, nnz).total;
-  if (jp.smem > 100 * 1024) return jp;  // the draws keep the factorising path
+  if (m < 1 || m > kJacThreads * kRowsPerThread || max_row > 32) return jp;
+  jp.nnz = max_row <= 8 ? 8 : (max_row <= 16 ? 16 : (max_row <= 24 ? 24 : 32));  // ELL slots
+  jp.smem = JacSmem(m).total;
+  const void *kern = jp.nnz == 8 ? jacobi_kernel<8>()
+                     : jp.nnz == 16 ? jacobi_kernel<16>()
+                     : jp.nnz == 24 ? jacobi_kernel<24>()
+                                    : jacobi_kernel<32>();
   int per_sm = 0;
-  cudaFuncSetAttribute(k_forecast_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jp.smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forecast_jacobi, kJacThreads,
-                                                    jp.smem) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kJacThreads, jp.smem) !=
+          cudaSuccess ||
       per_sm < 1) {
     (void)cudaGetLastError();
     return jp;
   }
   jp.grid = num_sms * per_sm;
-  jp.nnz = nnz;
   jp.ok = 1;
   return jp;
 }
@@ -218,9 +247,21 @@ JacobiPlan plan_jacobi(int m, int nnz, int num_sms) {
 void launch_forecast_jacobi(cudaStream_t s, const JacobiPlan &jp, int m, int P, long n,
                             GammaRows rows, const float *theta_dm, const double *nu, double *y,
                             double *logdet, int *list) {
-  const long grid = std::min<long>(jp.grid, n);
-  k_forecast_jacobi<<<(unsigned)std::max<long>(grid, 1), kJacThreads, jp.smem, s>>>(
-      m, P, n, jp.nnz, rows, theta_dm, nu, y, logdet, list);
+  const unsigned grid = (unsigned)std::max<long>(std::min<long>(jp.grid, n), 1);
+  switch (jp.nnz) {
+    case 8:
+      k_forecast_jacobi<8><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
+      break;
+    case 16:
+      k_forecast_jacobi<16><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
+      break;
+    case 24:
+      k_forecast_jacobi<24><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
+      break;
+    default:
+      k_forecast_jacobi<32><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
+      break;
+  }
 }
 
 }  // namespace sgdlm

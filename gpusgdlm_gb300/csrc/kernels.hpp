@@ -132,10 +132,11 @@ void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan
 // (forecast_kernels.cu).  ok = 0: the shared-memory working set of a draw does
 // not fit, every draw keeps the factorising path.
 struct JacobiPlan {
-  int ok, grid, nnz;
+  int ok, grid, nnz;  // nnz: ELL slots per row (8, 16, 24 or 32)
   size_t smem;
 };
-JacobiPlan plan_jacobi(int m, int nnz, int num_sms);
+// m <= 512 and at most 32 simultaneous parents per series, else ok = 0.
+JacobiPlan plan_jacobi(int m, int max_row, int num_sms);
 // y (draw-major) of every draw whose iteration converges (logdet[i] set to NaN:
 // not factored); the others are appended to list (n + 1 ints, [0] zero on entry).
 // theta_dm: the draws' draw-major copy; nu: series-major right-hand sides.
