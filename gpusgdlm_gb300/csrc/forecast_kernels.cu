@@ -109,8 +109,11 @@ __device__ bool jacobi(int m, const Rows<K> &R, const float *c, float *xa, float
         }
         const float v = a0 + a1;
         nxt[r] = v;
-        dmax = fmaxf(dmax, fabsf(v - cur[r]));
-        xmax = fmaxf(xmax, fabsf(v));
+        // fmaxf drops NaN operands: a NaN (an overflowed iterate times a padded
+        // zero slot) must count as divergence, so it becomes infinity here
+        const float av = fabsf(v), dv = fabsf(v - cur[r]);
+        xmax = (av == av) ? fmaxf(xmax, av) : INFINITY;
+        dmax = (dv == dv) ? fmaxf(dmax, dv) : INFINITY;
       }
     }
     float *t = cur;
@@ -198,11 +201,12 @@ __global__ void __launch_bounds__(kJacThreads)
       ok = jacobi<K>(m, R, res, other, nuf, red, kCorrSweepTol, &dv);
       float dmax = 0.f, ymax = 0.f;
       for (int r = tid; r < m; r += blockDim.x) {
-        dmax = fmaxf(dmax, fabsf(dv[r]));
-        ymax = fmaxf(ymax, fabsf(yv[r]));
+        const float ad = fabsf(dv[r]), ay = fabsf(yv[r]);
+        dmax = (ad == ad) ? fmaxf(dmax, ad) : INFINITY;
+        ymax = (ay == ay) ? fmaxf(ymax, ay) : INFINITY;
       }
       block_max2f(dmax, ymax, red);
-      ok = ok && ymax < INFINITY && (double)dmax <= kCorrTol * (double)ymax;
+      ok = ok && ymax < INFINITY && dmax < INFINITY && (double)dmax <= kCorrTol * (double)ymax;
       if (ok)
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)yv[r] + (double)dv[r];
