@@ -108,7 +108,9 @@ class LuTuning(C.Structure):
 class BatchTuning(C.Structure):
     _fields_ = [
         ("buckets", C.c_int),
+        ("lu_plans_kept", C.c_int),
         ("concurrency", C.c_int),
+        ("ms_untuned", C.c_double),
         ("ms_per_step", C.c_double),
         ("ms_candidates", C.c_double * 4),
     ]

@@ -1949,15 +1949,71 @@ int sgdlm_batch_step(sgdlm_batch_handle b) {
   return batch_launch(b);
 }
 
+}  // extern "C"
+
+namespace {
+
+// Time of one recorded batch step (mean over `replays` replays after one
+// warm-up), with the engines' states restored afterwards.
+int batch_time(sgdlm_batch *b, int replays, const BatchSnapshot &snap, double *ms_out) {
+  int st = batch_capture(b);
+  if (!st) st = batch_launch(b);  // warm-up
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  if (!st) {
+    cudaEventRecord(e0, b->origin);
+    for (int r = 0; r < replays && !st; ++r) st = batch_launch(b);
+    cudaEventRecord(e1, b->origin);
+    cudaEventSynchronize(e1);
+  }
+  for (auto *h : b->eng) cudaStreamSynchronize(h->stream);
+  float ms = 0.f;
+  if (!st) cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  *ms_out = ms / replays;
+  return batch_restore(b, snap);
+}
+
+int set_plans(sgdlm_batch *b, const std::vector<int> &levels, const std::vector<int> &tc, int c) {
+  for (size_t i = 0; i < b->eng.size(); ++i) {
+    sgdlm_engine *h = b->eng[i];
+    h->lu_opt.allow_tc = tc[i];
+    int st = sgdlm_set_elimination_levels(h, levels[i]);
+    if (!st) st = sgdlm_set_lu_options(h, tc[i], c == 1 ? 0 : 2 * h->num_sms / c);
+    if (st) return st;
+  }
+  return SGDLM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int sgdlm_batch_autotune(sgdlm_batch_handle b, int replays, sgdlm_batch_tuning *out) {
   if (!b || !out || replays < 1) return SGDLM_ERR_BAD_ARG;
   if (!b->recorded) return SGDLM_ERR_WRONG_STATE;
   cudaSetDevice(b->eng[0]->device);
   *out = sgdlm_batch_tuning{};
   for (auto *h : b->eng) cudaStreamSynchronize(h->stream);
+  const size_t k = b->eng.size();
+  BatchSnapshot snap;
+  int st = batch_save(b, snap);
+  if (st) return st;
+  std::vector<int> lev0(k), tc0(k), lev1(k), tc1(k);
+  for (size_t i = 0; i < k; ++i) {
+    lev0[i] = b->eng[i]->elim_levels;
+    tc0[i] = b->eng[i]->lu_opt.allow_tc;
+  }
+  double base = 0.0;
+  if ((st = set_plans(b, lev0, tc0, 1)) || (st = batch_time(b, replays, snap, &base))) return st;
   // (1) per m bucket (m rounded up to 32): tune the LU on one engine, apply to the rest
   std::vector<int> bucket_done;
-  for (size_t i = 0; i < b->eng.size(); ++i) {
+  lev1 = lev0;
+  tc1 = tc0;
+  for (size_t i = 0; i < k; ++i) {
     sgdlm_engine *h = b->eng[i];
     const int bucket = (int)((h->m + 31) / 32);
     bool seen = false;
@@ -1965,58 +2021,40 @@ int sgdlm_batch_autotune(sgdlm_batch_handle b, int replays, sgdlm_batch_tuning *
     if (seen) continue;
     bucket_done.push_back(bucket);
     sgdlm_lu_tuning t{};
-    int st = sgdlm_tune_lu(h, &t);
-    if (st) return st;
-    for (size_t j = 0; j < b->eng.size(); ++j) {
-      sgdlm_engine *g = b->eng[j];
-      if (j == i || (int)((g->m + 31) / 32) != bucket) continue;
-      g->lu_opt.allow_tc = h->lu_opt.allow_tc;
-      if ((st = sgdlm_set_elimination_levels(g, h->elim_levels))) return st;
-    }
+    if ((st = sgdlm_tune_lu(h, &t))) return st;
+    for (size_t j = 0; j < k; ++j)
+      if ((int)((b->eng[j]->m + 31) / 32) == bucket) {
+        lev1[j] = h->elim_levels;
+        tc1[j] = h->lu_opt.allow_tc;
+      }
   }
   out->buckets = (int)bucket_done.size();
-  // (2) concurrency: each engine's LU grid capped at 2 x SMs / c, timed on the graph
-  BatchSnapshot snap;
-  int st = batch_save(b, snap);
-  if (st) return st;
+  if ((st = batch_restore(b, snap))) return st;  // the LU tuner drew with the current state
+  // keep the tuned plans only if the whole batch step is faster with them
+  double tuned = 0.0;
+  if ((st = set_plans(b, lev1, tc1, 1)) || (st = batch_time(b, replays, snap, &tuned))) return st;
+  const bool keep = tuned < base;
+  const std::vector<int> &lev = keep ? lev1 : lev0, &tc = keep ? tc1 : tc0;
+  // (2) concurrency: each engine's LU grid capped at 2 x SMs / c
   const int cs[4] = {1, 2, 4, 8};
-  double best = 1e300;
+  double best = keep ? tuned : base;
   int best_c = 1;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  for (int ci = 0; ci < 4; ++ci) {
-    for (auto *h : b->eng)
-      if ((st = sgdlm_set_lu_options(h, h->lu_opt.allow_tc, cs[ci] == 1 ? 0 : 2 * h->num_sms / cs[ci])))
-        break;
-    if (!st) st = batch_capture(b);
-    if (!st) st = batch_launch(b);  // warm-up
-    if (!st) {
-      cudaEventRecord(e0, b->origin);
-      for (int r = 0; r < replays && !st; ++r) st = batch_launch(b);
-      cudaEventRecord(e1, b->origin);
-      cudaEventSynchronize(e1);
-    }
-    for (auto *h : b->eng) cudaStreamSynchronize(h->stream);
-    if (st) break;
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    out->ms_candidates[ci] = ms / replays;
-    if (ms / replays < best) {
-      best = ms / replays;
+  out->ms_candidates[0] = best;
+  for (int ci = 1; ci < 4; ++ci) {
+    double ms = 0.0;
+    if ((st = set_plans(b, lev, tc, cs[ci])) || (st = batch_time(b, replays, snap, &ms))) return st;
+    out->ms_candidates[ci] = ms;
+    if (ms < best) {
+      best = ms;
       best_c = cs[ci];
     }
-    if ((st = batch_restore(b, snap))) break;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (st) return st;
-  for (auto *h : b->eng)
-    if ((st = sgdlm_set_lu_options(h, h->lu_opt.allow_tc, best_c == 1 ? 0 : 2 * h->num_sms / best_c)))
-      return st;
+  if ((st = set_plans(b, lev, tc, best_c))) return st;
   if ((st = batch_restore(b, snap))) return st;
   out->concurrency = best_c;
   out->ms_per_step = best;
+  out->lu_plans_kept = keep ? 1 : 0;
+  out->ms_untuned = base;
   return batch_capture(b);
 }
 

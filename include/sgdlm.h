@@ -295,14 +295,18 @@ int sgdlm_batch_record(sgdlm_batch_handle b, const double *const *d_y, const dou
 int sgdlm_batch_step(sgdlm_batch_handle b);
 typedef struct {
   int buckets;                 /* m buckets (m rounded up to 32) tuned */
+  int lu_plans_kept;           /* 1: the per-bucket LU plans made the step faster and are kept */
   int concurrency;             /* chosen c: each engine's LU grid capped at (2 x SMs) / c */
-  double ms_per_step;          /* batch step time with the chosen c */
+  double ms_untuned;           /* batch step time before tuning */
+  double ms_per_step;          /* batch step time with the chosen plans and c */
   double ms_candidates[4];     /* c = 1, 2, 4, 8 */
 } sgdlm_batch_tuning;
 /* Autotuner: per m bucket, sgdlm_tune_lu on one engine and its choice applied
- * to the bucket; then the concurrency c by timing `replays` recorded steps per
- * candidate (the engines' parameters and RNG states are restored afterwards)
- * and re-records with the best.  Needs a recording. */
+ * to the bucket, kept only if the whole batch step gets faster; then the
+ * concurrency c.  Every candidate is timed over `replays` recorded steps (the
+ * engines' parameters and RNG states are restored after each), so the tuned
+ * step is never slower than the untuned one as measured.  Re-records with the
+ * choice.  Needs a recording. */
 int sgdlm_batch_autotune(sgdlm_batch_handle b, int replays, sgdlm_batch_tuning *out);
 
 /* The handle's CUDA stream (cudaStream_t), for events and graph capture. */
