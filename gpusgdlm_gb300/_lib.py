@@ -51,6 +51,7 @@ class Stats(C.Structure):
         ("ms_total", C.c_double),
         ("ms_lu_forecast", C.c_double),
         ("forecast_draws_factored", C.c_uint64),
+        ("draws_pivoted_full", C.c_uint64),
     ]
 
     def as_dict(self):
@@ -188,6 +189,8 @@ SIGNATURES = {
     "sgdlm_set_lu_options": [_H, _i, _i],
     "sgdlm_get_lu_options": [_H, _Pi, _Pi],
     "sgdlm_set_forecast_solver": [_H, _i],
+    "sgdlm_set_warp_lu": [_H, _i],
+    "sgdlm_get_warp_lu": [_H, C.POINTER(_i), C.POINTER(_i)],
     "sgdlm_tune_lu": [_H, C.POINTER(LuTuning)],
     "sgdlm_batch_create": [C.POINTER(_H), _sz, C.POINTER(C.c_void_p)],
     "sgdlm_batch_destroy": [C.c_void_p],

@@ -32,6 +32,7 @@ SOURCES = [
     "mlp_kernels.cu",
     "proposal_kernels.cu",
     "forecast_kernels.cu",
+    "warp_lu.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]

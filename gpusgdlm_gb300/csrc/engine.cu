@@ -552,6 +552,14 @@ void sample_draws(sgdlm_engine *h, const double *m_t, const double *C_t, const d
   h->launches += 2;
 }
 
+// Small systems: one warp per draw, partial pivoting, no redo.
+bool warp_lu(const sgdlm_engine *h) { return h->m <= (size_t)kWarpLuMaxM && h->lu_opt.allow_warp; }
+
+// Forecasts of FP32 draws are solved iteratively first (block LU path only).
+template <typename T> bool iterative_forecast(const sgdlm_engine *h) {
+  return std::is_same<T, float>::value && h->forecast_iterative && h->jac.ok && !warp_lu(h);
+}
+
 template <typename T>
 int lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   const long n = (long)h->nsim;
@@ -564,9 +572,16 @@ int lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
                           h->x32.ptr, as<T>(h->lambda), key, h->nu_fc.ptr);
     h->launches += 2;
   }
+  if (warp_lu(h)) {
+    launch_lu_warp<T>(h->stream, (int)h->m, (int)h->P, n, h->num_sms, h->sp.ptr, as<T>(h->theta),
+                      as<T>(h->theta_dm), h->logdet.ptr, h->draw_flags.ptr,
+                      x ? h->nu_fc.ptr : nullptr, x ? y : nullptr);
+    h->launches += 1;
+    return SGDLM_OK;
+  }
   // forecasts of FP32 draws: the iterative solve first; the LU kernels then
   // factor only the draws it leaves in jac_list
-  const bool iterative = x && std::is_same<T, float>::value && h->forecast_iterative && h->jac.ok;
+  const bool iterative = iterative_forecast<T>(h) && x;
   if (iterative) {
     CK(cudaMemsetAsync(h->jac_list.ptr, 0, sizeof(int), h->stream));
     launch_forecast_jacobi(h->stream, h->jac, (int)h->m, (int)h->P, n, rows,
@@ -580,7 +595,7 @@ int lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
                as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
                refine, y, rows, x ? h->nu_fc.ptr : nullptr, h->pivot_list.ptr,
                iterative ? h->jac_list.ptr : nullptr);
-  launch_lu_fallback<T>(h->stream, h->plan, n, h->sp.ptr, as<T>(h->theta),
+  launch_lu_fallback<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
                         as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
                         as<T>(h->lambda), key, y, rows, h->pivot_list.ptr);
   h->launches += 2;
@@ -759,14 +774,16 @@ int collect_flags(sgdlm_engine *h, bool with_series) {
                        cudaMemcpyDeviceToHost, h->stream));
   }
   CK(cudaStreamSynchronize(h->stream));
-  uint64_t piv = 0, sing = 0, cap = 0, newton = 0;
+  uint64_t piv = 0, piv_full = 0, sing = 0, cap = 0, newton = 0;
   for (int v : f) {
     piv += (v & DRAW_FLAG_REDONE) ? 1 : 0;
+    piv_full += (v & DRAW_FLAG_FULL_PIVOT) ? 1 : 0;
     sing += (v & DRAW_FLAG_SINGULAR) ? 1 : 0;
     cap += (v & DRAW_FLAG_GAMMA_CAP) ? 1 : 0;
   }
   for (int v : sf) newton += (v & 2) ? 1 : 0;
   h->stats.draws_pivoted = piv;
+  h->stats.draws_pivoted_full = piv_full;
   h->stats.draws_singular = sing;
   h->stats.gamma_cap_hits = cap;
   if (with_series) h->stats.newton_fallbacks = newton;
@@ -877,8 +894,7 @@ int forecast(sgdlm_engine *h, double *o_y, const double *x, double *o_lambda, do
   if ((st = lu_draws<T>(h, h->x_t.ptr, key, ydst))) return st;
   CK(cudaEventRecord(h->ev[2], s));
   int factored = (int)n;
-  if (std::is_same<T, float>::value && h->forecast_iterative && h->jac.ok &&
-      (st = d2h(h, &factored, h->jac_list.ptr, sizeof(int))))
+  if (iterative_forecast<T>(h) && (st = d2h(h, &factored, h->jac_list.ptr, sizeof(int))))
     return st;
   if (o_y && ydst == h->y_fc.ptr && (st = d2h(h, o_y, h->y_fc.ptr, n * m * sizeof(double))))
     return st;
@@ -1672,6 +1688,18 @@ int sgdlm_set_lu_options(sgdlm_handle h, int allow_tensor_cores, int max_ctas) {
   if (!h->mem_init) return SGDLM_OK;
   cudaStreamSynchronize(h->stream);
   return replan_sim(h);
+}
+
+int sgdlm_set_warp_lu(sgdlm_handle h, int enable) {
+  HCHECK(h);
+  h->lu_opt.allow_warp = enable ? 1 : 0;
+  return SGDLM_OK;
+}
+int sgdlm_get_warp_lu(sgdlm_handle h, int *enabled, int *in_use) {
+  HCHECK(h);
+  if (enabled) *enabled = h->lu_opt.allow_warp;
+  if (in_use) *in_use = warp_lu(h) ? 1 : 0;
+  return SGDLM_OK;
 }
 
 int sgdlm_set_forecast_solver(sgdlm_handle h, int iterative) {

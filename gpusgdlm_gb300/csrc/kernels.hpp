@@ -27,6 +27,7 @@ enum : int {
   DRAW_FLAG_PIVOT = 2,          // no-pivot LU multiplier above threshold -> pivoted redo
   DRAW_FLAG_SINGULAR = 4,       // zero / non-finite pivot: weight 0, forecast NaN
   DRAW_FLAG_REDONE = 8,         // draw was refactored by the pivoting fallback
+  DRAW_FLAG_FULL_PIVOT = 16,    // ... over the full matrix (its sparse levels failed)
 };
 
 // Philox key and epoch of one sampling call.  When dev_epoch is set (fused,
@@ -86,6 +87,7 @@ struct LuPlan {
   int prog_smem;       // the solve phase stages the level programs in shared memory
   int tc;              // trailing updates on the tensor cores (tcgen05)
   size_t scratch_elems_per_cta;  // dense core + per-draw values of the sparse levels
+  size_t fb_elems_per_cta;       // the redo's: the above, or a full m_p x m_p slab
   size_t scratch_elems_total;    // covers both passes
 };
 // Tuning knobs of the fast pass: allow_tc = 0 keeps the FFMA instantiation where
@@ -94,7 +96,16 @@ struct LuPlan {
 struct LuOptions {
   int allow_tc = 1;
   int max_grid = 0;
+  int allow_warp = 1;  // m <= kWarpLuMaxM: one warp per draw (launch_lu_warp)
 };
+constexpr int kWarpLuMaxM = 32;
+// Warp-per-draw LU with partial pivoting for m <= kWarpLuMaxM: log|det| of every
+// draw and, when y != nullptr, the forecast solve y_i = (I - Gamma_i)^-1 nu_i
+// (nu series-major, nu[r*n + i]; y draw-major, y[i*m + r]).
+template <typename T>
+void launch_lu_warp(cudaStream_t s, int m, int P, long n, int num_sms, const unsigned *sp,
+                    const T *theta, const T *theta_dm, double *logdet, int *draw_flags,
+                    const double *nu, double *y);
 // core_n / nv / n_solve / prog_len come from the elimination plan (core_n = m and
 // the others 0 without one).
 template <typename T>
@@ -152,7 +163,7 @@ void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, co
                         const double *x, const float *x32, const T *lambda, RngKey key,
                         double *nu);
 template <typename T>
-void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n,
+void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan &ep,
                         const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
                         double *logdet, int *draw_flags, const double *x,
                         const T *lambda, RngKey key, double *y, GammaRows rows,

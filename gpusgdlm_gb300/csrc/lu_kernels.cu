@@ -29,8 +29,9 @@
 //     filtering regime.  Every multiplier (the levels', the diagonal blocks'
 //     and C D^-1) is checked against kPivotThreshold; a draw with a larger one,
 //     or a zero / non-finite pivot, is appended to the redo list and redone by
-//     k_lu_fallback with partial pivoting on the full matrix (getrf
-//     semantics).  |det| does not depend on the elimination order.
+//     k_lu_fallback: the sparse levels again, then partial pivoting on the
+//     dense core (getrf semantics); a draw whose level pivots fail is pivoted
+//     over the full matrix.  |det| does not depend on the elimination order.
 //  3. Forecasts: the right-hand sides (k_forecast_nu, all draws beforehand) go
 //     through the levels' forward program and ride along the block
 //     elimination (b2 -= C D^-1 b1); the back solve x1 = D^-1 (b1 - B x2) runs
@@ -162,17 +163,21 @@ struct Smem {
 };
 
 // Shared memory of the pivoting redo: the 32-column panel (column-major, stride
-// mp), one 128-column chunk of the row panel U12, the right-hand side and
-// correction, the row permutation, one diagonal block and the FP64 forecast
-// vectors.
+// of the factored matrix's order, at most mp), one 128-column chunk of the row
+// panel U12, the right-hand side and correction, the row permutation, one
+// diagonal block, the FP64 forecast vectors and the node-indexed vectors of the
+// levels' solve programs.
 constexpr int kFbChunk = 128;
 constexpr int kFbRefine = 3;  // refinement steps of the pivoting pass's forecast solves
+// the redo eliminates the sparse levels unpivoted unless a multiplier exceeds this
+// (then it pivots over the full matrix)
+constexpr double kLevelMultMax = 65536.0;
 // the fast pass's forecast of a draw is kept when its refinement correction is at
 // most this fraction of the solution (the error left is about its square)
 constexpr double kRefineTol = 1e-3;
 struct FallbackSmem {
   size_t off_pan, off_U, off_piv, off_pivabs, off_cand, off_D, off_z, off_d, off_perm, off_nu,
-      off_res, off_red, total;
+      off_res, off_red, off_zf, off_yf, off_yd, total;
   __host__ __device__ FallbackSmem(int mp, int m, size_t tsz) {
     size_t o = 0;
     auto take = [&](size_t bytes) {
@@ -192,6 +197,9 @@ struct FallbackSmem {
     off_nu = take((size_t)m * sizeof(double));
     off_res = take((size_t)m * sizeof(double));
     off_red = take(64 * sizeof(double));
+    off_zf = take((size_t)m * tsz);
+    off_yf = take((size_t)m * tsz);
+    off_yd = take((size_t)m * tsz);
     total = o;
   }
 };
@@ -2051,225 +2059,355 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   }
 }
 
-// Partial-pivoting LU of the full matrix for the draws the fast pass flagged
-// (getrf semantics: at each column the row with the largest |entry| becomes the
-// pivot row).  Blocked right-looking LU with 32-column panels:
+// Pivoting redo of the draws the fast pass flagged.  The sparse levels' pivots
+// are diagonal entries of (I - Gamma) as updated by earlier levels, eliminated
+// without pivoting as in the fast pass (their multipliers only feed the
+// products of the next levels); the redo pivots where the fast pass's checks
+// look: in the dense core, by partial pivoting (getrf semantics on the core:
+// at each column the row with the largest |entry| becomes the pivot row).  A
+// draw whose level pivots are zero or non-finite, or whose level multipliers
+// exceed kLevelMultMax, is factored instead with partial pivoting on the full
+// m_p x m_p matrix.  log|det| = sum over the levels' pivots + the core's (the
+// levels are a symmetric permutation plus exact block elimination).
+//
+// Both factorisations are the blocked right-looking LU of pivot_lu (32-column
+// panels):
 //  (a) the panel (rows k0.., columns k0..k0+31) is factored with partial pivoting
 //      in shared memory, three barriers per column (pivot search, row swap,
-//      elimination);
+//      update);
 //  (b) the panel's row swaps are applied to the other columns and the right-hand
 //      side, and the factors are written back;
 //  (c) U12 = L11^-1 A12 by forward substitution, one column per thread, in
 //      128-column chunks, each followed by the register-tiled trailing update
 //      A22 -= L21 U12 of those columns.
+template <typename T> struct FbBufs {
+  T *pan, *Uc, *pivabs, *cand_v, *z;
+  int *piv, *cand_i, *perm;
+  bool *singular;
+};
+
+// LU with partial pivoting of the N x N column-major matrix A (N a multiple of
+// 32) in place; perm records the row permutation and, when `rhs`, z (length N)
+// is permuted alongside.  pivabs[0..N) receives |u_jj|.  Returns true (uniform
+// over the block) when a pivot column is zero or non-finite.
+template <typename T>
+__device__ bool pivot_lu(T *__restrict__ A, int N, bool rhs, const FbBufs<T> &b) {
+  using V = Vec<T>;
+  constexpr int W = V::W;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = blockDim.x >> 5;
+  for (int r = tid; r < N; r += blockDim.x) b.perm[r] = r;
+  if (tid == 0) *b.singular = false;
+  __syncthreads();
+  for (int k0 = 0; k0 < N && !*b.singular; k0 += kB) {
+    const int Rp = N - k0, r0 = k0 + kB, R = N - r0;
+    // (a) panel -> shared memory, factored with partial pivoting
+    for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
+      const int c = u / (Rp / W), rw = u - c * (Rp / W);
+      T v[W];
+      V::ld(A + (size_t)(k0 + rw * W) + (size_t)N * (k0 + c), v);
+      V::st(b.pan + c * N + rw * W, v);
+    }
+    __syncthreads();
+    for (int j = 0; j < kB; ++j) {
+      // pivot search in the working precision (ties -> lowest row)
+      T best = T(-1);
+      int bidx = j;
+      for (int r = j + tid; r < Rp; r += blockDim.x) {
+        const T v = dabs(b.pan[j * N + r]);
+        if (v > best) {
+          best = v;
+          bidx = r;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const T ov = __shfl_xor_sync(kFull, best, o);
+        const int oi = __shfl_xor_sync(kFull, bidx, o);
+        if (ov > best || (ov == best && oi < bidx)) {
+          best = ov;
+          bidx = oi;
+        }
+      }
+      if (lane == 0) {
+        b.cand_v[warp] = best;
+        b.cand_i[warp] = bidx;
+      }
+      __syncthreads();
+      T bv = b.cand_v[0];
+      int p = b.cand_i[0];
+      for (int w = 1; w < nwarps; ++w)
+        if (b.cand_v[w] > bv || (b.cand_v[w] == bv && b.cand_i[w] < p)) {
+          bv = b.cand_v[w];
+          p = b.cand_i[w];
+        }
+      if (!(bv > T(0)) || !(bv <= (T)3.0e38)) {
+        if (tid == 0) *b.singular = true;
+        break;  // uniform: every thread computed the same bv
+      }
+      if (p != j && tid < kB) {
+        const T t0 = b.pan[tid * N + j];
+        b.pan[tid * N + j] = b.pan[tid * N + p];
+        b.pan[tid * N + p] = t0;
+      }
+      if (tid == 0) b.piv[j] = p;
+      __syncthreads();
+      const T pv = b.pan[j * N + j];
+      if (tid == 0) b.pivabs[k0 + j] = dabs(pv);
+      for (int r = j + 1 + tid; r < Rp; r += blockDim.x) {
+        const T l = b.pan[j * N + r] / pv;
+        b.pan[j * N + r] = l;
+        for (int c = j + 1; c < kB; ++c) b.pan[c * N + r] -= l * b.pan[c * N + j];
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (*b.singular) break;
+    // (b) factors back to global; the block's swaps on the other columns, the
+    // permutation and the right-hand side
+    for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
+      const int c = u / (Rp / W), rw = u - c * (Rp / W);
+      T v[W];
+      V::ld(b.pan + c * N + rw * W, v);
+      V::st(A + (size_t)(k0 + rw * W) + (size_t)N * (k0 + c), v);
+    }
+    for (int c = tid; c < N - kB; c += blockDim.x) {
+      const int col = c < k0 ? c : c + kB;
+      T *cp = A + (size_t)N * col;
+      for (int j = 0; j < kB; ++j) {
+        const int p = b.piv[j];
+        if (p != j) {
+          const T t0 = cp[k0 + j];
+          cp[k0 + j] = cp[k0 + p];
+          cp[k0 + p] = t0;
+        }
+      }
+    }
+    if (tid == 0) {
+      for (int j = 0; j < kB; ++j) {
+        const int p = b.piv[j];
+        if (p != j) {
+          const int tp = b.perm[k0 + j];
+          b.perm[k0 + j] = b.perm[k0 + p];
+          b.perm[k0 + p] = tp;
+          if (rhs) {
+            const T tz = b.z[k0 + j];
+            b.z[k0 + j] = b.z[k0 + p];
+            b.z[k0 + p] = tz;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // (c) U12 chunk by chunk, each followed by its trailing update
+    for (int c_off = 0; c_off < R; c_off += kFbChunk) {
+      const int C = min(kFbChunk, R - c_off);
+      for (int t = tid; t < C; t += blockDim.x) {
+        T *cp = A + (size_t)k0 + (size_t)N * (r0 + c_off + t);
+        T xv[kB];
+#pragma unroll
+        for (int q = 0; q < kB; q += W) V::ld(cp + q, xv + q);
+#pragma unroll
+        for (int q = 1; q < kB; ++q) {
+          T acc = xv[q];
+#pragma unroll
+          for (int qq = 0; qq < q; ++qq) acc -= b.pan[qq * N + q] * xv[qq];
+          xv[q] = acc;
+        }
+#pragma unroll
+        for (int q = 0; q < kB; q += W) {
+          V::st(cp + q, xv + q);
+          V::st(b.Uc + t * kUs + q, xv + q);
+        }
+      }
+      __syncthreads();
+      if (R > 0) trailing_update<T>(A, N, r0, R, c_off, C, b.pan + kB, b.Uc, N);
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  return *b.singular;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_lu_fallback(int m, int P, int mp, long n, const unsigned *__restrict__ sp,
+    k_lu_fallback(int m, int P, int mp, int dp, size_t per_cta, long n, EliminationPlan ep,
+                  const unsigned *__restrict__ sp,
                   const T *__restrict__ theta_sm, const T *__restrict__ theta_dm,
                   T *__restrict__ scratch,
                   double *__restrict__ logdet, int *__restrict__ draw_flags,
                   const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
                   double *__restrict__ y, GammaRows rows, const int *__restrict__ pivot_list) {
-  using V = Vec<T>;
-  constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Theta<T> theta{theta_sm, theta_dm, m, P, n};
   const FallbackSmem L(mp, m, sizeof(T));
-  T *pan = reinterpret_cast<T *>(smem_raw + L.off_pan);            // pan[c * mp + r]
-  T *Uc = reinterpret_cast<T *>(smem_raw + L.off_U);               // U12 chunk [t][kUs]
-  int *piv = reinterpret_cast<int *>(smem_raw + L.off_piv);        // block's pivot rows
-  T *pivabs = reinterpret_cast<T *>(smem_raw + L.off_pivabs);      // |u_jj|, all columns
-  T *cand_v = reinterpret_cast<T *>(smem_raw + L.off_cand);        // per-warp pivot candidates
-  int *cand_i = reinterpret_cast<int *>(cand_v + kWarps);
-  T *z = reinterpret_cast<T *>(smem_raw + L.off_z);
+  __shared__ bool s_singular;
+  __shared__ int s_level_bad;
+  FbBufs<T> b;
+  b.pan = reinterpret_cast<T *>(smem_raw + L.off_pan);      // pan[c * N + r]
+  b.Uc = reinterpret_cast<T *>(smem_raw + L.off_U);         // U12 chunk [t][kUs]
+  b.piv = reinterpret_cast<int *>(smem_raw + L.off_piv);    // the panel's pivot rows
+  b.pivabs = reinterpret_cast<T *>(smem_raw + L.off_pivabs);
+  b.cand_v = reinterpret_cast<T *>(smem_raw + L.off_cand);  // per-warp pivot candidates
+  b.cand_i = reinterpret_cast<int *>(b.cand_v + kWarps);
+  b.z = reinterpret_cast<T *>(smem_raw + L.off_z);
+  b.perm = reinterpret_cast<int *>(smem_raw + L.off_perm);
+  b.singular = &s_singular;
   double *nu = reinterpret_cast<double *>(smem_raw + L.off_nu);
   double *res = reinterpret_cast<double *>(smem_raw + L.off_res);
   double *red = reinterpret_cast<double *>(smem_raw + L.off_red);  // 64 doubles
-  int *perm = reinterpret_cast<int *>(smem_raw + L.off_perm);
   T *d = reinterpret_cast<T *>(smem_raw + L.off_d);
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarps = blockDim.x >> 5;
-  T *A = scratch + (size_t)blockIdx.x * mp * mp;
+  T *zf = reinterpret_cast<T *>(smem_raw + L.off_zf);  // node-indexed right-hand side
+  T *yf = reinterpret_cast<T *>(smem_raw + L.off_yf);  // node-indexed solution
+  T *yd = reinterpret_cast<T *>(smem_raw + L.off_yd);  // node-indexed correction
+  const int tid = threadIdx.x;
+  T *A = scratch + (size_t)blockIdx.x * per_cta;
+  T *vals = A + (size_t)dp * dp;  // the levels' value slots (core path)
   const bool solve = (x != nullptr);
-  __shared__ bool s_singular;
+  const bool planned = (ep.core_map != nullptr);
 
   // the flagged draws: the fast pass's list, or all n draws' flags
   const long cnt = pivot_list ? min((long)pivot_list[0], n) : n;
   for (long q = blockIdx.x; q < cnt; q += gridDim.x) {
     const long i = pivot_list ? (long)pivot_list[1 + q] : q;
     if (!(draw_flags[i] & DRAW_FLAG_PIVOT)) continue;
-    build_full<T>(m, P, mp, n, i, sp, theta, A);
     if (solve) {
       forecast_rhs<T>(m, P, n, i, rows, theta, x, lambda, key, nu);
       __syncthreads();
-      for (int r = tid; r < mp; r += blockDim.x) z[r] = (r < m) ? (T)nu[r] : T(0);
     }
-    for (int r = tid; r < mp; r += blockDim.x) perm[r] = r;
-    if (tid == 0) s_singular = false;
-    __syncthreads();
-    for (int k0 = 0; k0 < mp && !s_singular; k0 += kB) {
-      const int Rp = mp - k0, r0 = k0 + kB, R = mp - r0;
-      // (a) panel -> shared memory, factored with partial pivoting
-      for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
-        const int c = u / (Rp / W), rw = u - c * (Rp / W);
-        T v[W];
-        V::ld(A + (size_t)(k0 + rw * W) + (size_t)mp * (k0 + c), v);
-        V::st(pan + c * mp + rw * W, v);
-      }
-      __syncthreads();
-      for (int j = 0; j < kB; ++j) {
-        // pivot search in the working precision (ties -> lowest row)
-        T best = T(-1);
-        int bidx = j;
-        for (int r = j + tid; r < Rp; r += blockDim.x) {
-          const T v = dabs(pan[j * mp + r]);
-          if (v > best) {
-            best = v;
-            bidx = r;
-          }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const T ov = __shfl_xor_sync(kFull, best, o);
-          const int oi = __shfl_xor_sync(kFull, bidx, o);
-          if (ov > best || (ov == best && oi < bidx)) {
-            best = ov;
-            bidx = oi;
-          }
-        }
-        if (lane == 0) {
-          cand_v[warp] = best;
-          cand_i[warp] = bidx;
-        }
-        __syncthreads();
-        T b = cand_v[0];
-        int p = cand_i[0];
-        for (int w = 1; w < nwarps; ++w)
-          if (cand_v[w] > b || (cand_v[w] == b && cand_i[w] < p)) {
-            b = cand_v[w];
-            p = cand_i[w];
-          }
-        if (!(b > T(0)) || !(b <= (T)3.0e38)) {
-          if (tid == 0) s_singular = true;
-          break;  // uniform: every thread computed the same b
-        }
-        if (p != j && tid < kB) {
-          const T t0 = pan[tid * mp + j];
-          pan[tid * mp + j] = pan[tid * mp + p];
-          pan[tid * mp + p] = t0;
-        }
-        if (tid == 0) piv[j] = p;
-        __syncthreads();
-        const T pv = pan[j * mp + j];
-        if (tid == 0) pivabs[k0 + j] = dabs(pv);
-        for (int r = j + 1 + tid; r < Rp; r += blockDim.x) {
-          const T l = pan[j * mp + r] / pv;
-          pan[j * mp + r] = l;
-          for (int c = j + 1; c < kB; ++c) pan[c * mp + r] -= l * pan[c * mp + j];
-        }
-        __syncthreads();
-      }
-      __syncthreads();
-      if (s_singular) break;
-      // (b) factors back to global; the block's swaps on the other columns,
-      // the permutation and the right-hand side
-      for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
-        const int c = u / (Rp / W), rw = u - c * (Rp / W);
-        T v[W];
-        V::ld(pan + c * mp + rw * W, v);
-        V::st(A + (size_t)(k0 + rw * W) + (size_t)mp * (k0 + c), v);
-      }
-      for (int c = tid; c < mp - kB; c += blockDim.x) {
-        const int col = c < k0 ? c : c + kB;
-        T *cp = A + (size_t)mp * col;
-        for (int j = 0; j < kB; ++j) {
-          const int p = piv[j];
-          if (p != j) {
-            const T t0 = cp[k0 + j];
-            cp[k0 + j] = cp[k0 + p];
-            cp[k0 + p] = t0;
-          }
-        }
-      }
+    double ld_part = 0.0;
+    bool core = planned;
+    if (planned) {
+      // ---- the sparse levels, without pivoting
       if (tid == 0) {
-        for (int j = 0; j < kB; ++j) {
-          const int p = piv[j];
-          if (p != j) {
-            const int tp = perm[k0 + j];
-            perm[k0 + j] = perm[k0 + p];
-            perm[k0 + p] = tp;
-            if (solve) {
-              const T tz = z[k0 + j];
-              z[k0 + j] = z[k0 + p];
-              z[k0 + p] = tz;
-            }
-          }
-        }
+        vals[kSlotZero] = T(0);
+        vals[kSlotOne] = T(1);
+        s_level_bad = 0;
       }
+      for (int r = tid; r < m; r += blockDim.x) {
+        vals[ep.diag_slot[r]] = T(1);
+        if (solve) zf[r] = (T)nu[r];
+      }
+      for (int k = tid; k < ep.nnz0; k += blockDim.x) vals[ep.l0_slot[k]] = -theta.at(i, ep.l0_e[k]);
       __syncthreads();
-      // (c) U12 chunk by chunk, each followed by its trailing update
-      for (int c_off = 0; c_off < R; c_off += kFbChunk) {
-        const int C = min(kFbChunk, R - c_off);
-        for (int t = tid; t < C; t += blockDim.x) {
-          T *cp = A + (size_t)k0 + (size_t)mp * (r0 + c_off + t);
-          T xv[kB];
-#pragma unroll
-          for (int q = 0; q < kB; q += W) V::ld(cp + q, xv + q);
-#pragma unroll
-          for (int q = 1; q < kB; ++q) {
-            T acc = xv[q];
-#pragma unroll
-            for (int qq = 0; qq < q; ++qq) acc -= pan[qq * mp + q] * xv[qq];
-            xv[q] = acc;
-          }
-#pragma unroll
-          for (int q = 0; q < kB; q += W) {
-            V::st(cp + q, xv + q);
-            V::st(Uc + t * kUs + q, xv + q);
-          }
+      bool bad = false;
+      for (int lev = 0; lev < ep.nlev; ++lev) {
+        for (int g = ep.lev_piv[lev] + tid; g < ep.lev_piv[lev + 1]; g += blockDim.x) {
+          const T pv = vals[ep.piv[g]];
+          if (!(finite_t(pv) && pv != T(0))) bad = true;
+          ld_part += log_abs(pv);
+        }
+        for (int g = ep.lev_scale[lev] + tid; g < ep.lev_scale[lev + 1]; g += blockDim.x) {
+          const unsigned w = ep.scale[g];
+          const T l = vals[lo16(w)] / vals[hi16(w)];
+          if (!(dabs(l) <= (T)kLevelMultMax)) bad = true;
+          vals[lo16(w)] = l;
         }
         __syncthreads();
-        if (R > 0) trailing_update<T>(A, mp, r0, R, c_off, C, pan + kB, Uc, mp);
+        // new entries: one chunk of 32 entries per warp at a time, lane l its entry
+        for (int ch = ep.lev_chunk[lev] + (tid >> 5); ch < ep.lev_chunk[lev + 1]; ch += kWarps) {
+          const int lane = tid & 31;
+          const unsigned e = ep.ent[(size_t)ch * 32 + lane];
+          const int t0 = ep.chunk_tofs[ch], K = (ep.chunk_tofs[ch + 1] - t0) >> 5;
+          T v = vals[hi16(e)];
+          for (int k = 0; k < K; ++k) {
+            const unsigned w = ep.terms[t0 + 32 * k + lane];
+            v -= vals[lo16(w)] * vals[hi16(w)];
+          }
+          if ((unsigned)lo16(e) != kSlotNone) vals[lo16(e)] = v;
+        }
+        __syncthreads();
+        if (solve) level_forward<T>(ep, lev, vals, zf);
         __syncthreads();
       }
+      if (bad) atomicOr(&s_level_bad, 1);
+      __syncthreads();
+      core = (s_level_bad == 0);
     }
-    double ld = 0.0;
-    if (!s_singular)
-      for (int r = tid; r < mp; r += blockDim.x) ld += log_abs(pivabs[r]);
-    ld = block_sum_det(ld, red);  // contains __syncthreads
+    int N;
+    if (core) {
+      // ---- dense core through the slot map; its right-hand side
+      N = dp;
+      for (int qq = tid; qq < dp * dp; qq += blockDim.x) A[qq] = vals[ep.core_map[qq]];
+      if (solve)
+        for (int r = tid; r < dp; r += blockDim.x) b.z[r] = (r < ep.core_n) ? zf[ep.core_node[r]] : T(0);
+      __syncthreads();
+    } else {
+      // ---- the full matrix
+      N = mp;
+      ld_part = 0.0;
+      build_full<T>(m, P, mp, n, i, sp, theta, A);
+      if (solve)
+        for (int r = tid; r < mp; r += blockDim.x) b.z[r] = (r < m) ? (T)nu[r] : T(0);
+      __syncthreads();
+    }
+    const bool singular = pivot_lu<T>(A, N, solve, b);
+    if (!singular)
+      for (int r = tid; r < N; r += blockDim.x) ld_part += log_abs(b.pivabs[r]);
+    const double ld = block_sum_det(ld_part, red);  // contains __syncthreads
     if (tid == 0) {
-      if (s_singular) {
+      const int how = DRAW_FLAG_REDONE | (core ? 0 : DRAW_FLAG_FULL_PIVOT);
+      if (singular) {
         logdet[i] = -INFINITY;
-        atomicOr(&draw_flags[i], DRAW_FLAG_SINGULAR | DRAW_FLAG_REDONE);
+        atomicOr(&draw_flags[i], DRAW_FLAG_SINGULAR | how);
       } else {
         logdet[i] = ld;
-        atomicOr(&draw_flags[i], DRAW_FLAG_REDONE);
+        atomicOr(&draw_flags[i], how);
       }
     }
     __syncthreads();
     if (solve) {
-      if (s_singular) {
+      if (singular) {
         for (int r = tid; r < m; r += blockDim.x) y[(size_t)i * m + r] = NAN;
-      } else {
-        block_forward_solve<T>(A, mp, z, D);
-        block_back_solve<T>(A, mp, z, D);
+      } else if (core) {
+        // core solution, then the levels' backward program
+        block_forward_solve<T>(A, N, b.z, D);
+        block_back_solve<T>(A, N, b.z, D);
+        for (int r = tid; r < ep.core_n; r += blockDim.x) yf[ep.core_node[r]] = b.z[r];
+        __syncthreads();
+        levels_backward<T>(ep, vals, zf, yf);
         // the draws that reach this pass are the ill-conditioned ones: refine
         // kFbRefine times (FP64 residual of the working-precision solution),
         // which recovers working-precision accuracy while cond * eps < 1
         for (int it = 0; it < kFbRefine; ++it) {
           if (it > 0) {
-            for (int r = tid; r < m; r += blockDim.x) z[r] += d[r];
+            for (int r = tid; r < m; r += blockDim.x) yf[r] += yd[r];
             __syncthreads();
           }
-          residual<T>(m, P, n, i, rows, theta, nu, z, res);
-          for (int r = tid; r < mp; r += blockDim.x) d[r] = (perm[r] < m) ? (T)res[perm[r]] : T(0);
+          residual<T>(m, P, n, i, rows, theta, nu, yf, res);
+          for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)res[r];
           __syncthreads();
-          block_forward_solve<T>(A, mp, d, D);
-          block_back_solve<T>(A, mp, d, D);
+          levels_forward<T>(ep, vals, zf);
+          for (int r = tid; r < N; r += blockDim.x) {
+            const int pr = b.perm[r];
+            d[r] = (pr < ep.core_n) ? zf[ep.core_node[pr]] : T(0);
+          }
+          __syncthreads();
+          block_forward_solve<T>(A, N, d, D);
+          block_back_solve<T>(A, N, d, D);
+          for (int r = tid; r < ep.core_n; r += blockDim.x) yd[ep.core_node[r]] = d[r];
+          __syncthreads();
+          levels_backward<T>(ep, vals, zf, yd);
         }
         for (int r = tid; r < m; r += blockDim.x)
-          y[(size_t)i * m + r] = (double)z[r] + (double)d[r];
+          y[(size_t)i * m + r] = (double)yf[r] + (double)yd[r];
+      } else {
+        block_forward_solve<T>(A, N, b.z, D);
+        block_back_solve<T>(A, N, b.z, D);
+        for (int it = 0; it < kFbRefine; ++it) {
+          if (it > 0) {
+            for (int r = tid; r < m; r += blockDim.x) b.z[r] += d[r];
+            __syncthreads();
+          }
+          residual<T>(m, P, n, i, rows, theta, nu, b.z, res);
+          for (int r = tid; r < N; r += blockDim.x) d[r] = (b.perm[r] < m) ? (T)res[b.perm[r]] : T(0);
+          __syncthreads();
+          block_forward_solve<T>(A, N, d, D);
+          block_back_solve<T>(A, N, d, D);
+        }
+        for (int r = tid; r < m; r += blockDim.x)
+          y[(size_t)i * m + r] = (double)b.z[r] + (double)d[r];
       }
     }
     __syncthreads();
@@ -2321,10 +2459,12 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solv
   pl.grid = (int)grid;
   pl.scratch_elems_per_cta = (size_t)pl.dp * pl.dp + (((size_t)nv + 3) / 4) * 4;
   const size_t total = pl.scratch_elems_per_cta * pl.grid;
-  const size_t full = (size_t)pl.mp * pl.mp;
+  // the redo needs the dense core and the value slots, or a full m_p x m_p slab,
+  // per CTA; it shares the slab array
+  const size_t full = std::max((size_t)pl.mp * pl.mp, pl.scratch_elems_per_cta);
+  pl.fb_elems_per_cta = full;
   long fb = num_sms;
   if (fb > n) fb = n;
-  // the redo needs a full m_p x m_p slab per CTA; it shares the slab array
   if ((size_t)fb * full > total) {
     const long fit = (long)(total / full);
     fb = std::max(fit, std::min(fb, 16L));
@@ -2370,17 +2510,17 @@ void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, co
 }
 
 template <typename T>
-void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const unsigned *sp,
-                        const T *theta, const T *theta_dm, T *scratch, double *logdet,
-                        int *draw_flags,
+void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &ep,
+                        const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
+                        double *logdet, int *draw_flags,
                         const double *x, const T *lambda, RngKey key, double *y,
                         GammaRows rows, const int *pivot_list) {
   if (pl.smem_fallback > 48 * 1024)
     cudaFuncSetAttribute(k_lu_fallback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)pl.smem_fallback);
   k_lu_fallback<T><<<pl.fb_grid, pl.block, pl.smem_fallback, s>>>(
-      pl.m, pl.P, pl.mp, n, sp, theta, theta_dm, scratch, logdet, draw_flags, x, lambda, key, y,
-      rows, pivot_list);
+      pl.m, pl.P, pl.mp, pl.dp, pl.fb_elems_per_cta, n, ep, sp, theta, theta_dm, scratch, logdet,
+      draw_flags, x, lambda, key, y, rows, pivot_list);
 }
 
 template LuPlan plan_lu<float>(int, int, long, int, int, int, int, int, LuOptions);
@@ -2401,11 +2541,13 @@ template void launch_forecast_nu<float>(cudaStream_t, int, int, long, GammaRows,
 template void launch_forecast_nu<double>(cudaStream_t, int, int, long, GammaRows,
                                          const double *, const double *, const float *,
                                          const double *, RngKey, double *);
-template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long, const unsigned *,
+template void launch_lu_fallback<float>(cudaStream_t, const LuPlan &, long,
+                                        const EliminationPlan &, const unsigned *,
                                         const float *, const float *, float *, double *, int *,
                                         const double *,
                                         const float *, RngKey, double *, GammaRows, const int *);
-template void launch_lu_fallback<double>(cudaStream_t, const LuPlan &, long, const unsigned *,
+template void launch_lu_fallback<double>(cudaStream_t, const LuPlan &, long,
+                                         const EliminationPlan &, const unsigned *,
                                          const double *, const double *, double *, double *,
                                          int *,
                                          const double *, const double *, RngKey, double *,

@@ -150,7 +150,7 @@ extern "C" int sgdlm_log_det_noalloc(size_t m, size_t max_p, size_t n, const flo
   launch_lu<float>(s, pl, (long)n, no_plan, d_sp, d_theta, nullptr, (float *)scratch, d_log_det,
                    d_flags,
                    nullptr, nullptr, no_key, false, nullptr, no_rows);
-  launch_lu_fallback<float>(s, pl, (long)n, d_sp, d_theta, nullptr, (float *)scratch, d_log_det,
+  launch_lu_fallback<float>(s, pl, (long)n, no_plan, d_sp, d_theta, nullptr, (float *)scratch, d_log_det,
                             d_flags,
                             nullptr, nullptr, no_key, nullptr, no_rows);
   const cudaError_t e = cudaGetLastError();

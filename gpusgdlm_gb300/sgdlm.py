@@ -500,6 +500,16 @@ class SGDLM:
     def setForecastSolver(self, iterative: bool = True):
         self._check(self._lib.sgdlm_set_forecast_solver(self._h, 1 if iterative else 0))
 
+    def setWarpLu(self, enable: bool = True):
+        """m <= 32: one warp per draw with partial pivoting (default), or the
+        block LU kernels (include/sgdlm.h, sgdlm_set_warp_lu)."""
+        self._check(self._lib.sgdlm_set_warp_lu(self._h, 1 if enable else 0))
+
+    def getWarpLu(self):
+        en, use = C.c_int(), C.c_int()
+        self._lib.sgdlm_get_warp_lu(self._h, C.byref(en), C.byref(use))
+        return {"enabled": bool(en.value), "in_use": bool(use.value)}
+
     def getLuOptions(self):
         tc, mx = C.c_int(), C.c_int()
         self._lib.sgdlm_get_lu_options(self._h, C.byref(tc), C.byref(mx))

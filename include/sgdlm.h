@@ -78,6 +78,10 @@ typedef struct {
   /* last computeForecast: draws whose solve needed the LU factorisation (the rest
    * converged in the iterative solve of FP32 draws; all draws in FP64) */
   uint64_t forecast_draws_factored;
+  /* of draws_pivoted: draws whose sparse levels failed too (a zero, non-finite or
+   * huge level pivot multiplier), pivoted over the full matrix; the others were
+   * pivoted in the dense core only */
+  uint64_t draws_pivoted_full;
 } sgdlm_stats;
 
 /* ---- lifetime (HostWrapperFactory.cu:5-35, HostWrapperImpl.cu:12-105) ---- */
@@ -262,6 +266,12 @@ int sgdlm_set_lu_options(sgdlm_handle h, int allow_tensor_cores, int max_ctas);
  * factored.  Results equal to the refinement tolerance. */
 int sgdlm_set_forecast_solver(sgdlm_handle h, int iterative);
 int sgdlm_get_lu_options(sgdlm_handle h, int *allow_tensor_cores, int *max_ctas);
+/* Small systems (m <= 32): 1 (default) one warp per draw, each lane one row, LU
+ * with partial pivoting (no redo pass, forecasts of FP32 draws refined three times);
+ * 0 the block LU kernels as for larger m.  in_use: whether this engine's m takes
+ * the warp path. */
+int sgdlm_set_warp_lu(sgdlm_handle h, int enable);
+int sgdlm_get_warp_lu(sgdlm_handle h, int *enabled, int *in_use);
 typedef struct {
   int levels;           /* chosen sparse elimination levels */
   int tensor_cores;     /* chosen: 1 tensor-core fast pass, 0 FFMA */

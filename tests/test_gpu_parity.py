@@ -402,6 +402,7 @@ def test_pivoting_fallback(built_lib, precision, levels):
     m, P = 3, 1
     sp = np.array([[0 + 3 * 1, 1 + 3 * 0, 2 + 3 * 0]], dtype=np.float64)  # 0<-1, 1<-0, 2<-0
     s = SGDLM(1, strict=True, precision=precision)
+    s.setWarpLu(False)  # the block LU kernels (m <= 32 takes the warp path by default)
     s.setSimultaneousParents([1, 1, 1], sp)
     s.setEliminationLevels(levels)
     s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
@@ -429,6 +430,7 @@ def test_pivoting_fallback_forecast(built_lib, precision):
     m, P = 3, 1
     sp = np.array([[0 + 3 * 1, 1 + 3 * 0, 2 + 3 * 0]], dtype=np.float64)
     s = SGDLM(1, strict=True, precision=precision)
+    s.setWarpLu(False)  # the block LU kernels (m <= 32 takes the warp path by default)
     s.setSimultaneousParents([1, 1, 1], sp)
     s.setEliminationLevels(0)
     s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
@@ -445,6 +447,54 @@ def test_pivoting_fallback_forecast(built_lib, precision):
     # one FP64-residual refinement leave absolute errors of a few 1e-6 there
     tol = dict(rtol=1e-5, atol=1e-5) if precision == "mixed" else dict(rtol=1e-10, atol=1e-12)
     np.testing.assert_allclose(out["y"], y, **tol)
+
+
+@pytest.mark.parametrize("g01,full", [(100.0, False), (1.0e5, True)])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_pivoting_redo_core_and_full(built_lib, precision, g01, full):
+    """The redo keeps the sparse levels and pivots in the dense core, unless a
+    level multiplier is huge.  Parents 0<-1, 1<-0, 2<-0: level 0 eliminates nodes
+    1 and 2 (pivots 1), the core is node 0 and the level multiplier is
+    -Gamma_01.  Gamma_01 = 100 fails the fast pass's check (8) and is redone in
+    the core; Gamma_01 = 1e5 exceeds the levels' bound (65536) and is pivoted over
+    the full matrix.  log|det| and the forecasts against the oracle."""
+    m, P = 3, 1
+    sp = np.array([[0 + 3 * 1, 1 + 3 * 0, 2 + 3 * 0]], dtype=np.float64)
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setWarpLu(False)  # the block LU kernels (m <= 32 takes the warp path by default)
+    s.setSimultaneousParents([1, 1, 1], sp)
+    s.setEliminationLevels(4)
+    s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
+    mt = np.array([[g01, 20.0, -15.0]])
+    C = np.full((1, 1, m), 1e-6)
+    s.setPosteriorParameters(mt, C, np.full(m, 20.0), np.full(m, 1.0))
+    s.setRngState(9, 0)
+    s.computeVBPosterior(200, 200)
+    assert s.getEliminationInfo()["levels"] == 1
+    st = s.getStats()
+    assert st["draws_pivoted"] == 200
+    assert st["draws_pivoted_full"] == (200 if full else 0)
+    d = s.getDraws()
+    th = np.asfortranarray(d["thetas"].transpose(0, 2, 1))
+    spu = sp.astype(np.uint32)
+    tol = dict(rtol=1e-5, atol=1e-5) if precision == "mixed" else dict(rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(d["log_dets"], oracle.logdet(spu, th), **tol)
+    # forecasts of the same kind of draws (the iterative solve diverges on them)
+    s.setPriorParameters(mt, C, np.full(m, 20.0), np.full(m, 1.0))
+    s.setRngState(10, 0)
+    x = np.zeros((P, m), order="F")
+    out = s.computeForecastDebug(256, 256, x)
+    st = s.getStats()
+    assert st["draws_pivoted"] == 256
+    assert st["draws_pivoted_full"] == (256 if full else 0)
+    lam = np.asfortranarray(out["lambdas"].T)
+    th = np.asfortranarray(out["thetas"].transpose(0, 2, 1))
+    y, _ = oracle.forecast(spu, lam, th, x, 10, 0)
+    # normwise per draw: |y| reaches ~1e4 / 20 on the components that the large
+    # coefficient couples
+    err = np.abs(out["y"] - y).max(axis=0) / np.abs(y).max(axis=0)
+    assert err.max() <= (1e-5 if precision == "mixed" else 1e-11)
+    s.close()
 
 
 def test_fused_device_step_matches_api_sequence(built_lib):
