@@ -548,7 +548,7 @@ void sample_draws(sgdlm_engine *h, const double *m_t, const double *C_t, const d
   const T *U = std::is_same<T, float>::value ? reinterpret_cast<const T *>(h->U32.ptr)
                                               : reinterpret_cast<const T *>(h->U64.ptr);
   launch_sample<T>(h->stream, m, P, n, m_t, n_t, s_t, U, key, as<T>(h->lambda), as<T>(h->theta),
-                   as<T>(h->theta_dm), h->draw_flags.ptr);
+                   as<T>(h->theta_dm), h->draw_flags.ptr, h->p.ptr);
   h->launches += 2;
 }
 
@@ -746,7 +746,7 @@ int learned_draws(sgdlm_engine *h, RngKey key) {
   launch_proposal_params<T>(s, m, P, h->p.ptr, q.Out.ptr, h->m_t.ptr, h->n_t.ptr, h->s_t.ptr,
                             h->U64.ptr, q.mq.ptr, q.nq.ptr, q.sq.ptr, q.Uq64.ptr, Uq, q.cst.ptr);
   launch_sample<T>(s, m, P, n, q.mq.ptr, q.nq.ptr, q.sq.ptr, Uq, key, as<T>(h->lambda),
-                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr);
+                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr, h->p.ptr);
   h->launches += 8;
   CK(cudaEventRecord(h->ev[1], s));
   int st = lu_draws<T>(h, nullptr, key, nullptr);

@@ -8,8 +8,8 @@
 // iteration converges geometrically at O(nnz) per sweep -- a few ten thousand
 // flop per draw at m = 400 instead of 10^8.  A draw is solved here when
 //   (1) the sweeps from y = nu reach max|dy| <= 2^-20 max|y| within kMaxSweeps
-//       (FP32; each thread holds its rows' Gamma entries in registers in ELL
-//       form, the iterate is in shared memory),
+//       (FP32; one thread per row holds the row's Gamma entries in registers in
+//       ELL form, the iterate is in shared memory),
 //   (2) the FP64 residual r = nu - (I - Gamma_i) y, solved by the same
 //       iteration, gives a correction d with max|d| <= 1e-3 max|y| (the rule
 //       the factorising path applies to its refinement step); y + d is written.
@@ -23,8 +23,7 @@
 namespace sgdlm {
 namespace {
 
-constexpr int kJacThreads = 256;
-constexpr int kRowsPerThread = 2;  // m <= 512
+constexpr int kJacMaxThreads = 1024;  // one row per thread: m <= 1024
 constexpr int kMaxSweeps = 128;
 // The first solve stops at max|dy| <= 2^-20 max|y|; the correction, whose size
 // is that of y's error, needs only 2^-10 of its own size: y + d is then within
@@ -47,7 +46,7 @@ struct JacSmem {
     ya = take((size_t)m * sizeof(float));
     yb = take((size_t)m * sizeof(float));
     res = take((size_t)m * sizeof(float));
-    red = take(2 * (kJacThreads / 32) * sizeof(float));
+    red = take(2 * (kJacMaxThreads / 32) * sizeof(float));
     total = o;
   }
 };
@@ -75,46 +74,42 @@ __device__ __forceinline__ void block_max2f(float &a, float &b, float *red) {
   }
 }
 
-// A thread's rows r = threadIdx.x + 256 rr, in ELL form held in registers: K
-// slots per row (entries beyond the row's length have value 0 and point at the
-// row itself), the column indices packed two to a register.
-template <int K> struct Rows {
-  int r[kRowsPerThread];
-  uint32_t col[kRowsPerThread][K / 2];
-  float val[kRowsPerThread][K];
-  __device__ __forceinline__ int c(int rr, int q) const {
-    return (int)((col[rr][q >> 1] >> (16 * (q & 1))) & 0xFFFFu);
+// The thread's row r = threadIdx.x in ELL form held in registers: K slots
+// (entries beyond the row's length have value 0 and point at the row itself),
+// the column indices packed two to a register.
+template <int K> struct Row {
+  uint32_t col[K / 2];
+  float val[K];
+  __device__ __forceinline__ int c(int q) const {
+    return (int)((col[q >> 1] >> (16 * (q & 1))) & 0xFFFFu);
   }
 };
 
 // Sweeps x <- c + Gamma x from x = c.  Returns whether they converged
 // (max|dx| <= tol max|x|, everything finite); *out is the last iterate.
 template <int K>
-__device__ bool jacobi(int m, const Rows<K> &R, const float *c, float *xa, float *xb, float *red,
+__device__ bool jacobi(int m, const Row<K> &R, const float *c, float *xa, float *xb, float *red,
                        float tol, float **out) {
-  for (int r = threadIdx.x; r < m; r += blockDim.x) xa[r] = c[r];
+  const int r = threadIdx.x;
+  if (r < m) xa[r] = c[r];
   __syncthreads();
   float *cur = xa, *nxt = xb;
   for (int it = 1; it <= kMaxSweeps; ++it) {
     float dmax = 0.f, xmax = 0.f;
+    if (r < m) {
+      float a0 = c[r], a1 = 0.f;
 #pragma unroll
-    for (int rr = 0; rr < kRowsPerThread; ++rr) {
-      const int r = R.r[rr];
-      if (r < m) {
-        float a0 = c[r], a1 = 0.f;
-#pragma unroll
-        for (int q = 0; q < K; q += 2) {
-          a0 = fmaf(R.val[rr][q], cur[R.c(rr, q)], a0);
-          a1 = fmaf(R.val[rr][q + 1], cur[R.c(rr, q + 1)], a1);
-        }
-        const float v = a0 + a1;
-        nxt[r] = v;
-        // fmaxf drops NaN operands: a NaN (an overflowed iterate times a padded
-        // zero slot) must count as divergence, so it becomes infinity here
-        const float av = fabsf(v), dv = fabsf(v - cur[r]);
-        xmax = (av == av) ? fmaxf(xmax, av) : INFINITY;
-        dmax = (dv == dv) ? fmaxf(dmax, dv) : INFINITY;
+      for (int q = 0; q < K; q += 2) {
+        a0 = fmaf(R.val[q], cur[R.c(q)], a0);
+        a1 = fmaf(R.val[q + 1], cur[R.c(q + 1)], a1);
       }
+      const float v = a0 + a1;
+      nxt[r] = v;
+      // fmaxf drops NaN operands: a NaN (an overflowed iterate times a padded
+      // zero slot) must count as divergence, so it becomes infinity here
+      const float av = fabsf(v), dv = fabsf(v - cur[r]);
+      xmax = (av == av) ? av : INFINITY;
+      dmax = (dv == dv) ? dv : INFINITY;
     }
     float *t = cur;
     cur = nxt;
@@ -135,7 +130,7 @@ __device__ bool jacobi(int m, const Rows<K> &R, const float *c, float *xa, float
 }
 
 template <int K>
-__global__ void __launch_bounds__(kJacThreads)
+__global__ void __launch_bounds__(kJacMaxThreads)
     k_forecast_jacobi(int m, int P, long n, GammaRows rows, const float *__restrict__ theta_dm,
                       const double *__restrict__ nu, double *__restrict__ y,
                       double *__restrict__ logdet, int *__restrict__ list) {
@@ -147,33 +142,24 @@ __global__ void __launch_bounds__(kJacThreads)
   float *yb = reinterpret_cast<float *>(smem_raw + L.yb);
   float *res = reinterpret_cast<float *>(smem_raw + L.res);
   float *red = reinterpret_cast<float *>(smem_raw + L.red);
-  const int tid = threadIdx.x;
-  Rows<K> R;
-  int e0[kRowsPerThread], len[kRowsPerThread];
+  const int tid = threadIdx.x, r = tid;
+  Row<K> R;
+  const int e0 = r < m ? rows.rowptr[r] : 0;
+  const int len = r < m ? rows.rowptr[r + 1] - e0 : 0;
 #pragma unroll
-  for (int rr = 0; rr < kRowsPerThread; ++rr) {
-    const int r = tid + kJacThreads * rr;
-    R.r[rr] = r;
-    e0[rr] = r < m ? rows.rowptr[r] : 0;
-    len[rr] = r < m ? rows.rowptr[r + 1] - e0[rr] : 0;
-#pragma unroll
-    for (int q = 0; q < K; q += 2) {
-      const uint32_t c0 = q < len[rr] ? (uint32_t)rows.ent[e0[rr] + q].y : (uint32_t)(r < m ? r : 0);
-      const uint32_t c1 =
-          q + 1 < len[rr] ? (uint32_t)rows.ent[e0[rr] + q + 1].y : (uint32_t)(r < m ? r : 0);
-      R.col[rr][q >> 1] = c0 | (c1 << 16);
-    }
+  for (int q = 0; q < K; q += 2) {
+    const uint32_t self = (uint32_t)(r < m ? r : 0);
+    const uint32_t c0 = q < len ? (uint32_t)rows.ent[e0 + q].y : self;
+    const uint32_t c1 = q + 1 < len ? (uint32_t)rows.ent[e0 + q + 1].y : self;
+    R.col[q >> 1] = c0 | (c1 << 16);
   }
   const size_t row_len = (size_t)m * P;
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
     // this draw's Gamma entries (from its draw-major theta row) and nu
     const float *th = theta_dm + (size_t)i * row_len;
 #pragma unroll
-    for (int rr = 0; rr < kRowsPerThread; ++rr)
-#pragma unroll
-      for (int q = 0; q < K; ++q)
-        R.val[rr][q] = q < len[rr] ? th[__ldg(&rows.ent[e0[rr] + q].x)] : 0.f;
-    for (int r = tid; r < m; r += blockDim.x) {
+    for (int q = 0; q < K; ++q) R.val[q] = q < len ? th[__ldg(&rows.ent[e0 + q].x)] : 0.f;
+    if (r < m) {
       const double v = nu[(size_t)r * n + i];
       nud[r] = v;
       nuf[r] = (float)v;
@@ -184,15 +170,11 @@ __global__ void __launch_bounds__(kJacThreads)
     if (ok) {
       // residual in FP64 and its correction by the same iteration
       float *other = (yv == ya) ? yb : ya;
+      if (r < m) {
+        double v = nud[r] - (double)yv[r];
 #pragma unroll
-      for (int rr = 0; rr < kRowsPerThread; ++rr) {
-        const int r = R.r[rr];
-        if (r < m) {
-          double v = nud[r] - (double)yv[r];
-#pragma unroll
-          for (int q = 0; q < K; ++q) v += (double)R.val[rr][q] * (double)yv[R.c(rr, q)];
-          res[r] = (float)v;
-        }
+        for (int q = 0; q < K; ++q) v += (double)R.val[q] * (double)yv[R.c(q)];
+        res[r] = (float)v;
       }
       __syncthreads();
       // the correction's iterates go to `other` and nuf (nu's FP32 copy is no
@@ -200,16 +182,14 @@ __global__ void __launch_bounds__(kJacThreads)
       float *dv = nullptr;
       ok = jacobi<K>(m, R, res, other, nuf, red, kCorrSweepTol, &dv);
       float dmax = 0.f, ymax = 0.f;
-      for (int r = tid; r < m; r += blockDim.x) {
+      if (r < m) {
         const float ad = fabsf(dv[r]), ay = fabsf(yv[r]);
-        dmax = (ad == ad) ? fmaxf(dmax, ad) : INFINITY;
-        ymax = (ay == ay) ? fmaxf(ymax, ay) : INFINITY;
+        dmax = (ad == ad) ? ad : INFINITY;
+        ymax = (ay == ay) ? ay : INFINITY;
       }
       block_max2f(dmax, ymax, red);
       ok = ok && ymax < INFINITY && dmax < INFINITY && (double)dmax <= kCorrTol * (double)ymax;
-      if (ok)
-        for (int r = tid; r < m; r += blockDim.x)
-          y[(size_t)i * m + r] = (double)yv[r] + (double)dv[r];
+      if (ok && r < m) y[(size_t)i * m + r] = (double)yv[r] + (double)dv[r];
     }
     if (tid == 0) {
       if (ok) {
@@ -223,22 +203,38 @@ __global__ void __launch_bounds__(kJacThreads)
   }
 }
 
+// ELL widths: the smallest of these that holds the longest row
+constexpr int kJacWidths[] = {8, 12, 16, 18, 20, 24, 32};
+
 template <int K> void *jacobi_kernel() { return reinterpret_cast<void *>(k_forecast_jacobi<K>); }
+void *jacobi_kernel_for(int K) {
+  switch (K) {
+    case 8: return jacobi_kernel<8>();
+    case 12: return jacobi_kernel<12>();
+    case 16: return jacobi_kernel<16>();
+    case 18: return jacobi_kernel<18>();
+    case 20: return jacobi_kernel<20>();
+    case 24: return jacobi_kernel<24>();
+    default: return jacobi_kernel<32>();
+  }
+}
 
 }  // namespace
 
 JacobiPlan plan_jacobi(int m, int max_row, int num_sms) {
   JacobiPlan jp{};
-  if (m < 1 || m > kJacThreads * kRowsPerThread || max_row > 32) return jp;
-  jp.nnz = max_row <= 8 ? 8 : (max_row <= 16 ? 16 : (max_row <= 24 ? 24 : 32));  // ELL slots
+  if (m < 1 || m > kJacMaxThreads || max_row > 32) return jp;
+  jp.nnz = 32;
+  for (int k : kJacWidths)
+    if (max_row <= k) {
+      jp.nnz = k;
+      break;
+    }
+  jp.threads = (m + 31) / 32 * 32;
   jp.smem = JacSmem(m).total;
-  const void *kern = jp.nnz == 8 ? jacobi_kernel<8>()
-                     : jp.nnz == 16 ? jacobi_kernel<16>()
-                     : jp.nnz == 24 ? jacobi_kernel<24>()
-                                    : jacobi_kernel<32>();
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kJacThreads, jp.smem) !=
-          cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_kernel_for(jp.nnz), jp.threads,
+                                                    jp.smem) != cudaSuccess ||
       per_sm < 1) {
     (void)cudaGetLastError();
     return jp;
@@ -252,20 +248,19 @@ void launch_forecast_jacobi(cudaStream_t s, const JacobiPlan &jp, int m, int P, 
                             GammaRows rows, const float *theta_dm, const double *nu, double *y,
                             double *logdet, int *list) {
   const unsigned grid = (unsigned)std::max<long>(std::min<long>(jp.grid, n), 1);
+  const unsigned th = (unsigned)jp.threads;
+#define SGDLM_JACOBI(K)                                                                    \
+  k_forecast_jacobi<K><<<grid, th, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list)
   switch (jp.nnz) {
-    case 8:
-      k_forecast_jacobi<8><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
-      break;
-    case 16:
-      k_forecast_jacobi<16><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
-      break;
-    case 24:
-      k_forecast_jacobi<24><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
-      break;
-    default:
-      k_forecast_jacobi<32><<<grid, kJacThreads, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list);
-      break;
+    case 8: SGDLM_JACOBI(8); break;
+    case 12: SGDLM_JACOBI(12); break;
+    case 16: SGDLM_JACOBI(16); break;
+    case 18: SGDLM_JACOBI(18); break;
+    case 20: SGDLM_JACOBI(20); break;
+    case 24: SGDLM_JACOBI(24); break;
+    default: SGDLM_JACOBI(32); break;
   }
+#undef SGDLM_JACOBI
 }
 
 }  // namespace sgdlm

@@ -64,7 +64,9 @@ void launch_cholesky(cudaStream_t s, int m, int P, const unsigned *p, const doub
 template <typename T>
 void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                    const double *n_t, const double *s_t, const T *U, RngKey key,
-                   T *lambda, T *theta, T *theta_dm, int *draw_flags);
+                   T *lambda, T *theta, T *theta_dm, int *draw_flags,
+                   // p_j (the Cholesky factors' cut), or nullptr: all P coefficients
+                   const unsigned *p = nullptr);
 
 // (a9) multi-step evolution of forecast draws.  rSGDLM/src/SGDLM/SGDLM.cu:679-762
 template <typename T>
@@ -88,6 +90,7 @@ struct LuPlan {
   int tc;              // trailing updates on the tensor cores (tcgen05)
   size_t scratch_elems_per_cta;  // dense core + per-draw values of the sparse levels
   size_t fb_elems_per_cta;       // the redo's: the above, or a full m_p x m_p slab
+  int fb_core_smem;              // the redo factors the dense core in shared memory
   size_t scratch_elems_total;    // covers both passes
 };
 // Tuning knobs of the fast pass: allow_tc = 0 keeps the FFMA instantiation where
@@ -143,10 +146,10 @@ void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan
 // (forecast_kernels.cu).  ok = 0: the shared-memory working set of a draw does
 // not fit, every draw keeps the factorising path.
 struct JacobiPlan {
-  int ok, grid, nnz;  // nnz: ELL slots per row (8, 16, 24 or 32)
+  int ok, grid, threads, nnz;  // threads: m rounded up to 32; nnz: ELL slots per row (8..32)
   size_t smem;
 };
-// m <= 512 and at most 32 simultaneous parents per series, else ok = 0.
+// m <= 1024 and at most 32 simultaneous parents per series, else ok = 0.
 JacobiPlan plan_jacobi(int m, int max_row, int num_sms);
 // y (draw-major) of every draw whose iteration converges (logdet[i] set to NaN:
 // not factored); the others are appended to list (n + 1 ints, [0] zero on entry).

@@ -176,17 +176,23 @@ constexpr double kLevelMultMax = 65536.0;
 // most this fraction of the solution (the error left is about its square)
 constexpr double kRefineTol = 1e-3;
 struct FallbackSmem {
-  size_t off_pan, off_U, off_piv, off_pivabs, off_cand, off_D, off_z, off_d, off_perm, off_nu,
-      off_res, off_red, off_zf, off_yf, off_yd, total;
-  __host__ __device__ FallbackSmem(int mp, int m, size_t tsz) {
+  size_t off_pan, off_U, off_core, off_piv, off_pivabs, off_cand, off_D, off_z, off_d, off_perm,
+      off_nu, off_res, off_red, off_zf, off_yf, off_yd, total;
+  // core_dp > 0: the dense core (core_dp x core_dp) is factored in shared memory,
+  // in a region that the full-matrix path's panel buffers share
+  __host__ __device__ FallbackSmem(int mp, int m, size_t tsz, int core_dp = 0) {
     size_t o = 0;
     auto take = [&](size_t bytes) {
       const size_t at = o;
       o += (bytes + 15) & ~(size_t)15;
       return at;
     };
-    off_pan = take((size_t)kB * mp * tsz);
-    off_U = take((size_t)kFbChunk * kUs * tsz);
+    const size_t pan_bytes = ((size_t)kB * mp * tsz + 15) & ~(size_t)15;
+    const size_t u_bytes = (size_t)kFbChunk * kUs * tsz;
+    const size_t core_bytes = (size_t)core_dp * core_dp * tsz;
+    const size_t region = core_bytes > pan_bytes + u_bytes ? core_bytes : pan_bytes + u_bytes;
+    off_core = off_pan = take(region);
+    off_U = off_pan + pan_bytes;
     off_piv = take((size_t)kB * sizeof(int));
     off_pivabs = take((size_t)mp * tsz);
     off_cand = take((size_t)2 * kWarps * (tsz > 4 ? tsz : 4));
@@ -340,7 +346,7 @@ template <> struct Pair<double> {
 
 // Register-tiled trailing update A[r0:, r0:] -= Lp B over the rows r0 .. r0+R and
 // the C columns r0+c_off .. (a chunk of the R x R trailing matrix; R and C are
-// multiples of 32), B (32 x C) read from Up[t * kUs + c] with t relative to the
+// multiples of 32), B (32 x C) read from Up[t * Us + c] with t relative to the
 // chunk.  The region is cut exactly into units of 2W rows x 8 columns: rows
 // {ra .. ra+W-1, ra+R/2 .. ra+R/2+W-1} and columns {ca .. ca+3, ca+C/2 .. ca+C/2+3},
 // handed round-robin to the nthr threads tid = 0 .. nthr-1 (no padded tiles).  Consecutive threads take
@@ -350,7 +356,7 @@ template <> struct Pair<double> {
 template <typename T>
 __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r0, int R,
                                                 int c_off, int C, const T *__restrict__ Lp,
-                                                const T *__restrict__ Up, int Rmax,
+                                                const T *__restrict__ Up, int Rmax, int Us = kUs,
                                                 int tid = threadIdx.x, int nthr = blockDim.x) {
   using V = Vec<T>;
   constexpr int W = V::W;
@@ -383,7 +389,7 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
 #pragma unroll
       for (int b = 0; b < TN; ++b) {
         const int col = (b < 4) ? (ca + b) : (cb + b - 4);
-        Pair<T>::ld(Up + col * kUs + k2, u2[b]);
+        Pair<T>::ld(Up + col * Us + k2, u2[b]);
       }
 #pragma unroll
       for (int kk = 0; kk < 2; ++kk) {
@@ -431,7 +437,7 @@ __device__ __forceinline__ void trailing_update(T *__restrict__ A, int mp, int r
     for (int k2 = 0; k2 < kB; k2 += 2) {
       T u2[4][2];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) Pair<T>::ld(Up + (ca + b) * kUs + k2, u2[b]);
+      for (int b = 0; b < 4; ++b) Pair<T>::ld(Up + (ca + b) * Us + k2, u2[b]);
 #pragma unroll
       for (int kk = 0; kk < 2; ++kk) {
         T lv[W];
@@ -2089,8 +2095,11 @@ template <typename T> struct FbBufs {
 // LU with partial pivoting of the N x N column-major matrix A (N a multiple of
 // 32) in place; perm records the row permutation and, when `rhs`, z (length N)
 // is permuted alongside.  pivabs[0..N) receives |u_jj|.  Returns true (uniform
-// over the block) when a pivot column is zero or non-finite.
-template <typename T>
+// over the block) when a pivot column is zero or non-finite.  InSmem: A is in
+// shared memory, the panels are factored where they lie and the trailing update
+// reads U12 from A; otherwise each panel is staged in b.pan and U12's chunks in
+// b.Uc.
+template <typename T, bool InSmem>
 __device__ bool pivot_lu(T *__restrict__ A, int N, bool rhs, const FbBufs<T> &b) {
   using V = Vec<T>;
   constexpr int W = V::W;
@@ -2101,20 +2110,23 @@ __device__ bool pivot_lu(T *__restrict__ A, int N, bool rhs, const FbBufs<T> &b)
   __syncthreads();
   for (int k0 = 0; k0 < N && !*b.singular; k0 += kB) {
     const int Rp = N - k0, r0 = k0 + kB, R = N - r0;
-    // (a) panel -> shared memory, factored with partial pivoting
-    for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
-      const int c = u / (Rp / W), rw = u - c * (Rp / W);
-      T v[W];
-      V::ld(A + (size_t)(k0 + rw * W) + (size_t)N * (k0 + c), v);
-      V::st(b.pan + c * N + rw * W, v);
+    T *pan = InSmem ? A + (size_t)k0 * N + k0 : b.pan;  // pan[c * N + r]: row k0 + r, column k0 + c
+    // (a) the panel, factored with partial pivoting
+    if (!InSmem) {
+      for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
+        const int c = u / (Rp / W), rw = u - c * (Rp / W);
+        T v[W];
+        V::ld(A + (size_t)(k0 + rw * W) + (size_t)N * (k0 + c), v);
+        V::st(pan + c * N + rw * W, v);
+      }
+      __syncthreads();
     }
-    __syncthreads();
     for (int j = 0; j < kB; ++j) {
       // pivot search in the working precision (ties -> lowest row)
       T best = T(-1);
       int bidx = j;
       for (int r = j + tid; r < Rp; r += blockDim.x) {
-        const T v = dabs(b.pan[j * N + r]);
+        const T v = dabs(pan[j * N + r]);
         if (v > best) {
           best = v;
           bidx = r;
@@ -2146,30 +2158,32 @@ __device__ bool pivot_lu(T *__restrict__ A, int N, bool rhs, const FbBufs<T> &b)
         break;  // uniform: every thread computed the same bv
       }
       if (p != j && tid < kB) {
-        const T t0 = b.pan[tid * N + j];
-        b.pan[tid * N + j] = b.pan[tid * N + p];
-        b.pan[tid * N + p] = t0;
+        const T t0 = pan[tid * N + j];
+        pan[tid * N + j] = pan[tid * N + p];
+        pan[tid * N + p] = t0;
       }
       if (tid == 0) b.piv[j] = p;
       __syncthreads();
-      const T pv = b.pan[j * N + j];
+      const T pv = pan[j * N + j];
       if (tid == 0) b.pivabs[k0 + j] = dabs(pv);
       for (int r = j + 1 + tid; r < Rp; r += blockDim.x) {
-        const T l = b.pan[j * N + r] / pv;
-        b.pan[j * N + r] = l;
-        for (int c = j + 1; c < kB; ++c) b.pan[c * N + r] -= l * b.pan[c * N + j];
+        const T l = pan[j * N + r] / pv;
+        pan[j * N + r] = l;
+        for (int c = j + 1; c < kB; ++c) pan[c * N + r] -= l * pan[c * N + j];
       }
       __syncthreads();
     }
     __syncthreads();
     if (*b.singular) break;
-    // (b) factors back to global; the block's swaps on the other columns, the
+    // (b) the factors back to global; the block's swaps on the other columns, the
     // permutation and the right-hand side
-    for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
-      const int c = u / (Rp / W), rw = u - c * (Rp / W);
-      T v[W];
-      V::ld(b.pan + c * N + rw * W, v);
-      V::st(A + (size_t)(k0 + rw * W) + (size_t)N * (k0 + c), v);
+    if (!InSmem) {
+      for (int u = tid; u < kB * (Rp / W); u += blockDim.x) {
+        const int c = u / (Rp / W), rw = u - c * (Rp / W);
+        T v[W];
+        V::ld(pan + c * N + rw * W, v);
+        V::st(A + (size_t)(k0 + rw * W) + (size_t)N * (k0 + c), v);
+      }
     }
     for (int c = tid; c < N - kB; c += blockDim.x) {
       const int col = c < k0 ? c : c + kB;
@@ -2211,17 +2225,22 @@ __device__ bool pivot_lu(T *__restrict__ A, int N, bool rhs, const FbBufs<T> &b)
         for (int q = 1; q < kB; ++q) {
           T acc = xv[q];
 #pragma unroll
-          for (int qq = 0; qq < q; ++qq) acc -= b.pan[qq * N + q] * xv[qq];
+          for (int qq = 0; qq < q; ++qq) acc -= pan[qq * N + q] * xv[qq];
           xv[q] = acc;
         }
 #pragma unroll
         for (int q = 0; q < kB; q += W) {
           V::st(cp + q, xv + q);
-          V::st(b.Uc + t * kUs + q, xv + q);
+          if (!InSmem) V::st(b.Uc + t * kUs + q, xv + q);
         }
       }
       __syncthreads();
-      if (R > 0) trailing_update<T>(A, N, r0, R, c_off, C, b.pan + kB, b.Uc, N);
+      if (R > 0) {
+        if (InSmem)
+          trailing_update<T>(A, N, r0, R, c_off, C, pan + kB, A + (size_t)N * (r0 + c_off) + k0, N, N);
+        else
+          trailing_update<T>(A, N, r0, R, c_off, C, pan + kB, b.Uc, N);
+      }
       __syncthreads();
     }
   }
@@ -2231,7 +2250,8 @@ __device__ bool pivot_lu(T *__restrict__ A, int N, bool rhs, const FbBufs<T> &b)
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_lu_fallback(int m, int P, int mp, int dp, size_t per_cta, long n, EliminationPlan ep,
+    k_lu_fallback(int m, int P, int mp, int dp, size_t per_cta, int core_smem, long n,
+                  EliminationPlan ep,
                   const unsigned *__restrict__ sp,
                   const T *__restrict__ theta_sm, const T *__restrict__ theta_dm,
                   T *__restrict__ scratch,
@@ -2240,7 +2260,7 @@ __global__ void __launch_bounds__(kThreads)
                   double *__restrict__ y, GammaRows rows, const int *__restrict__ pivot_list) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const Theta<T> theta{theta_sm, theta_dm, m, P, n};
-  const FallbackSmem L(mp, m, sizeof(T));
+  const FallbackSmem L(mp, m, sizeof(T), core_smem ? dp : 0);
   __shared__ bool s_singular;
   __shared__ int s_level_bad;
   FbBufs<T> b;
@@ -2326,10 +2346,13 @@ __global__ void __launch_bounds__(kThreads)
       core = (s_level_bad == 0);
     }
     int N;
+    // the matrix factored: the dense core (in shared memory when it fits) or the
+    // full matrix (global)
+    T *F = (core && core_smem) ? reinterpret_cast<T *>(smem_raw + L.off_core) : A;
     if (core) {
       // ---- dense core through the slot map; its right-hand side
       N = dp;
-      for (int qq = tid; qq < dp * dp; qq += blockDim.x) A[qq] = vals[ep.core_map[qq]];
+      for (int qq = tid; qq < dp * dp; qq += blockDim.x) F[qq] = vals[ep.core_map[qq]];
       if (solve)
         for (int r = tid; r < dp; r += blockDim.x) b.z[r] = (r < ep.core_n) ? zf[ep.core_node[r]] : T(0);
       __syncthreads();
@@ -2342,7 +2365,8 @@ __global__ void __launch_bounds__(kThreads)
         for (int r = tid; r < mp; r += blockDim.x) b.z[r] = (r < m) ? (T)nu[r] : T(0);
       __syncthreads();
     }
-    const bool singular = pivot_lu<T>(A, N, solve, b);
+    const bool singular = (core && core_smem) ? pivot_lu<T, true>(F, N, solve, b)
+                                              : pivot_lu<T, false>(F, N, solve, b);
     if (!singular)
       for (int r = tid; r < N; r += blockDim.x) ld_part += log_abs(b.pivabs[r]);
     const double ld = block_sum_det(ld_part, red);  // contains __syncthreads
@@ -2362,8 +2386,8 @@ __global__ void __launch_bounds__(kThreads)
         for (int r = tid; r < m; r += blockDim.x) y[(size_t)i * m + r] = NAN;
       } else if (core) {
         // core solution, then the levels' backward program
-        block_forward_solve<T>(A, N, b.z, D);
-        block_back_solve<T>(A, N, b.z, D);
+        block_forward_solve<T>(F, N, b.z, D);
+        block_back_solve<T>(F, N, b.z, D);
         for (int r = tid; r < ep.core_n; r += blockDim.x) yf[ep.core_node[r]] = b.z[r];
         __syncthreads();
         levels_backward<T>(ep, vals, zf, yf);
@@ -2384,8 +2408,8 @@ __global__ void __launch_bounds__(kThreads)
             d[r] = (pr < ep.core_n) ? zf[ep.core_node[pr]] : T(0);
           }
           __syncthreads();
-          block_forward_solve<T>(A, N, d, D);
-          block_back_solve<T>(A, N, d, D);
+          block_forward_solve<T>(F, N, d, D);
+          block_back_solve<T>(F, N, d, D);
           for (int r = tid; r < ep.core_n; r += blockDim.x) yd[ep.core_node[r]] = d[r];
           __syncthreads();
           levels_backward<T>(ep, vals, zf, yd);
@@ -2393,8 +2417,8 @@ __global__ void __launch_bounds__(kThreads)
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)yf[r] + (double)yd[r];
       } else {
-        block_forward_solve<T>(A, N, b.z, D);
-        block_back_solve<T>(A, N, b.z, D);
+        block_forward_solve<T>(F, N, b.z, D);
+        block_back_solve<T>(F, N, b.z, D);
         for (int it = 0; it < kFbRefine; ++it) {
           if (it > 0) {
             for (int r = tid; r < m; r += blockDim.x) b.z[r] += d[r];
@@ -2403,8 +2427,8 @@ __global__ void __launch_bounds__(kThreads)
           residual<T>(m, P, n, i, rows, theta, nu, b.z, res);
           for (int r = tid; r < N; r += blockDim.x) d[r] = (b.perm[r] < m) ? (T)res[b.perm[r]] : T(0);
           __syncthreads();
-          block_forward_solve<T>(A, N, d, D);
-          block_back_solve<T>(A, N, d, D);
+          block_forward_solve<T>(F, N, d, D);
+          block_back_solve<T>(F, N, d, D);
         }
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)b.z[r] + (double)d[r];
@@ -2449,7 +2473,16 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solv
     const size_t used = (((size_t)n_solve + 3) / 4 * 4 * sizeof(T) + 15) & ~(size_t)15;
     pl.prog_smem = (pl.vals_smem && prog_len > 0 && used + (size_t)prog_len * 4 <= region) ? 1 : 0;
   }
+  // the redo factors the dense core in shared memory when it fits (one CTA per SM)
+  pl.fb_core_smem = 0;
   pl.smem_fallback = FallbackSmem(pl.mp, m, sizeof(T)).total;
+  if (nv > 0) {
+    const size_t with_core = FallbackSmem(pl.mp, m, sizeof(T), pl.dp).total;
+    if (with_core + 64 <= smem_budget(1)) {  // 64 bytes: the kernel's static shared memory
+      pl.fb_core_smem = 1;
+      pl.smem_fallback = with_core;
+    }
+  }
   int ctas_per_sm = pl.smem <= smem_budget(2) ? 2 : 1;
   if (sizeof(T) == 8) ctas_per_sm = 1;
   long grid = (long)num_sms * ctas_per_sm;
@@ -2519,7 +2552,8 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const Eliminat
     cudaFuncSetAttribute(k_lu_fallback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)pl.smem_fallback);
   k_lu_fallback<T><<<pl.fb_grid, pl.block, pl.smem_fallback, s>>>(
-      pl.m, pl.P, pl.mp, pl.dp, pl.fb_elems_per_cta, n, ep, sp, theta, theta_dm, scratch, logdet,
+      pl.m, pl.P, pl.mp, pl.dp, pl.fb_elems_per_cta, pl.fb_core_smem, n, ep, sp, theta, theta_dm,
+      scratch, logdet,
       draw_flags, x, lambda, key, y, rows, pivot_list);
 }
 

@@ -42,13 +42,19 @@ __global__ void __launch_bounds__(kSampleThreads)
     k_sample(int m, int P, long n, const double *__restrict__ m_t,
              const double *__restrict__ n_t, const double *__restrict__ s_t,
              const T *__restrict__ U, RngKey key, T *__restrict__ lambda,
-             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags) {
+             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags,
+             const unsigned *__restrict__ p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Us = reinterpret_cast<T *>(smem_raw);  // P*P, U[row + P*col]
   T *ms = Us + P * P;                       // P
   T *stage = ms + P;                        // blockDim.x * P
   __shared__ T ser[3];                      // the series' gamma shape and rate, s_j
   const int j = blockIdx.y;
+  // the series' active coefficients: U_j is zero outside its leading pj x pj
+  // block (the Cholesky factor's cut), so theta_k = m_k exactly for k >= pj and
+  // the normals z_l, l >= pj, are never used; they are not generated (counter-based
+  // streams: the others do not move)
+  const int pj = p ? min((int)p[j], P) : P;
   for (int e = threadIdx.x; e < P * P; e += blockDim.x) Us[e] = U[(size_t)j * P * P + e];
   for (int e = threadIdx.x; e < P; e += blockDim.x) ms[e] = (T)m_t[(size_t)j * P + e];
   if (threadIdx.x == 0) {
@@ -70,7 +76,7 @@ __global__ void __launch_bounds__(kSampleThreads)
     T z[PMAX];
 #pragma unroll
     for (int q = 0; q < PMAX / 4; ++q) {
-      if (4 * q < P) {
+      if (4 * q < pj) {
         const U4 r = philox((uint32_t)i, (uint32_t)j, tag_sub(TAG_THETA, q), ep, key.k0, key.k1);
         box_muller<T>(r.x, r.y, z[4 * q], z[4 * q + 1]);
         box_muller<T>(r.z, r.w, z[4 * q + 2], z[4 * q + 3]);
@@ -86,8 +92,10 @@ __global__ void __launch_bounds__(kSampleThreads)
     for (int k = 0; k < PMAX; ++k) {
       if (k < P) {
         T acc = T(0);
+        if (k < pj) {
 #pragma unroll
-        for (int l = 0; l <= k; ++l) acc += Us[l + P * k] * z[l];
+          for (int l = 0; l <= k; ++l) acc += Us[l + P * k] * z[l];
+        }
         row[k] = ms[k] + acc * rden;
       }
     }
@@ -211,7 +219,7 @@ template <typename T> size_t sample_smem(int P) {
 template <typename T>
 void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                    const double *n_t, const double *s_t, const T *U, RngKey key,
-                   T *lambda, T *theta, T *theta_dm, int *draw_flags) {
+                   T *lambda, T *theta, T *theta_dm, int *draw_flags, const unsigned *p) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
   const size_t smem = sample_smem<T>(P);
   if (smem > 48 * 1024) {
@@ -223,19 +231,19 @@ void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
   }
   if (P <= 8)
     k_sample<T, 8><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                      lambda, theta, theta_dm, draw_flags);
+                                                      lambda, theta, theta_dm, draw_flags, p);
   else if (P <= 16)
     k_sample<T, 16><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags);
+                                                       lambda, theta, theta_dm, draw_flags, p);
   else if (P <= 24)
     k_sample<T, 24><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags);
+                                                       lambda, theta, theta_dm, draw_flags, p);
   else if (P <= 32)
     k_sample<T, 32><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags);
+                                                       lambda, theta, theta_dm, draw_flags, p);
   else
     k_sample<T, 64><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags);
+                                                       lambda, theta, theta_dm, draw_flags, p);
 }
 
 template <typename T>
@@ -271,10 +279,11 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
 
 template void launch_sample<float>(cudaStream_t, int, int, long, const double *,
                                    const double *, const double *, const float *, RngKey,
-                                   float *, float *, float *, int *);
+                                   float *, float *, float *, int *, const unsigned *);
 template void launch_sample<double>(cudaStream_t, int, int, long, const double *,
                                     const double *, const double *, const double *,
-                                    RngKey, double *, double *, double *, int *);
+                                    RngKey, double *, double *, double *, int *,
+                                    const unsigned *);
 template void launch_evolve<float>(cudaStream_t, int, int, long, const unsigned *,
                                    const double *, const double *, const double *,
                                    const float *, RngKey, bool, bool, float *, float *,

@@ -31,6 +31,7 @@ pytestmark = pytest.mark.gpu
 def _engine_draws(m, P, p, sp, mt, C, n, precision="mixed", seed=17):
     s = SGDLM(1, strict=True, precision=precision)
     s.setSimultaneousParents(p, sp)
+    s.setWarpLu(False)  # the block LU kernels at every m, as the no-alloc path runs
     s.setEliminationLevels(0)  # the dense LU of the whole matrix, as the no-alloc path runs
     s.setDiscountFactors(np.full(m, 0.95), np.full((P, P, m), 0.95))
     s.setPosteriorParameters(mt, C, np.full(m, 20.0), np.full(m, 0.01))
