@@ -177,7 +177,8 @@ constexpr double kLevelMultMax = 65536.0;
 constexpr double kRefineTol = 1e-3;
 struct FallbackSmem {
   size_t off_pan, off_U, off_core, off_piv, off_pivabs, off_cand, off_D, off_z, off_d, off_perm,
-      off_nu, off_res, off_red, off_zf, off_yf, off_yd, total;
+      off_nu, off_res, off_red, off_zf, off_yf, off_yd, off_crow, off_ccv, off_cci, off_disp,
+      total;
   // core_dp > 0: the dense core (core_dp x core_dp) is factored in shared memory,
   // in a region that the full-matrix path's panel buffers share
   __host__ __device__ FallbackSmem(int mp, int m, size_t tsz, int core_dp = 0) {
@@ -196,6 +197,10 @@ struct FallbackSmem {
     off_piv = take((size_t)kB * sizeof(int));
     off_pivabs = take((size_t)mp * tsz);
     off_cand = take((size_t)2 * kWarps * (tsz > 4 ? tsz : 4));
+    off_crow = take((size_t)2 * kWarps * kB * tsz);
+    off_ccv = take((size_t)2 * kWarps * tsz);
+    off_cci = take((size_t)2 * kWarps * sizeof(int));
+    off_disp = take((size_t)kB * sizeof(int));
     off_D = take((size_t)kB * (kB + 1) * tsz);
     off_z = take((size_t)mp * tsz);
     off_d = take((size_t)mp * tsz);
@@ -2090,7 +2095,118 @@ template <typename T> struct FbBufs {
   T *pan, *Uc, *pivabs, *cand_v, *z;
   int *piv, *cand_i, *perm;
   bool *singular;
+  // the register panel's exchange: per warp and column parity its best candidate
+  // (|value|, row) and that row's 32 values; the displaced rows' positions
+  T *crow, *ccv;
+  int *cci, *disp;
 };
+
+// Factors the Rp x 32 panel pan (column-major, stride N, Rp <= blockDim.x) with
+// partial pivoting, one row per thread held in registers and one barrier per
+// column: each warp publishes its best candidate for the next column together
+// with that row's values while the current column's update runs, so that after
+// the barrier every thread knows the pivot row and reads it by broadcast.  Rows
+// stay in their registers; warp 0 tracks the row interchanges (b.piv, LAPACK's
+// ipiv relative to the panel) and the panel is written back in pivot order.
+// pivabs[0..32) receives |u_jj|.  Returns true (uniform) at a zero or
+// non-finite pivot column, the panel then left as it was.
+template <typename T>
+__device__ bool panel_regs(T *__restrict__ pan, int N, int Rp, T *__restrict__ pivabs,
+                           const FbBufs<T> &b) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const int r = tid;
+  const bool row_ok = r < Rp;
+  T a[kB];
+#pragma unroll
+  for (int c = 0; c < kB; ++c) a[c] = row_ok ? pan[c * N + r] : T(0);
+  bool done = !row_ok;
+  int pos = -1;
+  // warp 0's lanes: at = panel row now at position `lane`, dp = position of
+  // panel row `lane` (rows >= 32 only move when chosen)
+  int at = lane, dp = lane;
+  auto key = [](T v) { return v == v ? dabs(v) : T(INFINITY); };
+  auto publish = [&](int c, int par) {
+    T v = done ? T(-1) : key(a[c]);
+    int vi = r;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const T ov = __shfl_xor_sync(kFull, v, o);
+      const int oi = __shfl_xor_sync(kFull, vi, o);
+      if (ov > v || (ov == v && oi < vi)) {
+        v = ov;
+        vi = oi;
+      }
+    }
+    if (lane == 0) {
+      b.ccv[par * kWarps + warp] = v;
+      b.cci[par * kWarps + warp] = vi;
+    }
+    if (vi == r && v >= T(0)) {
+      T *dst = b.crow + (size_t)(par * kWarps + warp) * kB;
+#pragma unroll
+      for (int q = 0; q < kB; ++q) dst[q] = a[q];
+    }
+  };
+  publish(0, 0);
+  __syncthreads();
+  bool sing = false;
+#pragma unroll
+  for (int j = 0; j < kB; ++j) {
+    const int par = j & 1;
+    // the pivot: the best of the warps' candidates (ties -> lowest row)
+    T bv = lane < nwarps ? b.ccv[par * kWarps + lane] : T(-2);
+    int p = lane < nwarps ? b.cci[par * kWarps + lane] : 0x7fffffff;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      const T ov = __shfl_xor_sync(kFull, bv, o);
+      const int oi = __shfl_xor_sync(kFull, p, o);
+      if (ov > bv || (ov == bv && oi < p)) {
+        bv = ov;
+        p = oi;
+      }
+    }
+    bv = __shfl_sync(kFull, bv, 0);  // lanes 0..7 hold the warps' candidates
+    p = __shfl_sync(kFull, p, 0);
+    sing = sing || !(bv > T(0)) || !(bv <= (T)3.0e38);
+    if (!sing) {
+      const T *u = b.crow + (size_t)(par * kWarps + (p >> 5)) * kB;
+      const T pv = u[j];
+      if (tid == 0) pivabs[j] = dabs(pv);
+      if (r == p) {
+        done = true;
+        pos = j;
+      } else if (!done) {
+        const T l = a[j] / pv;
+        a[j] = l;
+#pragma unroll
+        for (int c = j + 1; c < kB; ++c) a[c] -= l * u[c];
+      }
+      if (warp == 0) {
+        // interchange j <-> q, q the chosen row's current position
+        const int q = p < kB ? __shfl_sync(kFull, dp, p) : p;
+        const int x = __shfl_sync(kFull, at, j);  // the row leaving position j
+        if (lane == x) dp = q;
+        if (q < kB && lane == q) at = x;
+        if (lane == j) at = p;
+        if (p < kB && lane == p) dp = j;
+        if (lane == 0) b.piv[j] = q;
+      }
+      if (j + 1 < kB) publish(j + 1, par ^ 1);
+    }
+    __syncthreads();
+  }
+  if (sing) return true;
+  if (warp == 0) b.disp[lane] = dp;
+  __syncthreads();
+  if (row_ok) {
+    const int f = done ? pos : (r < kB ? b.disp[r] : r);
+#pragma unroll
+    for (int c = 0; c < kB; ++c) pan[c * N + f] = a[c];
+  }
+  __syncthreads();
+  return false;
+}
 
 // LU with partial pivoting of the N x N column-major matrix A (N a multiple of
 // 32) in place; perm records the row permutation and, when `rhs`, z (length N)
@@ -2121,6 +2237,12 @@ __device__ bool pivot_lu(T *__restrict__ A, int N, bool rhs, const FbBufs<T> &b)
       }
       __syncthreads();
     }
+    if (Rp <= (int)blockDim.x) {
+      if (panel_regs<T>(pan, N, Rp, b.pivabs + k0, b)) {
+        if (tid == 0) *b.singular = true;
+        __syncthreads();
+      }
+    } else
     for (int j = 0; j < kB; ++j) {
       // pivot search in the working precision (ties -> lowest row)
       T best = T(-1);
@@ -2273,6 +2395,10 @@ __global__ void __launch_bounds__(kThreads)
   b.z = reinterpret_cast<T *>(smem_raw + L.off_z);
   b.perm = reinterpret_cast<int *>(smem_raw + L.off_perm);
   b.singular = &s_singular;
+  b.crow = reinterpret_cast<T *>(smem_raw + L.off_crow);
+  b.ccv = reinterpret_cast<T *>(smem_raw + L.off_ccv);
+  b.cci = reinterpret_cast<int *>(smem_raw + L.off_cci);
+  b.disp = reinterpret_cast<int *>(smem_raw + L.off_disp);
   double *nu = reinterpret_cast<double *>(smem_raw + L.off_nu);
   double *res = reinterpret_cast<double *>(smem_raw + L.off_res);
   double *red = reinterpret_cast<double *>(smem_raw + L.off_red);  // 64 doubles

@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(128)
                 const T *__restrict__ U, const double *__restrict__ mq, const double *__restrict__ nq,
                 const double *__restrict__ sq, const T *__restrict__ Uq,
                 const double *__restrict__ cst, double *__restrict__ lr) {
-  __shared__ T Us[PMAX * PMAX], Uqs[PMAX * PMAX], ms[PMAX], mqs[PMAX];
+  __shared__ T Us[PMAX * PMAX], Uqs[PMAX * PMAX], ms[PMAX], mqs[PMAX], rd[PMAX], rdq[PMAX];
   const int j = blockIdx.y;
   const int pj = (int)p[j];
   for (int e = threadIdx.x; e < P * P; e += blockDim.x) {
@@ -209,6 +209,9 @@ __global__ void __launch_bounds__(128)
   for (int e = threadIdx.x; e < P; e += blockDim.x) {
     ms[e] = (T)m_t[(size_t)j * P + e];
     mqs[e] = (T)mq[(size_t)j * P + e];
+    // the diagonals' reciprocals, once per series (the solves multiply)
+    rd[e] = T(1) / U[(size_t)j * P * P + e + P * e];
+    rdq[e] = T(1) / Uq[(size_t)j * P * P + e + P * e];
   }
   __syncthreads();
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -226,17 +229,21 @@ __global__ void __launch_bounds__(128)
         ap -= Us[l + P * k] * wp[l];
         aq -= Uqs[l + P * k] * wq[l];
       }
-      wp[k] = ap / Us[k + P * k];
-      wq[k] = aq / Uqs[k + P * k];
+      wp[k] = ap * rd[k];
+      wq[k] = aq * rdq[k];
       qp += wp[k] * wp[k];
       qq += wq[k] * wq[k];
     } else {
       wp[k] = wq[k] = T(0);
     }
   }
-  const double lam = (double)lambda[(size_t)j * n + i];
+  const T lamt = lambda[(size_t)j * n + i];
+  const double lam = (double)lamt;
   const double nn = n_t[j], ss = s_t[j], n2 = nq[j], s2 = sq[j];
-  lr[(size_t)j * n + i] = cst[j] + 0.5 * (nn - n2) * log(lam) - 0.5 * (nn * ss - n2 * s2) * lam -
+  // log(lambda) in the draws' precision: FP32 draws carry 2^-24 of lambda anyway,
+  // and the FP64 logarithm is the kernel's most expensive operation on GB300
+  const double loglam = (double)dev_log(lamt);
+  lr[(size_t)j * n + i] = cst[j] + 0.5 * (nn - n2) * loglam - 0.5 * (nn * ss - n2 * s2) * lam -
                           0.5 * lam * (ss * (double)qp - s2 * (double)qq);
 }
 
