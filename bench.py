@@ -449,7 +449,8 @@ def run_c4(args):
                 pv = plain_at.computeVBPosterior(n, n)
                 sd = np.sqrt(np.stack([np.diag(ref["C"][:, :, j]) for j in range(m)], 1))
                 for key, v in (("learned", vb), ("plain", pv)):
-                    errs[key].append(float(np.sqrt(np.mean(((v["m"] - ref["m"]) / sd)[mask] ** 2))))
+                    z = (v["m"] - ref["m"])[mask] / sd[mask]  # active coefficients only
+                    errs[key].append(float(np.sqrt(np.mean(z ** 2))))
             if 1.0 / np.sum(vb["IS_weights"] ** 2) > n / 2:
                 s.setPosteriorParameters(vb["m"], vb["C"], vb["n"], vb["s"])
             s.computePrior()
