@@ -1478,6 +1478,145 @@ __device__ __forceinline__ void level_forward(const EliminationPlan &ep, int lev
   }
 }
 
+// The value slots of draw i before the levels: the constants, the unit diagonal
+// and the level-0 entries -theta (each thread's sixteen gathers in flight at once).
+template <typename T>
+__device__ __forceinline__ void build_slots(const EliminationPlan &ep, int m, long i,
+                                            const Theta<T> &theta, T *vals) {
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    vals[kSlotZero] = T(0);
+    vals[kSlotOne] = T(1);
+  }
+  for (int r = tid; r < m; r += blockDim.x) vals[ep.diag_slot[r]] = T(1);
+  for (int k0 = tid; k0 < ep.nnz0; k0 += 16 * kThreads) {
+    int e[16], sl[16];
+#pragma unroll
+    for (int h = 0; h < 16; ++h) {
+      const bool ok = k0 + h * kThreads < ep.nnz0;
+      e[h] = ok ? ep.l0_e[k0 + h * kThreads] : -1;
+      sl[h] = ok ? ep.l0_slot[k0 + h * kThreads] : 0;
+    }
+    T th[16];
+#pragma unroll
+    for (int h = 0; h < 16; ++h) th[h] = e[h] >= 0 ? theta.at(i, e[h]) : T(0);
+#pragma unroll
+    for (int h = 0; h < 16; ++h)
+      if (e[h] >= 0) vals[sl[h]] = -th[h];
+  }
+}
+
+// The sparse levels over the value slots `vals` (shared memory, or global when
+// they do not fit), as the pivoting redo runs them (k_lu has the same loop
+// inline): per level the pivots (sum log|pivot| into ld_part; a zero or
+// non-finite pivot sets bad), the multipliers (bad above tau), a barrier, then the
+// new entries, and a barrier.  A warp takes chunks c_begin + w + 8i; lane l
+// prefetches the term offsets of its warp's chunk i = base + l, so that the term
+// loads do not wait on a dependent load; kLevFlight chunks are in flight at a
+// time (the plan's words come from L2: the rounds are latency-bound).  With zf,
+// the right-hand side's forward program of each level rides along.
+template <typename T>
+__device__ __forceinline__ void run_levels(const EliminationPlan &ep, T *vals, T tau, bool &bad,
+                                           double &ld_part, T *zf) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int lev = 0; lev < ep.nlev; ++lev) {
+    for (int q = ep.lev_piv[lev] + tid; q < ep.lev_piv[lev + 1]; q += blockDim.x) {
+      const T pv = vals[ep.piv[q]];
+      if (!(finite_t(pv) && pv != T(0))) bad = true;
+      ld_part += log_abs(pv);
+    }
+    for (int q = ep.lev_scale[lev] + tid; q < ep.lev_scale[lev + 1]; q += blockDim.x) {
+      const unsigned w = ep.scale[q];
+      const T l = vals[lo16(w)] / vals[hi16(w)];
+      if (!(dabs(l) <= tau)) bad = true;
+      vals[lo16(w)] = l;
+    }
+    __syncthreads();
+    // new entries
+    const int c_begin = ep.lev_chunk[lev], c_end = ep.lev_chunk[lev + 1];
+    const int n_w = (c_begin + warp < c_end) ? (c_end - c_begin - warp + kWarps - 1) / kWarps : 0;
+    for (int base = 0; base < n_w; base += 32) {
+      int my_t0 = 0, my_t1 = 0;
+      if (base + lane < n_w) {
+        const int ci = c_begin + warp + (base + lane) * kWarps;
+        my_t0 = ep.chunk_tofs[ci];
+        my_t1 = ep.chunk_tofs[ci + 1];
+      }
+      const int n_here = min(32, n_w - base);
+      for (int i0 = 0; i0 < n_here; i0 += kLevFlight) {
+        unsigned e[kLevFlight];
+        int toff[kLevFlight], K[kLevFlight];
+#pragma unroll
+        for (int h = 0; h < kLevFlight; ++h) {
+          const int ii = i0 + h;
+          const int t0 = __shfl_sync(kFull, my_t0, ii & 31);
+          const int t1 = __shfl_sync(kFull, my_t1, ii & 31);
+          const bool ok = ii < n_here;
+          const int ch = c_begin + warp + (base + ii) * kWarps;
+          e[h] = ok ? __ldg(ep.ent + (size_t)ch * 32 + lane) : kSlotNone;  // none: no store, base 0
+          K[h] = ok ? (t1 - t0) >> 5 : 0;
+          toff[h] = t0 + lane;
+        }
+        // the first term's word is loaded before the entry word is first used, so
+        // that the two loads from L2 overlap (most entries have one term)
+        unsigned w0[kLevFlight];
+#pragma unroll
+        for (int h = 0; h < kLevFlight; ++h) w0[h] = K[h] > 0 ? __ldg(ep.terms + toff[h]) : 0u;
+        T v[kLevFlight];
+        int Kmax = 0;
+#pragma unroll
+        for (int h = 0; h < kLevFlight; ++h) {
+          v[h] = vals[hi16(e[h])] - vals[lo16(w0[h])] * vals[hi16(w0[h])];
+          Kmax = max(Kmax, K[h]);
+        }
+#pragma unroll 1
+        for (int k = 1; k < Kmax; ++k) {
+          unsigned w[kLevFlight];
+#pragma unroll
+          for (int h = 0; h < kLevFlight; ++h) w[h] = (k < K[h]) ? __ldg(ep.terms + toff[h] + 32 * k) : 0u;
+#pragma unroll
+          for (int h = 0; h < kLevFlight; ++h) v[h] -= vals[lo16(w[h])] * vals[hi16(w[h])];
+        }
+#pragma unroll
+        for (int h = 0; h < kLevFlight; ++h)
+          if ((unsigned)lo16(e[h]) != kSlotNone) vals[lo16(e[h])] = v[h];
+      }
+    }
+    if (zf) level_forward<T>(ep, lev, vals, zf);
+    __syncthreads();
+  }
+}
+
+// The dense core (d_p x d_p, column-major) from the value slots through the
+// plan's slot map: four cells per 8-byte map word pair, eight pairs in flight
+// per thread.
+template <typename T>
+__device__ __forceinline__ void scatter_core(const EliminationPlan &ep, int dp, const T *vals,
+                                             T *__restrict__ A) {
+  using V = Vec<T>;
+  constexpr int W = V::W;
+  const int tid = threadIdx.x;
+  const uint2 *map4 = reinterpret_cast<const uint2 *>(ep.core_map);
+  const int nq = dp * dp / 4;
+  for (int q0 = tid; q0 < nq; q0 += 8 * kThreads) {
+    uint2 w[8];
+#pragma unroll
+    for (int h = 0; h < 8; ++h) {
+      const int q = q0 + h * kThreads;
+      w[h] = q < nq ? map4[q] : make_uint2(0u, 0u);
+    }
+#pragma unroll
+    for (int h = 0; h < 8; ++h) {
+      const int q = q0 + h * kThreads;
+      if (q < nq) {
+        T v4[4] = {vals[lo16(w[h].x)], vals[hi16(w[h].x)], vals[lo16(w[h].y)], vals[hi16(w[h].y)]};
+#pragma unroll
+        for (int g = 0; g < 4; g += W) V::st(A + (size_t)q * 4 + g, v4 + g);
+      }
+    }
+  }
+}
+
 template <typename T>
 __device__ void levels_forward(const EliminationPlan &ep, const T *vals, T *z) {
   for (int lev = 0; lev < ep.nlev; ++lev) {
@@ -1694,7 +1833,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
       }
     }
     __syncthreads();
-    // ---- sparse levels
+    // ---- sparse levels (the loop of run_levels, kept inline here: through the
+    // function this kernel measured 2 % slower)
     for (int lev = 0; lev < ep.nlev; ++lev) {
       for (int q = ep.lev_piv[lev] + tid; q < ep.lev_piv[lev + 1]; q += blockDim.x) {
         const T pv = vals[ep.piv[q]];
@@ -2412,6 +2552,8 @@ __global__ void __launch_bounds__(kThreads)
   T *vals = A + (size_t)dp * dp;  // the levels' value slots (core path)
   const bool solve = (x != nullptr);
   const bool planned = (ep.core_map != nullptr);
+  // the levels' value slots fit the core's region (d_p^2 values, rounded copies)
+  const bool lvals_smem = planned && core_smem && ((ep.nv + 3) / 4) * 4 <= dp * dp;
 
   // the flagged draws: the fast pass's list, or all n draws' flags
   const long cnt = pivot_list ? min((long)pivot_list[0], n) : n;
@@ -2425,46 +2567,19 @@ __global__ void __launch_bounds__(kThreads)
     double ld_part = 0.0;
     bool core = planned;
     if (planned) {
-      // ---- the sparse levels, without pivoting
-      if (tid == 0) {
-        vals[kSlotZero] = T(0);
-        vals[kSlotOne] = T(1);
-        s_level_bad = 0;
-      }
-      for (int r = tid; r < m; r += blockDim.x) {
-        vals[ep.diag_slot[r]] = T(1);
-        if (solve) zf[r] = (T)nu[r];
-      }
-      for (int k = tid; k < ep.nnz0; k += blockDim.x) vals[ep.l0_slot[k]] = -theta.at(i, ep.l0_e[k]);
+      // ---- the sparse levels, without pivoting: the value slots in the dense
+      // core's shared-memory region while the levels run (the core is formed
+      // after them), then copied out for the scatter and the solves
+      T *lv = lvals_smem ? reinterpret_cast<T *>(smem_raw + L.off_core) : vals;
+      if (tid == 0) s_level_bad = 0;
+      build_slots<T>(ep, m, i, theta, lv);
+      if (solve)
+        for (int r = tid; r < m; r += blockDim.x) zf[r] = (T)nu[r];
       __syncthreads();
       bool bad = false;
-      for (int lev = 0; lev < ep.nlev; ++lev) {
-        for (int g = ep.lev_piv[lev] + tid; g < ep.lev_piv[lev + 1]; g += blockDim.x) {
-          const T pv = vals[ep.piv[g]];
-          if (!(finite_t(pv) && pv != T(0))) bad = true;
-          ld_part += log_abs(pv);
-        }
-        for (int g = ep.lev_scale[lev] + tid; g < ep.lev_scale[lev + 1]; g += blockDim.x) {
-          const unsigned w = ep.scale[g];
-          const T l = vals[lo16(w)] / vals[hi16(w)];
-          if (!(dabs(l) <= (T)kLevelMultMax)) bad = true;
-          vals[lo16(w)] = l;
-        }
-        __syncthreads();
-        // new entries: one chunk of 32 entries per warp at a time, lane l its entry
-        for (int ch = ep.lev_chunk[lev] + (tid >> 5); ch < ep.lev_chunk[lev + 1]; ch += kWarps) {
-          const int lane = tid & 31;
-          const unsigned e = ep.ent[(size_t)ch * 32 + lane];
-          const int t0 = ep.chunk_tofs[ch], K = (ep.chunk_tofs[ch + 1] - t0) >> 5;
-          T v = vals[hi16(e)];
-          for (int k = 0; k < K; ++k) {
-            const unsigned w = ep.terms[t0 + 32 * k + lane];
-            v -= vals[lo16(w)] * vals[hi16(w)];
-          }
-          if ((unsigned)lo16(e) != kSlotNone) vals[lo16(e)] = v;
-        }
-        __syncthreads();
-        if (solve) level_forward<T>(ep, lev, vals, zf);
+      run_levels<T>(ep, lv, (T)kLevelMultMax, bad, ld_part, solve ? zf : nullptr);
+      if (lv != vals) {
+        copy_vals<T>(vals, lv, ep.nv);
         __syncthreads();
       }
       if (bad) atomicOr(&s_level_bad, 1);
@@ -2478,7 +2593,7 @@ __global__ void __launch_bounds__(kThreads)
     if (core) {
       // ---- dense core through the slot map; its right-hand side
       N = dp;
-      for (int qq = tid; qq < dp * dp; qq += blockDim.x) F[qq] = vals[ep.core_map[qq]];
+      scatter_core<T>(ep, dp, vals, F);
       if (solve)
         for (int r = tid; r < dp; r += blockDim.x) b.z[r] = (r < ep.core_n) ? zf[ep.core_node[r]] : T(0);
       __syncthreads();
@@ -2619,15 +2734,11 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solv
   pl.scratch_elems_per_cta = (size_t)pl.dp * pl.dp + (((size_t)nv + 3) / 4) * 4;
   const size_t total = pl.scratch_elems_per_cta * pl.grid;
   // the redo needs the dense core and the value slots, or a full m_p x m_p slab,
-  // per CTA; it shares the slab array
+  // per CTA; it shares the slab array, which grows to one slab per SM for it
   const size_t full = std::max((size_t)pl.mp * pl.mp, pl.scratch_elems_per_cta);
   pl.fb_elems_per_cta = full;
   long fb = num_sms;
   if (fb > n) fb = n;
-  if ((size_t)fb * full > total) {
-    const long fit = (long)(total / full);
-    fb = std::max(fit, std::min(fb, 16L));
-  }
   if (fb < 1) fb = 1;
   pl.fb_grid = (int)fb;
   pl.scratch_elems_total = std::max(total, (size_t)pl.fb_grid * full);
