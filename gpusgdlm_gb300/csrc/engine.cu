@@ -124,6 +124,7 @@ struct sgdlm_engine {
   DevBuf<unsigned> p, sp;
   DevBuf<int> g_rowptr;
   DevBuf<int2> g_ent;
+  DevBuf<int> g_jac_order;  // the rows by decreasing length (iterative forecast solves)
   DevBuf<int> g_extptr, g_extk;
   // evolution matrices G (P x P x m, FP64 and the FP32 copy the draws use)
   DevBuf<double> G_t;
@@ -277,7 +278,15 @@ int upload_gamma_rows(sgdlm_engine *h) {
   CK(cudaMemcpy(h->g_extk.ptr, extk.data(), extk.size() * sizeof(int), cudaMemcpyHostToDevice));
   int max_row = 0;
   for (size_t r = 0; r < m; ++r) max_row = std::max(max_row, rowptr[r + 1] - rowptr[r]);
+  std::vector<int> order(m);
+  for (size_t r = 0; r < m; ++r) order[r] = (int)r;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return rowptr[a + 1] - rowptr[a] > rowptr[b + 1] - rowptr[b];
+  });
+  CK(h->g_jac_order.alloc(m));
+  CK(cudaMemcpy(h->g_jac_order.ptr, order.data(), m * sizeof(int), cudaMemcpyHostToDevice));
   h->jac = plan_jacobi((int)m, max_row, h->num_sms);
+  h->jac.order = h->g_jac_order.ptr;
   return SGDLM_OK;
 }
 
@@ -432,6 +441,7 @@ void release_all(sgdlm_engine *h) {
   h->sp.release();
   h->g_rowptr.release();
   h->g_ent.release();
+  h->g_jac_order.release();
   h->g_extptr.release();
   h->g_extk.release();
   h->G_t.release();

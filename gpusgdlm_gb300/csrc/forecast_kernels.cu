@@ -85,12 +85,14 @@ template <int K> struct Row {
   }
 };
 
-// Sweeps x <- c + Gamma x from x = c.  Returns whether they converged
-// (max|dx| <= tol max|x|, everything finite); *out is the last iterate.
+// Sweeps x <- c + Gamma x from x = c over this thread's row r.  Returns whether
+// they converged (max|dx| <= tol max|x|, everything finite); *out is the last
+// iterate.  wlen: the longest row of this warp, rounded up to even (warp-uniform):
+// slots beyond it are padding in every row of the warp (value 0, so skipping them
+// leaves every sum unchanged).
 template <int K>
-__device__ bool jacobi(int m, const Row<K> &R, const float *c, float *xa, float *xb, float *red,
-                       float tol, float **out) {
-  const int r = threadIdx.x;
+__device__ bool jacobi(int m, int r, int wlen, const Row<K> &R, const float *c, float *xa,
+                       float *xb, float *red, float tol, float **out) {
   if (r < m) xa[r] = c[r];
   __syncthreads();
   float *cur = xa, *nxt = xb;
@@ -100,13 +102,15 @@ __device__ bool jacobi(int m, const Row<K> &R, const float *c, float *xa, float 
       float a0 = c[r], a1 = 0.f;
 #pragma unroll
       for (int q = 0; q < K; q += 2) {
+        if (q >= wlen) break;
         a0 = fmaf(R.val[q], cur[R.c(q)], a0);
         a1 = fmaf(R.val[q + 1], cur[R.c(q + 1)], a1);
       }
       const float v = a0 + a1;
       nxt[r] = v;
       // fmaxf drops NaN operands: a NaN (an overflowed iterate times a padded
-      // zero slot) must count as divergence, so it becomes infinity here
+      // zero slot, or inf - inf) must count as divergence, so it becomes infinity
+      // here
       const float av = fabsf(v), dv = fabsf(v - cur[r]);
       xmax = (av == av) ? av : INFINITY;
       dmax = (dv == dv) ? dv : INFINITY;
@@ -133,7 +137,8 @@ template <int K>
 __global__ void __launch_bounds__(kJacMaxThreads)
     k_forecast_jacobi(int m, int P, long n, GammaRows rows, const float *__restrict__ theta_dm,
                       const double *__restrict__ nu, double *__restrict__ y,
-                      double *__restrict__ logdet, int *__restrict__ list) {
+                      double *__restrict__ logdet, int *__restrict__ list,
+                      const int *__restrict__ order) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const JacSmem L(m);
   double *nud = reinterpret_cast<double *>(smem_raw + L.nud);
@@ -142,10 +147,12 @@ __global__ void __launch_bounds__(kJacMaxThreads)
   float *yb = reinterpret_cast<float *>(smem_raw + L.yb);
   float *res = reinterpret_cast<float *>(smem_raw + L.res);
   float *red = reinterpret_cast<float *>(smem_raw + L.red);
-  const int tid = threadIdx.x, r = tid;
+  const int tid = threadIdx.x;
+  const int r = (tid < m && order) ? order[tid] : tid;  // this thread's row (r >= m: none)
   Row<K> R;
   const int e0 = r < m ? rows.rowptr[r] : 0;
   const int len = r < m ? rows.rowptr[r + 1] - e0 : 0;
+  const int wlen = (__reduce_max_sync(0xffffffffu, (unsigned)len) + 1) & ~1;
 #pragma unroll
   for (int q = 0; q < K; q += 2) {
     const uint32_t self = (uint32_t)(r < m ? r : 0);
@@ -166,7 +173,7 @@ __global__ void __launch_bounds__(kJacMaxThreads)
     }
     __syncthreads();
     float *yv = nullptr;
-    bool ok = jacobi<K>(m, R, nuf, ya, yb, red, kSweepTol, &yv);
+    bool ok = jacobi<K>(m, r, wlen, R, nuf, ya, yb, red, kSweepTol, &yv);
     if (ok) {
       // residual in FP64 and its correction by the same iteration
       float *other = (yv == ya) ? yb : ya;
@@ -180,7 +187,7 @@ __global__ void __launch_bounds__(kJacMaxThreads)
       // the correction's iterates go to `other` and nuf (nu's FP32 copy is no
       // longer needed); yv keeps y
       float *dv = nullptr;
-      ok = jacobi<K>(m, R, res, other, nuf, red, kCorrSweepTol, &dv);
+      ok = jacobi<K>(m, r, wlen, R, res, other, nuf, red, kCorrSweepTol, &dv);
       float dmax = 0.f, ymax = 0.f;
       if (r < m) {
         const float ad = fabsf(dv[r]), ay = fabsf(yv[r]);
@@ -250,7 +257,8 @@ void launch_forecast_jacobi(cudaStream_t s, const JacobiPlan &jp, int m, int P, 
   const unsigned grid = (unsigned)std::max<long>(std::min<long>(jp.grid, n), 1);
   const unsigned th = (unsigned)jp.threads;
 #define SGDLM_JACOBI(K)                                                                    \
-  k_forecast_jacobi<K><<<grid, th, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list)
+  k_forecast_jacobi<K><<<grid, th, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list, \
+                                                 jp.order)
   switch (jp.nnz) {
     case 8: SGDLM_JACOBI(8); break;
     case 12: SGDLM_JACOBI(12); break;

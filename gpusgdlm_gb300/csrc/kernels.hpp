@@ -148,6 +148,10 @@ void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan
 struct JacobiPlan {
   int ok, grid, threads, nnz;  // threads: m rounded up to 32; nnz: ELL slots per row (8..32)
   size_t smem;
+  // thread t takes row order[t] (the rows by decreasing length, so that a warp's
+  // rows are of similar length and its sweeps stop at its own longest row), or
+  // nullptr: thread t takes row t
+  const int *order;
 };
 // m <= 1024 and at most 32 simultaneous parents per series, else ok = 0.
 JacobiPlan plan_jacobi(int m, int max_row, int num_sms);
