@@ -723,37 +723,35 @@ __device__ __forceinline__ void named_sync_n(int id, int n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
-// The two-tile update's product -L U (this warp's lanes, columns [cb, ce)) is
-// added to E in global memory in 8-column chunks: the E values of the next chunk
-// are loaded while the current one is added (the first chunk is loaded before
-// the MMA wait).  Not inlined: its registers stay out of the kernel's peak.  Rows
-// at or beyond R are padding: loaded as 0, never stored.
-constexpr int kEc = 8;
-__device__ __forceinline__ void e_chunk_load(const float *E, int dp, int R, int row, int c0,
-                                             float (&e)[kEc]) {
-#pragma unroll
-  for (int j = 0; j < kEc; ++j) e[j] = row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f;
+// 16 columns of tensor memory at taddr into v.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
 }
+// The two-tile update's product -L U (this warp's lanes, columns [cb, ce), a
+// multiple of 16 wide) is added to E in global memory in 16-column chunks: a
+// chunk's E loads and its tensor-memory read are issued together and waited for
+// once (8-column chunks, each loaded one chunk ahead, took 1 % longer per VB pass;
+// 32-column chunks spill).  Not inlined: its registers stay out of the kernel's
+// peak.  Rows at or beyond R are padding: never loaded or stored.
 __device__ __noinline__ void tmem_add_e(float *E, int dp, int R, int row, int cb, int ce,
-                                        uint32_t tlane, float (&e0)[kEc]) {
-  for (int c0 = cb; c0 < ce; c0 += kEc) {
-    float e1[kEc];
-    if (c0 + kEc < ce) e_chunk_load(E, dp, R, row, c0 + kEc, e1);
-    uint32_t v[kEc];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-          "=r"(v[7])
-        : "r"(tlane + (uint32_t)c0));
+                                        uint32_t tlane) {
+  for (int c0 = cb; c0 < ce; c0 += 16) {
+    float e[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) e[j] = row < R ? E[(size_t)row + (size_t)dp * (c0 + j)] : 0.f;
+    uint32_t v[16];
+    tmem_ld16(tlane + (uint32_t)c0, v);
     asm volatile("tcgen05.wait::ld.sync.aligned;");
     if (row < R) {
 #pragma unroll
-      for (int j = 0; j < kEc; ++j)
-        E[(size_t)row + (size_t)dp * (c0 + j)] = __fadd_rn(e0[j], __uint_as_float(v[j]));
-    }
-    if (c0 + kEc < ce) {
-#pragma unroll
-      for (int j = 0; j < kEc; ++j) e0[j] = e1[j];
+      for (int j = 0; j < 16; ++j)
+        E[(size_t)row + (size_t)dp * (c0 + j)] = __fadd_rn(e[j], __uint_as_float(v[j]));
     }
   }
 }
@@ -779,16 +777,6 @@ __device__ __forceinline__ void e_to_tmem(const float *E, int dp, int R, int row
         "r"(v[15]));
   }
   asm volatile("tcgen05.wait::st.sync.aligned;");
-}
-// 16 columns of tensor memory at taddr into v.
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-        "=r"(v[14]), "=r"(v[15])
-      : "r"(taddr));
 }
 // E = E + (-L U), both in tensor memory, columns [cb, ce) of this warp's lanes,
 // stored to global (rows at or beyond R are not stored).
@@ -945,17 +933,11 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
           *dst = d;
         }
       }
-      if (kB < ce) {  // the rest of warp 0's half
-        float e0[kEc];
-        e_chunk_load(E, dp, R, row, kB, e0);
-        tmem_add_e(E, dp, R, row, kB, ce, tlane, e0);
-      }
+      if (kB < ce) tmem_add_e(E, dp, R, row, kB, ce, tlane);  // the rest of warp 0's half
     } else {
-      float e0[kEc];
       const bool mine = quarter * 32 < R && cb < ce;
-      if (mine) e_chunk_load(E, dp, R, row, cb, e0);
       mma_wait(mbar, mphase, bad);
-      if (mine) tmem_add_e(E, dp, R, row, cb, ce, tlane, e0);
+      if (mine) tmem_add_e(E, dp, R, row, cb, ce, tlane);
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
@@ -972,11 +954,9 @@ __device__ void tc_trailing_update(float *__restrict__ A, int dp, int r0, int R,
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
               smem_u32(&mbar->bar)));
     }
-    float e0[kEc];
     const bool mine = 128 + quarter * 32 < R && cb < ce;
-    if (mine) e_chunk_load(E, dp, R, row, cb, e0);
     mma_wait(mbar, mphase, bad);
-    if (mine) tmem_add_e(E, dp, R, row, cb, ce, tlane, e0);
+    if (mine) tmem_add_e(E, dp, R, row, cb, ce, tlane);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
