@@ -141,7 +141,10 @@ struct sgdlm_engine {
   DevBuf<float> U32;
   std::vector<unsigned> h_p, h_sp;
   // simulation
-  DevBuf<unsigned char> lambda, theta, theta_dm, lu_scratch;
+  DevBuf<unsigned char> lambda, theta, lu_scratch;
+  // the draws' Gamma entries draw-major (GammaDraws), room for m * P per draw
+  DevBuf<unsigned char> theta_g;
+  int g_nnz = 0;  // Gamma entries (rows' CSR length)
   DevBuf<double> logdet, w, y_fc, nu_fc, stats6, wpart, part_a, part_b;
   DevBuf<int> draw_flags, series_flags;
   DevBuf<int> pivot_list;  // nsim + 1: count, then the draws flagged for the redo
@@ -276,6 +279,7 @@ int upload_gamma_rows(sgdlm_engine *h) {
   CK(h->g_extk.alloc(extk.size()));
   CK(cudaMemcpy(h->g_extptr.ptr, extptr.data(), (m + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->g_extk.ptr, extk.data(), extk.size() * sizeof(int), cudaMemcpyHostToDevice));
+  h->g_nnz = rowptr[m];
   int max_row = 0;
   for (size_t r = 0; r < m; ++r) max_row = std::max(max_row, rowptr[r + 1] - rowptr[r]);
   std::vector<int> order(m);
@@ -414,7 +418,7 @@ int alloc_state(sgdlm_engine *h) {
 void release_sim(sgdlm_engine *h) {
   h->lambda.release();
   h->theta.release();
-  h->theta_dm.release();
+  h->theta_g.release();
   h->lu_scratch.release();
   h->logdet.release();
   h->w.release();
@@ -484,7 +488,7 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   vb_chunking((long)nsim, (int)m, h->num_sms, &h->chunks, &h->chunk_draws);
   CK(h->lambda.alloc(m * nsim * ts));
   CK(h->theta.alloc(m * nsim * P * ts));
-  CK(h->theta_dm.alloc(m * nsim * P * ts));
+  CK(h->theta_g.alloc(m * nsim * P * ts));
   CK(h->lu_scratch.alloc(pl.scratch_elems_total * ts));
   CK(h->logdet.alloc(nsim));
   CK(h->w.alloc(nsim));
@@ -547,6 +551,12 @@ void advance_device_epoch(sgdlm_engine *h, uint32_t delta) {
   }
 }
 
+// The sampler's draw-major copy of the Gamma entries (read by the LU and
+// iterative-solve kernels).
+template <typename T> GammaDraws<T> gamma_draws(sgdlm_engine *h) {
+  return GammaDraws<T>{as<T>(h->theta_g), h->g_rowptr.ptr, h->sp.ptr, h->g_nnz};
+}
+
 // sample -> LU -> fallback, from the given normal-gamma parameters (posterior
 // for VB, forecasting prior for forecasts).
 template <typename T>
@@ -558,7 +568,7 @@ void sample_draws(sgdlm_engine *h, const double *m_t, const double *C_t, const d
   const T *U = std::is_same<T, float>::value ? reinterpret_cast<const T *>(h->U32.ptr)
                                               : reinterpret_cast<const T *>(h->U64.ptr);
   launch_sample<T>(h->stream, m, P, n, m_t, n_t, s_t, U, key, as<T>(h->lambda), as<T>(h->theta),
-                   as<T>(h->theta_dm), h->draw_flags.ptr, h->p.ptr);
+                   gamma_draws<T>(h), h->draw_flags.ptr, h->p.ptr);
   h->launches += 2;
 }
 
@@ -584,7 +594,7 @@ int lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   }
   if (warp_lu(h)) {
     launch_lu_warp<T>(h->stream, (int)h->m, (int)h->P, n, h->num_sms, h->sp.ptr, as<T>(h->theta),
-                      as<T>(h->theta_dm), h->logdet.ptr, h->draw_flags.ptr,
+                      h->logdet.ptr, h->draw_flags.ptr,
                       x ? h->nu_fc.ptr : nullptr, x ? y : nullptr);
     h->launches += 1;
     return SGDLM_OK;
@@ -595,18 +605,18 @@ int lu_draws(sgdlm_engine *h, const double *x, RngKey key, double *y) {
   if (iterative) {
     CK(cudaMemsetAsync(h->jac_list.ptr, 0, sizeof(int), h->stream));
     launch_forecast_jacobi(h->stream, h->jac, (int)h->m, (int)h->P, n, rows,
-                           reinterpret_cast<const float *>(h->theta_dm.ptr), h->nu_fc.ptr, y,
+                           reinterpret_cast<const float *>(h->theta_g.ptr), h->g_nnz, h->nu_fc.ptr, y,
                            h->logdet.ptr, h->jac_list.ptr);
     h->launches += 1;
   }
   // the fast pass appends the draws it flags to pivot_list; the redo visits those
   CK(cudaMemsetAsync(h->pivot_list.ptr, 0, sizeof(int), h->stream));
   launch_lu<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
-               as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
+               as<T>(h->theta_g), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x, as<T>(h->lambda), key,
                refine, y, rows, x ? h->nu_fc.ptr : nullptr, h->pivot_list.ptr,
                iterative ? h->jac_list.ptr : nullptr);
   launch_lu_fallback<T>(h->stream, h->plan, n, h->elim_dev, h->sp.ptr, as<T>(h->theta),
-                        as<T>(h->theta_dm), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
+                        as<T>(h->theta_g), as<T>(h->lu_scratch), h->logdet.ptr, h->draw_flags.ptr, x,
                         as<T>(h->lambda), key, y, rows, h->pivot_list.ptr);
   h->launches += 2;
   return SGDLM_OK;
@@ -756,7 +766,7 @@ int learned_draws(sgdlm_engine *h, RngKey key) {
   launch_proposal_params<T>(s, m, P, h->p.ptr, q.Out.ptr, h->m_t.ptr, h->n_t.ptr, h->s_t.ptr,
                             h->U64.ptr, q.mq.ptr, q.nq.ptr, q.sq.ptr, q.Uq64.ptr, Uq, q.cst.ptr);
   launch_sample<T>(s, m, P, n, q.mq.ptr, q.nq.ptr, q.sq.ptr, Uq, key, as<T>(h->lambda),
-                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr, h->p.ptr);
+                   as<T>(h->theta), gamma_draws<T>(h), h->draw_flags.ptr, h->p.ptr);
   h->launches += 8;
   CK(cudaEventRecord(h->ev[1], s));
   int st = lu_draws<T>(h, nullptr, key, nullptr);
@@ -973,7 +983,7 @@ template <typename T> int evolve(sgdlm_engine *h, bool with_G = false) {
   launch_evolve<T>(h->stream, m, P, n, h->p.ptr, h->fn_t.ptr, h->fs_t.ptr, h->beta.ptr, UW,
                    key, (h->compat & SGDLM_COMPAT_UNSCALED_EVOLUTION) != 0,
                    (h->compat & SGDLM_COMPAT_BETA_NO_BOOST) != 0, as<T>(h->lambda),
-                   as<T>(h->theta), as<T>(h->theta_dm), h->draw_flags.ptr,
+                   as<T>(h->theta), gamma_draws<T>(h), h->draw_flags.ptr,
                    with_G ? (std::is_same<T, float>::value
                                  ? reinterpret_cast<const T *>(h->G32.ptr)
                                  : reinterpret_cast<const T *>(h->G_t.ptr))

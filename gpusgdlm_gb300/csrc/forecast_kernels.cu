@@ -135,7 +135,8 @@ __device__ bool jacobi(int m, int r, int wlen, const Row<K> &R, const float *c, 
 
 template <int K>
 __global__ void __launch_bounds__(kJacMaxThreads)
-    k_forecast_jacobi(int m, int P, long n, GammaRows rows, const float *__restrict__ theta_dm,
+    k_forecast_jacobi(int m, int P, long n, GammaRows rows, const float *__restrict__ theta_g,
+                      int nnz,
                       const double *__restrict__ nu, double *__restrict__ y,
                       double *__restrict__ logdet, int *__restrict__ list,
                       const int *__restrict__ order) {
@@ -160,12 +161,11 @@ __global__ void __launch_bounds__(kJacMaxThreads)
     const uint32_t c1 = q + 1 < len ? (uint32_t)rows.ent[e0 + q + 1].y : self;
     R.col[q >> 1] = c0 | (c1 << 16);
   }
-  const size_t row_len = (size_t)m * P;
   for (long i = blockIdx.x; i < n; i += gridDim.x) {
-    // this draw's Gamma entries (from its draw-major theta row) and nu
-    const float *th = theta_dm + (size_t)i * row_len;
+    // this draw's Gamma entries (row r's run of its Gamma copy) and nu
+    const float *th = theta_g + (size_t)i * nnz + e0;
 #pragma unroll
-    for (int q = 0; q < K; ++q) R.val[q] = q < len ? th[__ldg(&rows.ent[e0 + q].x)] : 0.f;
+    for (int q = 0; q < K; ++q) R.val[q] = q < len ? th[q] : 0.f;
     if (r < m) {
       const double v = nu[(size_t)r * n + i];
       nud[r] = v;
@@ -196,7 +196,9 @@ __global__ void __launch_bounds__(kJacMaxThreads)
       }
       block_max2f(dmax, ymax, red);
       ok = ok && ymax < INFINITY && dmax < INFINITY && (double)dmax <= kCorrTol * (double)ymax;
-      if (ok && r < m) y[(size_t)i * m + r] = (double)yv[r] + (double)dv[r];
+      // thread t writes row t (block_max2f ended on a barrier): a warp's stores are
+      // one contiguous run, also when y is page-locked host memory
+      if (ok && tid < m) y[(size_t)i * m + tid] = (double)yv[tid] + (double)dv[tid];
     }
     if (tid == 0) {
       if (ok) {
@@ -252,12 +254,12 @@ JacobiPlan plan_jacobi(int m, int max_row, int num_sms) {
 }
 
 void launch_forecast_jacobi(cudaStream_t s, const JacobiPlan &jp, int m, int P, long n,
-                            GammaRows rows, const float *theta_dm, const double *nu, double *y,
-                            double *logdet, int *list) {
+                            GammaRows rows, const float *theta_g, int nnz, const double *nu,
+                            double *y, double *logdet, int *list) {
   const unsigned grid = (unsigned)std::max<long>(std::min<long>(jp.grid, n), 1);
   const unsigned th = (unsigned)jp.threads;
 #define SGDLM_JACOBI(K)                                                                    \
-  k_forecast_jacobi<K><<<grid, th, jp.smem, s>>>(m, P, n, rows, theta_dm, nu, y, logdet, list, \
+  k_forecast_jacobi<K><<<grid, th, jp.smem, s>>>(m, P, n, rows, theta_g, nnz, nu, y, logdet, list, \
                                                  jp.order)
   switch (jp.nnz) {
     case 8: SGDLM_JACOBI(8); break;

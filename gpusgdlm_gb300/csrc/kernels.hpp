@@ -59,12 +59,26 @@ void launch_to_float(cudaStream_t s, size_t n, const double *src, float *dst);
 void launch_cholesky(cudaStream_t s, int m, int P, const unsigned *p, const double *C,
                      double *U64, float *U32);
 
+// The draws' Gamma entries (the simultaneous-parent coefficients), draw-major in
+// the CSR order of the rows of Gamma: row j holds series j's coefficients at the
+// positions sp[j*P + k] < m*m, in increasing k, from rowptr[j] on (GammaRows).
+// Draw i's entry q is v[i*nnz + q].  That order is also the order of increasing
+// theta index j*P + k, i.e. the elimination plan's level-0 order.  The sampler
+// writes this copy beside the series-major theta; the LU and iterative-solve
+// kernels read a draw's nnz values as one run.
+template <typename T> struct GammaDraws {
+  T *v;                 // nsim * nnz, or nullptr: not written
+  const int *rowptr;    // m + 1
+  const unsigned *sp;   // P x m
+  int nnz;
+};
+
 // (a3) lambda_ij ~ Gamma(n_j/2, rate n_j s_j/2); theta_ij = m_j + U_j' z/sqrt(s_j lambda_ij).
 // rSGDLM/src/SGDLM/SGDLM.cu:623-677
 template <typename T>
 void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                    const double *n_t, const double *s_t, const T *U, RngKey key,
-                   T *lambda, T *theta, T *theta_dm, int *draw_flags,
+                   T *lambda, T *theta, GammaDraws<T> gd, int *draw_flags,
                    // p_j (the Cholesky factors' cut), or nullptr: all P coefficients
                    const unsigned *p = nullptr);
 
@@ -73,7 +87,7 @@ template <typename T>
 void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
                    const double *r_t, const double *c_t, const double *beta,
                    const T *UW, RngKey key, bool compat_unscaled_omega,
-                   bool compat_beta_no_boost, T *lambda, T *theta, T *theta_dm,
+                   bool compat_beta_no_boost, T *lambda, T *theta, GammaDraws<T> gd,
                    int *draw_flags, const T *G = nullptr);
 
 // (a4)/(a8) batched LU of (I - Gamma_i): log|det| per draw, and optionally the
@@ -107,7 +121,7 @@ constexpr int kWarpLuMaxM = 32;
 // (nu series-major, nu[r*n + i]; y draw-major, y[i*m + r]).
 template <typename T>
 void launch_lu_warp(cudaStream_t s, int m, int P, long n, int num_sms, const unsigned *sp,
-                    const T *theta, const T *theta_dm, double *logdet, int *draw_flags,
+                    const T *theta, double *logdet, int *draw_flags,
                     const double *nu, double *y);
 // core_n / nv / n_solve / prog_len come from the elimination plan (core_n = m and
 // the others 0 without one).
@@ -127,9 +141,10 @@ struct GammaRows {
 };
 struct EliminationPlan;
 template <typename T>
-// theta: the draws series-major; theta_dm: their draw-major copy, or nullptr.
+// theta: the draws series-major; theta_g: their Gamma entries (GammaDraws layout,
+// ep.nnz0 per draw), or nullptr (then gathered from theta).
 void launch_lu(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan &ep,
-               const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
+               const unsigned *sp, const T *theta, const T *theta_g, T *scratch,
                double *logdet, int *draw_flags,
                // forecast solve (x == nullptr: log|det| only)
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
@@ -157,9 +172,11 @@ struct JacobiPlan {
 JacobiPlan plan_jacobi(int m, int max_row, int num_sms);
 // y (draw-major) of every draw whose iteration converges (logdet[i] set to NaN:
 // not factored); the others are appended to list (n + 1 ints, [0] zero on entry).
-// theta_dm: the draws' draw-major copy; nu: series-major right-hand sides.
+// theta_g: the draws' Gamma entries (GammaDraws layout, nnz per draw); nu:
+// series-major right-hand sides.
 void launch_forecast_jacobi(cudaStream_t s, const JacobiPlan &jp, int m, int P, long n,
-                            GammaRows rows, const float *theta_dm, const double *nu, double *y,
+                            GammaRows rows, const float *theta_g, int nnz, const double *nu,
+                            double *y,
                             double *logdet, int *list);
 // The forecast right-hand sides nu_ij = z_ij / sqrt(lambda_ij) + x_j' phi_ij of all
 // draws (series-major, nu[j*n + i]); theta series-major; x32: an FP32 copy of x
@@ -171,7 +188,7 @@ void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, co
                         double *nu);
 template <typename T>
 void launch_lu_fallback(cudaStream_t s, const LuPlan &plan, long n, const EliminationPlan &ep,
-                        const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
+                        const unsigned *sp, const T *theta, const T *theta_g, T *scratch,
                         double *logdet, int *draw_flags, const double *x,
                         const T *lambda, RngKey key, double *y, GammaRows rows,
                         // the list launch_lu appended to (only those draws are

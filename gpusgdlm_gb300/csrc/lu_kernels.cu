@@ -215,18 +215,24 @@ struct FallbackSmem {
   }
 };
 
-// The draws' theta, series-major (theta[(j*n + i)*P + k], the sampler's layout)
-// and, when present, the draw-major copy theta_dm[(i*m + j)*P + k] in which one
-// draw's values are one contiguous row; the LU kernels read the latter.
+// The draws' theta, series-major (theta[(j*n + i)*P + k], the sampler's layout),
+// and, when present, their Gamma entries draw-major (GammaDraws: draw i's entry q
+// at g[i*nnz + q], q the CSR position of the entry = its index in the plan's
+// level-0 list), so that a draw's Gamma values are one contiguous run.
 template <typename T> struct Theta {
-  const T *sm, *dm;
-  int m, P;
+  const T *sm, *g;
+  int m, P, nnz;
   long n;
-  __device__ __forceinline__ T at(long i, int e) const {  // e = j*P + k
-    return dm ? dm[(size_t)i * m * P + e] : sm[((size_t)(e / P) * n + i) * P + e % P];
+  // by theta index e = j*P + k (series-major copy)
+  __device__ __forceinline__ T at(long i, int e) const {
+    return sm[((size_t)(e / P) * n + i) * P + e % P];
+  }
+  // Gamma entry q of draw i, whose theta index is e
+  __device__ __forceinline__ T gamma(long i, int q, int e) const {
+    return g ? g[(size_t)i * nnz + q] : at(i, e);
   }
   __device__ __forceinline__ const T *row(long i, int j) const {
-    return dm ? dm + ((size_t)i * m + j) * P : sm + ((size_t)j * n + i) * P;
+    return sm + ((size_t)j * n + i) * P;
   }
 };
 
@@ -1474,12 +1480,12 @@ __device__ __forceinline__ void build_slots(const EliminationPlan &ep, int m, lo
 #pragma unroll
     for (int h = 0; h < 16; ++h) {
       const bool ok = k0 + h * kThreads < ep.nnz0;
-      e[h] = ok ? ep.l0_e[k0 + h * kThreads] : -1;
+      e[h] = ok ? (theta.g ? 0 : ep.l0_e[k0 + h * kThreads]) : -1;  // the index only without the Gamma copy
       sl[h] = ok ? ep.l0_slot[k0 + h * kThreads] : 0;
     }
     T th[16];
 #pragma unroll
-    for (int h = 0; h < 16; ++h) th[h] = e[h] >= 0 ? theta.at(i, e[h]) : T(0);
+    for (int h = 0; h < 16; ++h) th[h] = e[h] >= 0 ? theta.gamma(i, k0 + h * kThreads, e[h]) : T(0);
 #pragma unroll
     for (int h = 0; h < 16; ++h)
       if (e[h] >= 0) vals[sl[h]] = -th[h];
@@ -1639,7 +1645,7 @@ __device__ void residual(int m, int P, long n, long i, GammaRows rows, Theta<T> 
       T th[8];
 #pragma unroll
       for (int h = 0; h < 8; ++h)
-        th[h] = ec[h].x >= 0 ? theta.at(i, ec[h].x) : T(0);
+        th[h] = ec[h].x >= 0 ? theta.gamma(i, q0 + h, ec[h].x) : T(0);
 #pragma unroll
       for (int h = 0; h < 8; ++h)
         if (ec[h].x >= 0) v += (double)th[h] * (double)y[ec[h].y];
@@ -1672,7 +1678,7 @@ __device__ void residual_rhs(int m, int P, long n, long i, GammaRows rows, Theta
         for (int h = 0; h < 8; ++h) ec[h] = (q0 + h < q1) ? __ldg(rows.ent + q0 + h) : make_int2(-1, 0);
         float th[8];
 #pragma unroll
-        for (int h = 0; h < 8; ++h) th[h] = ec[h].x >= 0 ? (float)theta.at(i, ec[h].x) : 0.f;
+        for (int h = 0; h < 8; ++h) th[h] = ec[h].x >= 0 ? (float)theta.gamma(i, q0 + h, ec[h].x) : 0.f;
 #pragma unroll
         for (int h = 0; h < 8; ++h) {
           if (ec[h].x < 0) continue;
@@ -1712,7 +1718,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     k_lu(int m, int P, int dp, size_t per_cta, int vals_smem, int prog_smem, long n,
          EliminationPlan ep,
          const unsigned *__restrict__ sp, const T *__restrict__ theta_sm,
-         const T *__restrict__ theta_dm, T *__restrict__ scratch,
+         const T *__restrict__ theta_g, T *__restrict__ scratch,
          double *__restrict__ logdet, int *__restrict__ draw_flags,
          const double *__restrict__ x, const T *__restrict__ lambda, RngKey key, bool refine,
          double *__restrict__ y, GammaRows rows, const double *__restrict__ nu_in,
@@ -1721,7 +1727,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   using V = Vec<T>;
   constexpr int W = V::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Theta<T> theta{theta_sm, theta_dm, m, P, n};
+  const Theta<T> theta{theta_sm, theta_g, m, P, ep.nnz0, n};
   const Smem L(dp, m, sizeof(T), vals_smem ? ep.nv : 0, TC);
   T *D = reinterpret_cast<T *>(smem_raw + L.off_D);  // D^-1, row-major, stride kB
   T *prow = reinterpret_cast<T *>(smem_raw + L.off_prow);
@@ -1785,12 +1791,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
 #pragma unroll
         for (int h = 0; h < 16; ++h) {
           const bool ok = k0 + h * kThreads < ep.nnz0;
-          e[h] = ok ? ep.l0_e[k0 + h * kThreads] : -1;
+          e[h] = ok ? (theta.g ? 0 : ep.l0_e[k0 + h * kThreads]) : -1;  // the index only without the Gamma copy
           sl[h] = ok ? ep.l0_slot[k0 + h * kThreads] : 0;
         }
         T th[16];
 #pragma unroll
-        for (int h = 0; h < 16; ++h) th[h] = e[h] >= 0 ? theta.at(i, e[h]) : T(0);
+        for (int h = 0; h < 16; ++h) th[h] = e[h] >= 0 ? theta.gamma(i, k0 + h * kThreads, e[h]) : T(0);
 #pragma unroll
         for (int h = 0; h < 16; ++h)
           if (e[h] >= 0) vals[sl[h]] = -th[h];
@@ -2495,13 +2501,13 @@ __global__ void __launch_bounds__(kThreads)
     k_lu_fallback(int m, int P, int mp, int dp, size_t per_cta, int core_smem, long n,
                   EliminationPlan ep,
                   const unsigned *__restrict__ sp,
-                  const T *__restrict__ theta_sm, const T *__restrict__ theta_dm,
+                  const T *__restrict__ theta_sm, const T *__restrict__ theta_g,
                   T *__restrict__ scratch,
                   double *__restrict__ logdet, int *__restrict__ draw_flags,
                   const double *__restrict__ x, const T *__restrict__ lambda, RngKey key,
                   double *__restrict__ y, GammaRows rows, const int *__restrict__ pivot_list) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const Theta<T> theta{theta_sm, theta_dm, m, P, n};
+  const Theta<T> theta{theta_sm, theta_g, m, P, ep.nnz0, n};
   const FallbackSmem L(mp, m, sizeof(T), core_smem ? dp : 0);
   __shared__ bool s_singular;
   __shared__ int s_level_bad;
@@ -2727,7 +2733,7 @@ LuPlan plan_lu(int m, int P, long n, int num_sms, int core_n, int nv, int n_solv
 
 template <typename T>
 void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &ep,
-               const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
+               const unsigned *sp, const T *theta, const T *theta_g, T *scratch,
                double *logdet, int *draw_flags,
                const double *x, const T *lambda, RngKey key, bool refine, double *y,
                GammaRows rows, const double *nu_in, int *pivot_list, const int *draw_list) {
@@ -2738,7 +2744,7 @@ void launch_lu(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem);
     kernel<<<pl.grid, pl.block, pl.smem, s>>>(pl.m, pl.P, pl.dp, pl.scratch_elems_per_cta,
                                               pl.vals_smem, pl.prog_smem, n, ep, sp, theta,
-                                              theta_dm, scratch,
+                                              theta_g, scratch,
                                               logdet, draw_flags, x, lambda, key, refine, y, rows,
                                               nu_in, pivot_list, draw_list);
   };
@@ -2761,7 +2767,7 @@ void launch_forecast_nu(cudaStream_t s, int m, int P, long n, GammaRows rows, co
 
 template <typename T>
 void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const EliminationPlan &ep,
-                        const unsigned *sp, const T *theta, const T *theta_dm, T *scratch,
+                        const unsigned *sp, const T *theta, const T *theta_g, T *scratch,
                         double *logdet, int *draw_flags,
                         const double *x, const T *lambda, RngKey key, double *y,
                         GammaRows rows, const int *pivot_list) {
@@ -2769,7 +2775,7 @@ void launch_lu_fallback(cudaStream_t s, const LuPlan &pl, long n, const Eliminat
     cudaFuncSetAttribute(k_lu_fallback<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)pl.smem_fallback);
   k_lu_fallback<T><<<pl.fb_grid, pl.block, pl.smem_fallback, s>>>(
-      pl.m, pl.P, pl.mp, pl.dp, pl.fb_elems_per_cta, pl.fb_core_smem, n, ep, sp, theta, theta_dm,
+      pl.m, pl.P, pl.mp, pl.dp, pl.fb_elems_per_cta, pl.fb_core_smem, n, ep, sp, theta, theta_g,
       scratch, logdet,
       draw_flags, x, lambda, key, y, rows, pivot_list);
 }

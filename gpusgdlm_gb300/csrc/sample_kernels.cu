@@ -8,7 +8,9 @@
 // pair: its normals come out of Philox in registers, U_j sits in shared memory
 // (every thread of the block shares series j, so reads are broadcasts), and the
 // block's theta rows are staged in shared memory so the series-major store is one
-// contiguous coalesced run.
+// contiguous coalesced run.  From the same staged rows the block writes its draws'
+// Gamma entries to the draw-major Gamma copy (GammaDraws), which the LU and
+// iterative-solve kernels read as one run per draw.
 #include "kernels.hpp"
 #include "rng.cuh"
 
@@ -17,23 +19,31 @@ namespace {
 
 constexpr int kSampleThreads = 128;
 
-// Writes draw i's row of series j (P values) into the draw-major copy
-// theta_dm[(i*m + j)*P + k] used by the LU kernels (one contiguous row per draw),
-// with 16-byte stores when the rows are 16-byte aligned.
+// The series' Gamma coefficients: k of the c-th entry of its row (gks[c], the k
+// with a simultaneous parent, sp[j*P + k] < m*m, in increasing k), their count and
+// the row's first position in the CSR order.  One thread.
+__device__ __forceinline__ void gamma_row_of(const unsigned *__restrict__ sp, const int *rowptr,
+                                             int j, int P, unsigned mm, int *gks, int *gcnt,
+                                             int *gq0) {
+  int c = 0;
+  for (int k = 0; k < P; ++k)
+    if (sp[(size_t)j * P + k] < mm) gks[c++] = k;
+  *gcnt = c;
+  *gq0 = rowptr[j];
+}
+
+// The block's draws i0 .. i0 + cnt - 1 of series j, staged row by row (P values
+// per draw), to their Gamma runs of the draw-major copy (GammaDraws: draw i's run
+// at v[i*nnz + q0 ..]).  Consecutive threads take consecutive entries, so a warp
+// writes the runs of several draws at once.
 template <typename T>
-__device__ __forceinline__ void write_draw_major(T *__restrict__ theta_dm, int m, int P, long i,
-                                                 int j, const T *row) {
-  T *dst = theta_dm + ((size_t)i * m + j) * P;
-  if ((P * sizeof(T)) % 16 == 0) {
-    for (int k = 0; k < P; k += (int)(16 / sizeof(T))) {
-      if (sizeof(T) == 4)
-        *reinterpret_cast<float4 *>(dst + k) =
-            make_float4((float)row[k], (float)row[k + 1], (float)row[k + 2], (float)row[k + 3]);
-      else
-        *reinterpret_cast<double2 *>(dst + k) = make_double2((double)row[k], (double)row[k + 1]);
-    }
-  } else {
-    for (int k = 0; k < P; ++k) dst[k] = row[k];
+__device__ __forceinline__ void write_gamma_runs(const GammaDraws<T> &gd, int P, long i0, int cnt,
+                                                 const T *stage, const int *gks, int gcnt,
+                                                 int gq0) {
+  const int tot = cnt * gcnt;
+  for (int x = threadIdx.x; x < tot; x += blockDim.x) {
+    const int t = x / gcnt, c = x - t * gcnt;
+    gd.v[(size_t)(i0 + t) * gd.nnz + gq0 + c] = stage[(size_t)t * P + gks[c]];
   }
 }
 
@@ -42,13 +52,14 @@ __global__ void __launch_bounds__(kSampleThreads)
     k_sample(int m, int P, long n, const double *__restrict__ m_t,
              const double *__restrict__ n_t, const double *__restrict__ s_t,
              const T *__restrict__ U, RngKey key, T *__restrict__ lambda,
-             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags,
+             T *__restrict__ theta, GammaDraws<T> gd, int *__restrict__ draw_flags,
              const unsigned *__restrict__ p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Us = reinterpret_cast<T *>(smem_raw);  // P*P, U[row + P*col]
   T *ms = Us + P * P;                       // P
   T *stage = ms + P;                        // blockDim.x * P
   __shared__ T ser[3];                      // the series' gamma shape and rate, s_j
+  __shared__ int gks[64], gcnt, gq0;        // its Gamma coefficients (gamma_row_of)
   const int j = blockIdx.y;
   // the series' active coefficients: U_j is zero outside its leading pj x pj
   // block (the Cholesky factor's cut), so theta_k = m_k exactly for k >= pj and
@@ -57,6 +68,8 @@ __global__ void __launch_bounds__(kSampleThreads)
   const int pj = p ? min((int)p[j], P) : P;
   for (int e = threadIdx.x; e < P * P; e += blockDim.x) Us[e] = U[(size_t)j * P * P + e];
   for (int e = threadIdx.x; e < P; e += blockDim.x) ms[e] = (T)m_t[(size_t)j * P + e];
+  if (gd.v && threadIdx.x == 32)
+    gamma_row_of(gd.sp, gd.rowptr, j, P, (unsigned)m * (unsigned)m, gks, &gcnt, &gq0);
   if (threadIdx.x == 0) {
     // FP64 once per series (FP64 is a narrow pipe on this GPU)
     const double nj = n_t[j], sj = s_t[j];
@@ -100,10 +113,10 @@ __global__ void __launch_bounds__(kSampleThreads)
       }
     }
     lambda[(size_t)j * n + i] = lam;
-    if (theta_dm) write_draw_major<T>(theta_dm, m, P, i, j, row);
     if (fail) atomicOr(&draw_flags[i], DRAW_FLAG_GAMMA_CAP);
   }
   __syncthreads();
+  if (gd.v) write_gamma_runs<T>(gd, P, i0, (int)min((long)blockDim.x, n - i0), stage, gks, gcnt, gq0);
   const long cnt = (long)min((long)blockDim.x, n - i0) * P;
   T *dst = theta + ((size_t)j * n + i0) * P;
   if (((size_t)j * n + i0) * P * sizeof(T) % 16 == 0 && cnt * sizeof(T) % 16 == 0 &&
@@ -127,13 +140,16 @@ __global__ void __launch_bounds__(kSampleThreads)
              const double *__restrict__ r_t, const double *__restrict__ c_t,
              const double *__restrict__ beta, const T *__restrict__ UW, RngKey key,
              bool compat_unscaled, bool compat_no_boost, T *__restrict__ lambda,
-             T *__restrict__ theta, T *__restrict__ theta_dm, int *__restrict__ draw_flags,
+             T *__restrict__ theta, GammaDraws<T> gd, int *__restrict__ draw_flags,
              const T *__restrict__ G) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Us = reinterpret_cast<T *>(smem_raw);
   T *Gs = Us + P * P;  // G_j when an evolution matrix is given
   T *stage = Gs + (G ? P * P : 0);
+  __shared__ int gks[64], gcnt, gq0;  // the series' Gamma coefficients (gamma_row_of)
   const int j = blockIdx.y;
+  if (gd.v && threadIdx.x == 0)
+    gamma_row_of(gd.sp, gd.rowptr, j, P, (unsigned)m * (unsigned)m, gks, &gcnt, &gq0);
   const long i0 = (long)blockIdx.x * blockDim.x;
   const long cnt = (long)min((long)blockDim.x, n - i0) * P;
   T *src = theta + ((size_t)j * n + i0) * P;
@@ -203,10 +219,10 @@ __global__ void __launch_bounds__(kSampleThreads)
         row[k] = acc + row[k];
       }
     }
-    if (theta_dm) write_draw_major<T>(theta_dm, m, P, i, j, row);
     if (fail) atomicOr(&draw_flags[i], DRAW_FLAG_GAMMA_CAP);
   }
   __syncthreads();
+  if (gd.v) write_gamma_runs<T>(gd, P, i0, (int)min((long)blockDim.x, n - i0), stage, gks, gcnt, gq0);
   for (long e = threadIdx.x; e < cnt; e += blockDim.x) src[e] = stage[e];
 }
 
@@ -219,7 +235,7 @@ template <typename T> size_t sample_smem(int P) {
 template <typename T>
 void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
                    const double *n_t, const double *s_t, const T *U, RngKey key,
-                   T *lambda, T *theta, T *theta_dm, int *draw_flags, const unsigned *p) {
+                   T *lambda, T *theta, GammaDraws<T> gd, int *draw_flags, const unsigned *p) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
   const size_t smem = sample_smem<T>(P);
   if (smem > 48 * 1024) {
@@ -231,26 +247,26 @@ void launch_sample(cudaStream_t s, int m, int P, long n, const double *m_t,
   }
   if (P <= 8)
     k_sample<T, 8><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                      lambda, theta, theta_dm, draw_flags, p);
+                                                      lambda, theta, gd, draw_flags, p);
   else if (P <= 16)
     k_sample<T, 16><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags, p);
+                                                       lambda, theta, gd, draw_flags, p);
   else if (P <= 24)
     k_sample<T, 24><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags, p);
+                                                       lambda, theta, gd, draw_flags, p);
   else if (P <= 32)
     k_sample<T, 32><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags, p);
+                                                       lambda, theta, gd, draw_flags, p);
   else
     k_sample<T, 64><<<grid, kSampleThreads, smem, s>>>(m, P, n, m_t, n_t, s_t, U, key,
-                                                       lambda, theta, theta_dm, draw_flags, p);
+                                                       lambda, theta, gd, draw_flags, p);
 }
 
 template <typename T>
 void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
                    const double *r_t, const double *c_t, const double *beta,
                    const T *UW, RngKey key, bool compat_unscaled_omega,
-                   bool compat_beta_no_boost, T *lambda, T *theta, T *theta_dm,
+                   bool compat_beta_no_boost, T *lambda, T *theta, GammaDraws<T> gd,
                    int *draw_flags, const T *G) {
   dim3 grid((unsigned)((n + kSampleThreads - 1) / kSampleThreads), (unsigned)m);
   const size_t smem =
@@ -265,7 +281,7 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
   k_evolve<T, PM><<<grid, kSampleThreads, smem, s>>>(m, P, n, p, r_t, c_t, beta, UW, \
                                                      key, compat_unscaled_omega,      \
                                                      compat_beta_no_boost, lambda,    \
-                                                     theta, theta_dm, draw_flags, G)
+                                                     theta, gd, draw_flags, G)
   if (P <= 8)
     SGDLM_EVOLVE(8);
   else if (P <= 16)
@@ -279,18 +295,18 @@ void launch_evolve(cudaStream_t s, int m, int P, long n, const unsigned *p,
 
 template void launch_sample<float>(cudaStream_t, int, int, long, const double *,
                                    const double *, const double *, const float *, RngKey,
-                                   float *, float *, float *, int *, const unsigned *);
+                                   float *, float *, GammaDraws<float>, int *, const unsigned *);
 template void launch_sample<double>(cudaStream_t, int, int, long, const double *,
                                     const double *, const double *, const double *,
-                                    RngKey, double *, double *, double *, int *,
+                                    RngKey, double *, double *, GammaDraws<double>, int *,
                                     const unsigned *);
 template void launch_evolve<float>(cudaStream_t, int, int, long, const unsigned *,
                                    const double *, const double *, const double *,
                                    const float *, RngKey, bool, bool, float *, float *,
-                                   float *, int *, const float *);
+                                   GammaDraws<float>, int *, const float *);
 template void launch_evolve<double>(cudaStream_t, int, int, long, const unsigned *,
                                     const double *, const double *, const double *,
                                     const double *, RngKey, bool, bool, double *,
-                                    double *, double *, int *, const double *);
+                                    double *, GammaDraws<double>, int *, const double *);
 
 }  // namespace sgdlm

@@ -54,7 +54,7 @@ __device__ __forceinline__ T lu_solve(const T (&a)[32], int m, int pos, const in
 template <typename T>
 __global__ void __launch_bounds__(kWarpLuThreads)
     k_lu_warp(int m, int P, long n, const unsigned *__restrict__ sp, const T *__restrict__ theta_sm,
-              const T *__restrict__ theta_dm, double *__restrict__ logdet,
+              double *__restrict__ logdet,
               int *__restrict__ draw_flags, const double *__restrict__ nu, double *__restrict__ y) {
   __shared__ T tile[kWarpLuWarps][32][33];  // the draw's (I - Gamma_i), row-major
   __shared__ int prow_s[kWarpLuWarps][32];
@@ -71,8 +71,7 @@ __global__ void __launch_bounds__(kWarpLuThreads)
     for (int e = lane; e < m * P; e += 32) {
       const unsigned pos = sp[e];
       if ((size_t)pos < mm) {
-        const T th = theta_dm ? theta_dm[(size_t)i * m * P + e]
-                              : theta_sm[((size_t)(e / P) * n + i) * P + e % P];
+        const T th = theta_sm[((size_t)(e / P) * n + i) * P + e % P];
         M[pos % (unsigned)m][pos / (unsigned)m] = -th;
       }
     }
@@ -159,21 +158,21 @@ __global__ void __launch_bounds__(kWarpLuThreads)
 
 template <typename T>
 void launch_lu_warp(cudaStream_t s, int m, int P, long n, int num_sms, const unsigned *sp,
-                    const T *theta, const T *theta_dm, double *logdet, int *draw_flags,
+                    const T *theta, double *logdet, int *draw_flags,
                     const double *nu, double *y) {
   long blocks = (n + kWarpLuWarps - 1) / kWarpLuWarps;
   const long cap = (long)num_sms * 16;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  k_lu_warp<T><<<(unsigned)blocks, kWarpLuThreads, 0, s>>>(m, P, n, sp, theta, theta_dm, logdet,
+  k_lu_warp<T><<<(unsigned)blocks, kWarpLuThreads, 0, s>>>(m, P, n, sp, theta, logdet,
                                                            draw_flags, nu, y);
 }
 
 template void launch_lu_warp<float>(cudaStream_t, int, int, long, int, const unsigned *,
-                                    const float *, const float *, double *, int *, const double *,
+                                    const float *, double *, int *, const double *,
                                     double *);
 template void launch_lu_warp<double>(cudaStream_t, int, int, long, int, const unsigned *,
-                                     const double *, const double *, double *, int *,
+                                     const double *, double *, int *,
                                      const double *, double *);
 
 }  // namespace sgdlm
