@@ -21,15 +21,24 @@ constexpr int kSampleThreads = 128;
 
 // The series' Gamma coefficients: k of the c-th entry of its row (gks[c], the k
 // with a simultaneous parent, sp[j*P + k] < m*m, in increasing k), their count and
-// the row's first position in the CSR order.  One thread.
+// the row's first position in the CSR order.  One whole warp: lane l tests k = l,
+// l + 32 (P <= 64) and places its k by a ballot of the lanes before it.
 __device__ __forceinline__ void gamma_row_of(const unsigned *__restrict__ sp, const int *rowptr,
                                              int j, int P, unsigned mm, int *gks, int *gcnt,
                                              int *gq0) {
-  int c = 0;
-  for (int k = 0; k < P; ++k)
-    if (sp[(size_t)j * P + k] < mm) gks[c++] = k;
-  *gcnt = c;
-  *gq0 = rowptr[j];
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  for (int k0 = 0; k0 < P; k0 += 32) {
+    const int k = k0 + lane;
+    const bool g = k < P && sp[(size_t)j * P + k] < mm;
+    const unsigned mask = __ballot_sync(0xffffffffu, g);
+    if (g) gks[base + __popc(mask & ((1u << lane) - 1u))] = k;
+    base += __popc(mask);
+  }
+  if (lane == 0) {
+    *gcnt = base;
+    *gq0 = rowptr[j];
+  }
 }
 
 // The block's draws i0 .. i0 + cnt - 1 of series j, staged row by row (P values
@@ -68,7 +77,7 @@ __global__ void __launch_bounds__(kSampleThreads)
   const int pj = p ? min((int)p[j], P) : P;
   for (int e = threadIdx.x; e < P * P; e += blockDim.x) Us[e] = U[(size_t)j * P * P + e];
   for (int e = threadIdx.x; e < P; e += blockDim.x) ms[e] = (T)m_t[(size_t)j * P + e];
-  if (gd.v && threadIdx.x == 32)
+  if (gd.v && (threadIdx.x >> 5) == 1)  // warp 1 (thread 0 sets up ser)
     gamma_row_of(gd.sp, gd.rowptr, j, P, (unsigned)m * (unsigned)m, gks, &gcnt, &gq0);
   if (threadIdx.x == 0) {
     // FP64 once per series (FP64 is a narrow pipe on this GPU)
@@ -148,7 +157,7 @@ __global__ void __launch_bounds__(kSampleThreads)
   T *stage = Gs + (G ? P * P : 0);
   __shared__ int gks[64], gcnt, gq0;  // the series' Gamma coefficients (gamma_row_of)
   const int j = blockIdx.y;
-  if (gd.v && threadIdx.x == 0)
+  if (gd.v && (threadIdx.x >> 5) == 0)
     gamma_row_of(gd.sp, gd.rowptr, j, P, (unsigned)m * (unsigned)m, gks, &gcnt, &gq0);
   const long i0 = (long)blockIdx.x * blockDim.x;
   const long cnt = (long)min((long)blockDim.x, n - i0) * P;
