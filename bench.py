@@ -15,6 +15,9 @@ beta = 0.97, Delta = 0.98.  Seeds are recorded in the output line.
           y_t, F_t, F_t+1 and D2H of the VB results and the forecast draws inside
           the timed region.
   fp64_gpu : the plain FP64 form (every kernel in FP64) on the same workload.
+  precision_config_50k_draws : 50 000 IS draws and forecasts 1..5 steps ahead
+          (10 000 draws each) per step, mixed and plain FP64 forms, C ABI calls
+          with page-locked host outputs.
 --impl reference runs the FP64 CPU implementation of the same step (the oracle
 port: the reference has no CPU path and its CUDA build cannot be built on the
 Arm GPU host) on all host cores: whole time steps at the full draw counts after
@@ -282,6 +285,103 @@ def run_fp64_form(args, s_mixed, wl, t0, dev, rank):
     ms = ev0.elapsed_time(ev1)
     s.close()
     return dict(ms=ms, steps=k)
+
+
+def run_c2(args):
+    """The precision configuration at its stated per-step sizes: m = 400, p_j <= 20,
+    50 000 IS draws per VB call and forecasts 1..5 steps ahead with 10 000 samples
+    each, through the C ABI with page-locked host outputs (the VB results and the
+    forecast draws of all five horizons, 160 MB, written to host memory every
+    step), the mixed form and the plain FP64 form from the same prior state after
+    a 30-step burn-in (2 000 draws); wall clock per time step, every call
+    synchronous."""
+    import torch
+
+    from gpusgdlm_gb300 import SGDLM
+    from gpusgdlm_gb300 import _lib as L
+
+    m, n_vb, n_fc, K = 400, 50000, 10000, 5
+    wl = make_workload(m=m, T=60, seed=args.seed)
+    P = wl["P"]
+
+    def engine(precision):
+        # corrected samplers: the reference's beta sampler of the evolution
+        # (make_beta, kernel_functions.cuh:725-798; Marsaglia-Tsang without the
+        # boost below shape one) gives NaN for shapes below 1/3, which (1 - beta) r / 2
+        # reaches here, and would make every 2..5-step forecast draw NaN
+        s = SGDLM(1, strict=True, precision=precision, compat=L.COMPAT_NONE)
+        s.setSimultaneousParents(wl["p"], np.where(wl["sp"] >= m * m, np.nan, wl["sp"]).astype(float))
+        s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+        return s
+
+    pin = lambda shape: torch.zeros(int(np.prod(shape)), dtype=torch.float64).pin_memory().numpy()  # noqa: E731
+    dp = C.POINTER(C.c_double)
+    ptr = lambda a: a.ctypes.data_as(dp)  # noqa: E731
+    om, oC, on, os_, ow = pin((P, m)), pin((P, P, m)), pin((m,)), pin((m,)), pin((n_vb,))
+    ofc = [pin((m, n_fc)) for _ in range(K)]
+    sw = C.c_double()
+    staged = {}
+    for t in range(1, 50):
+        yb, Fb = pin((m,)), pin((P, m))
+        yb[:] = wl["y"][t]
+        Fb[:] = wl["F_of"](t).ravel(order="F")
+        Xs = []
+        for k in range(1, K + 1):
+            Xb = pin((P, m))
+            Xb[:] = wl["F_of"](t + k, False).ravel(order="F")
+            Xs.append(Xb)
+        staged[t] = (yb, Fb, Xs)
+
+    def step(s, t):
+        lib, h = s._lib, s._h
+        yb, Fb, Xs = staged[t]
+        assert lib.sgdlm_compute_posterior(h, ptr(yb), ptr(Fb)) == 0
+        s._ensure_sim(n_vb, n_vb)
+        assert lib.sgdlm_compute_vb_posterior(h, ptr(om), ptr(oC), ptr(on), ptr(os_), ptr(ow),
+                                              C.byref(sw)) == 0
+        if 1.0 / float(np.dot(ow, ow)) > n_vb / 2:
+            assert lib.sgdlm_set_parameters(h, ptr(om), ptr(oC), ptr(on), ptr(os_)) == 0
+            lib.sgdlm_set_is_prior(h, 0)
+        assert lib.sgdlm_compute_prior(h, 0) == 0
+        s._ensure_sim(n_fc, n_fc)
+        assert lib.sgdlm_init_forecast_priors(h) == 0
+        for k in range(K):  # RcppWrapper.cpp:455-472
+            if k > 0:
+                assert lib.sgdlm_evolve_forecast_samples(h) == 0
+            assert lib.sgdlm_compute_forecast(h, ptr(ofc[k]), ptr(Xs[k]), None, None,
+                                              1 if k > 0 else 0) == 0
+
+    s = engine("mixed")
+    a, R, r, c = prior_arrays(m, P)
+    s.setPriorParameters(a, R, r, c)
+    s.setRngState(1234, 0)
+    t = 1
+    for _ in range(30):
+        s.computePosterior(wl["y"][t], wl["F_of"](t))
+        vb = s.computeVBPosterior(2000, 2000)
+        if 1.0 / np.sum(vb["IS_weights"] ** 2) > 1000:
+            s.setPosteriorParameters(vb["m"], vb["C"], vb["n"], vb["s"])
+        s.computePrior()
+        t += 1
+    st = s.getParameters()
+    seed, epoch = s.getRngState()
+    f = engine("fp64")
+    f.setPriorParameters(st["m"], st["C"], st["n"], st["s"])
+    f.setRngState(seed, epoch)
+    out = {}
+    for name, e, k in (("mixed", s, args.c2_steps), ("fp64", f, max(1, args.c2_steps // 2))):
+        step(e, t)  # warm-up: allocations of both draw counts
+        t0 = time.perf_counter()
+        for q in range(k):
+            step(e, t + 1 + q)
+        dt = time.perf_counter() - t0
+        out[name] = {"time_steps_per_s": k / dt, "ms_per_step": 1000.0 * dt / k, "timed_steps": k}
+        e.close()
+    return {"workload": f"m={m}, p_j<=20, {n_vb} IS draws + forecasts k=1..{K} x {n_fc} draws per "
+                        "step, C ABI with page-locked host outputs, corrected samplers (compat off)",
+            "mixed": out["mixed"], "fp64": out["fp64"],
+            "speedup_mixed_vs_fp64": out["mixed"]["time_steps_per_s"] / out["fp64"]["time_steps_per_s"],
+            "burn_in_steps": 30}
 
 
 def run_c3(args):
@@ -674,6 +774,8 @@ def main():
                     help="cap on the reference arm's timed full-size steps")
     ap.add_argument("--fp64-steps", type=int, default=3,
                     help="timed steps of the plain FP64 form (0: skip)")
+    ap.add_argument("--c2-steps", type=int, default=4,
+                    help="timed steps of the 50k-draw, five-horizon configuration (0: skip)")
     ap.add_argument("--c3-instances", type=int, default=64,
                     help="instances of the batched-form comparison (0: skip)")
     ap.add_argument("--c3-steps", type=int, default=12)
@@ -752,6 +854,8 @@ def main():
                            "note": "ESS of the decoupled (plain) proposal per second of "
                                    "computeVBPosterior device time at this workload"},
     }
+    if args.c2_steps > 0:
+        line["precision_config_50k_draws"] = run_c2(args)
     if args.c4_steps > 0:
         line["ess_per_s"] = run_c4(args)
     if args.c3_instances > 0:

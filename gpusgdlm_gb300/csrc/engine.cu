@@ -58,6 +58,9 @@ template <typename T> struct DevBuf {
     count = n;
     return cudaMemset(ptr, 0, n * sizeof(T));
   }
+  // at least n elements: the present allocation when it is large enough (its
+  // contents kept), else a new one
+  cudaError_t reserve(size_t n) { return (ptr && count >= n) ? cudaSuccess : alloc(n); }
   void release() {
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
@@ -428,6 +431,7 @@ void release_sim(sgdlm_engine *h) {
   h->part_b.release();
   h->draw_flags.release();
   h->pivot_list.release();
+  h->jac_list.release();
   h->sim_init = false;
   h->nsim = 0;
   h->nsim_batch = 0;
@@ -483,22 +487,25 @@ int alloc_sim(sgdlm_engine *h, size_t nsim) {
   LuPlan pl;
   int st = plan_sim(h, (long)nsim, &pl);
   if (st) return st;
-  release_sim(h);
+  // grow-only: a smaller draw count (e.g. forecasts of fewer draws between VB
+  // calls with more) keeps the allocations, so that alternating counts do not
+  // free and allocate gigabytes every call; every buffer is written before it
+  // is read within a call
   h->plan = pl;
   vb_chunking((long)nsim, (int)m, h->num_sms, &h->chunks, &h->chunk_draws);
-  CK(h->lambda.alloc(m * nsim * ts));
-  CK(h->theta.alloc(m * nsim * P * ts));
-  CK(h->theta_g.alloc(m * nsim * P * ts));
-  CK(h->lu_scratch.alloc(pl.scratch_elems_total * ts));
-  CK(h->logdet.alloc(nsim));
-  CK(h->w.alloc(nsim));
-  CK(h->y_fc.alloc(nsim * m));
-  CK(h->nu_fc.alloc(nsim * m));
-  CK(h->draw_flags.alloc(nsim));
-  CK(h->pivot_list.alloc(nsim + 1));
-  CK(h->jac_list.alloc(nsim + 1));
-  CK(h->part_a.alloc((size_t)h->chunks * m * (P + 2) + m * P));
-  CK(h->part_b.alloc((size_t)h->chunks * m * P * P));
+  CK(h->lambda.reserve(m * nsim * ts));
+  CK(h->theta.reserve(m * nsim * P * ts));
+  CK(h->theta_g.reserve(m * nsim * P * ts));
+  CK(h->lu_scratch.reserve(pl.scratch_elems_total * ts));
+  CK(h->logdet.reserve(nsim));
+  CK(h->w.reserve(nsim));
+  CK(h->y_fc.reserve(nsim * m));
+  CK(h->nu_fc.reserve(nsim * m));
+  CK(h->draw_flags.reserve(nsim));
+  CK(h->pivot_list.reserve(nsim + 1));
+  CK(h->jac_list.reserve(nsim + 1));
+  CK(h->part_a.reserve((size_t)h->chunks * m * (P + 2) + m * P));
+  CK(h->part_b.reserve((size_t)h->chunks * m * P * P));
   h->nsim = nsim;
   return SGDLM_OK;
 }

@@ -92,12 +92,14 @@ def vb_errors(vb, ref, p):
     return dict(mean_sd_units=em, cov_rel=ec, n_rel=en, s_rel=es)
 
 
-def bench_model(m, kmax, precision, seed_data, philox, T):
+def bench_model(m, kmax, precision, seed_data, philox, T, compat=None):
     import bench
+    from gpusgdlm_gb300 import _lib as L
 
     wl = bench.make_workload(m=m, kmax=kmax, T=T, seed=seed_data)
     P = wl["P"]
-    s = SGDLM(1, strict=True, precision=precision)
+    s = SGDLM(1, strict=True, precision=precision,
+              compat=L.COMPAT_REFERENCE if compat is None else compat)
     s.setSimultaneousParents(wl["p"], na_float(wl["sp"], m))
     s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
     a, R, r, c = bench.prior_arrays(m, P)
@@ -397,3 +399,77 @@ def test_m100_fp32_vs_fp64_T1000(built_lib):
     record("m100_T1000_mixed_vs_fp64_trajectory", mean_max_diff_sd_units=dmax,
            snapshots=len(runs["mixed"]))
     assert dmax < 0.5
+
+
+def test_c2_m400_50k_draws_forecasts_1_to_5(built_lib):
+    """The precision configuration at its stated sizes, over two steps after a
+    burn-in: m = 400, p_j <= 20, 50 000 IS draws per VB call and forecasts 1..5
+    steps ahead with 10 000 samples each (forecast draws evolved between the
+    steps, RcppWrapper.cpp:455-472).  The mixed form against the plain FP64 form
+    started from the same prior on the same Philox streams, so the two draw sets
+    differ by the FP32 rounding of the draws (about 1e-7 relative):
+      * VB posterior: means, C, s within 1e-4 (in the units of vb_errors); the
+        gamma shape n within 1e-3 relative: the refit's Newton solve for n sees
+        log E[lambda] - E[log lambda], of order 1/n, so its relative error is
+        about n times the draws' relative rounding;
+      * forecasts, per draw and horizon, normwise |y_mixed - y_fp64| / |y_fp64|
+        over the draws finite in both forms: median <= 1e-5 and at least 99 % of
+        the draws within 1e-3 (a gamma or beta acceptance decision that flips
+        between the precisions changes a draw completely; several-step draws
+        whose (I - Gamma) is nearly singular amplify the rounding).
+    Both engines use the corrected samplers (compat switches off): the reference's
+    beta sampler of the evolution (make_beta, kernel_functions.cuh:725-798)
+    applies Marsaglia-Tsang without the boost to shapes below one, which gives NaN
+    below 1/3; here the shape (1 - beta) r / 2 of some series falls there
+    (beta = 0.97, r about 20 after the burn-in), and every 2..5-step forecast draw
+    would be NaN, as the reference's would.
+    The FP64 form itself is pinned to the oracle by the parity tests."""
+    from gpusgdlm_gb300 import _lib as L
+
+    n_vb, n_fc, K = 50000, 10000, 5
+    s, wl = bench_model(400, 17, "mixed", 20261203, 1234, T=40, compat=L.COMPAT_NONE)
+    filter_steps(s, wl, 1, 31, 2000)
+    prior = s.getParameters()
+    seed, epoch = s.getRngState()
+    f = SGDLM(1, strict=True, precision="fp64", compat=L.COMPAT_NONE)
+    P, m = prior["m"].shape
+    f.setSimultaneousParents(wl["p"], na_float(wl["sp"], m))
+    f.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+    f.setPriorParameters(prior["m"], prior["C"], prior["n"], prior["s"])
+    f.setRngState(seed, epoch)
+    worst = dict(m=0.0, C=0.0, n=0.0, s=0.0)
+    horizons = {k: dict(median=0.0, within_1e3=1.0, finite=1.0) for k in range(1, K + 1)}
+    for t in (31, 32):
+        outs = {}
+        for name, e in (("mixed", s), ("fp64", f)):
+            e.computePosterior(wl["y"][t], wl["F_of"](t))
+            vb = e.computeVBPosterior(n_vb, n_vb)
+            if 1.0 / np.sum(vb["IS_weights"] ** 2) > n_vb / 2:
+                e.setPosteriorParameters(vb["m"], vb["C"], vb["n"], vb["s"])
+            e.computePrior()
+            F3 = np.stack([wl["F_of"](t + k, False) for k in range(1, K + 1)], axis=2)
+            y = e.computeForecast(n_fc, n_fc, F3)  # (m, n_fc, K)
+            outs[name] = (vb, y)
+        (vbm, ym), (vbf, yf) = outs["mixed"], outs["fp64"]
+        ve = vb_errors(vbm, vbf, wl["p"])
+        worst["m"] = max(worst["m"], ve["mean_sd_units"])
+        worst["C"] = max(worst["C"], ve["cov_rel"])
+        worst["n"] = max(worst["n"], ve["n_rel"])
+        worst["s"] = max(worst["s"], ve["s_rel"])
+        for k in range(1, K + 1):
+            a, b = ym[:, :, k - 1], yf[:, :, k - 1]
+            fin = np.all(np.isfinite(a), axis=0) & np.all(np.isfinite(b), axis=0)
+            rel = np.linalg.norm(a[:, fin] - b[:, fin], axis=0) / np.linalg.norm(b[:, fin], axis=0)
+            h = horizons[k]
+            h["finite"] = min(h["finite"], float(np.mean(fin)))
+            assert fin.any(), f"no forecast draw finite at horizon {k}"
+            h["median"] = max(h["median"], float(np.median(rel)))
+            h["within_1e3"] = min(h["within_1e3"], float(np.mean(rel <= 1e-3)))
+    s.close()
+    f.close()
+    record("c2_m400_50k_vb_draws_forecasts_1_to_5_mixed_vs_fp64", vb_draws=n_vb, forecast_draws=n_fc,
+           horizons={str(k): v for k, v in horizons.items()}, steps=[31, 32],
+           mean_sd_units=worst["m"], cov_rel=worst["C"], n_rel=worst["n"], s_rel=worst["s"])
+    assert max(worst["m"], worst["C"], worst["s"]) <= 1e-4 and worst["n"] <= 1e-3
+    for h in horizons.values():
+        assert h["median"] <= 1e-5 and h["within_1e3"] >= 0.99
