@@ -188,6 +188,43 @@ def test_multistep_forecast_matches_oracle(built_lib, golden, precision, compat)
     assert s.getRngState()[1] == epoch + 5
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_multistep_forecast_block_lu_matches_oracle(built_lib, precision):
+    """K = 3 step forecasts at m = 96, above the warp-per-draw LU's m <= 32: the
+    draws' Gamma entries reach the block LU and the iterative solve through the
+    sampler's and the evolution's draw-major Gamma copy.  Corrected samplers
+    (compat 0), an informative posterior (so most draws take the fast path and
+    the iterative solve), against the oracle on the same streams."""
+    import bench
+
+    wl = bench.make_workload(m=96, kmax=10, T=4, seed=777)
+    m, P = wl["m"], wl["P"]
+    rng = np.random.default_rng(5)
+    mt = np.asfortranarray(rng.normal(0.0, 0.05, (P, m)))
+    Ct = np.asfortranarray(np.repeat((1e-3 * np.eye(P))[:, :, None], m, axis=2))
+    nt, st = np.full(m, 50.0), np.full(m, 0.0025)
+    n, seed, epoch = 256, 31, 2
+    x3 = np.asfortranarray(np.stack([wl["F_of"](1 + k, False) for k in range(3)], axis=2))
+    s = SGDLM(1, strict=True, precision=precision)
+    s.setCompat(0)
+    s.setSimultaneousParents(wl["p"], na_sp(wl["sp"], m))
+    s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+    s.setRngState(seed, epoch)
+    s.setPosteriorParameters(mt, Ct, nt, st)
+    s.computePrior()
+    y = s.computeForecast(n, n, x3)
+    s.close()
+    o = OracleSGDLM(wl["p"], wl["sp"], np.full(m, 0.97), np.full((P, P, m), 0.98), seed=seed,
+                    epoch=epoch, compat=0)
+    o.set_parameters(mt, Ct, nt, st)
+    o.prior()
+    yo = o.forecast(n, x3)
+    assert y.shape == (m, n, 3)
+    assert np.isfinite(y).all() and np.isfinite(yo).all()
+    rtol, atol = (1e-8, 1e-10) if precision == "fp64" else (2e-3, 2e-4)
+    np.testing.assert_allclose(y, yo, rtol=rtol, atol=atol)
+
+
 def test_evo_prior_matches_reference(built_lib, golden):
     """computeEvoPrior against the reference's kernels (fixture m20_evo): a = G m and
     R = G R G' with the reference's cut-offs, FP64."""
