@@ -1574,7 +1574,7 @@ __device__ __forceinline__ void run_levels(const EliminationPlan &ep, T *vals, T
 }
 
 // The dense core (d_p x d_p, column-major) from the value slots through the
-// plan's slot map: four cells per 8-byte map word pair, eight pairs in flight
+// plan's slot map: four 16-bit slots per 8-byte word of the map, eight words in flight
 // per thread.
 template <typename T>
 __device__ __forceinline__ void scatter_core(const EliminationPlan &ep, int dp, const T *vals,
