@@ -168,7 +168,24 @@ struct Smem {
 // diagonal block, the FP64 forecast vectors and the node-indexed vectors of the
 // levels' solve programs.
 constexpr int kFbChunk = 128;
-constexpr int kFbRefine = 3;  // refinement steps of the pivoting pass's forecast solves
+constexpr int kFbRefine = 3;  // refinement steps of the pivoting pass's forecast solves, at most
+// ... fewer once a correction is below this fraction of the solution (FP32
+// resolution: a further step could only re-round the result)
+constexpr double kFbRefineStop = 1e-7;
+// Whether a refinement correction dv is below kFbRefineStop of the solution yv
+// over the first m entries (uniform over the block: block_max2 ends on a barrier
+// and every thread reads the same maxima; a NaN counts as not done).
+template <typename T>
+__device__ bool refine_done(int m, const T *dv, const T *yv, double *red) {
+  double dmax = 0.0, ymax = 0.0;
+  for (int r = threadIdx.x; r < m; r += blockDim.x) {
+    const double ad = fabs((double)dv[r]), ay = fabs((double)yv[r]);
+    dmax = (ad == ad && ad > dmax) ? ad : ((ad == ad) ? dmax : INFINITY);
+    ymax = (ay == ay && ay > ymax) ? ay : ((ay == ay) ? ymax : INFINITY);
+  }
+  block_max2(dmax, ymax, red);
+  return ymax < INFINITY && dmax <= kFbRefineStop * ymax;
+}
 // the redo eliminates the sparse levels unpivoted unless a multiplier exceeds this
 // (then it pivots over the full matrix)
 constexpr double kLevelMultMax = 65536.0;
@@ -2618,9 +2635,10 @@ __global__ void __launch_bounds__(kThreads)
         for (int r = tid; r < ep.core_n; r += blockDim.x) yf[ep.core_node[r]] = b.z[r];
         __syncthreads();
         levels_backward<T>(ep, vals, zf, yf);
-        // the draws that reach this pass are the ill-conditioned ones: refine
-        // kFbRefine times (FP64 residual of the working-precision solution),
-        // which recovers working-precision accuracy while cond * eps < 1
+        // the draws that reach this pass are the ill-conditioned ones: refine up
+        // to kFbRefine times (FP64 residual of the working-precision solution),
+        // which recovers working-precision accuracy while cond * eps < 1; stop
+        // once the correction is below kFbRefineStop of the solution
         for (int it = 0; it < kFbRefine; ++it) {
           if (it > 0) {
             for (int r = tid; r < m; r += blockDim.x) yf[r] += yd[r];
@@ -2640,6 +2658,7 @@ __global__ void __launch_bounds__(kThreads)
           for (int r = tid; r < ep.core_n; r += blockDim.x) yd[ep.core_node[r]] = d[r];
           __syncthreads();
           levels_backward<T>(ep, vals, zf, yd);
+          if (it + 1 < kFbRefine && refine_done<T>(m, yd, yf, red)) break;
         }
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)yf[r] + (double)yd[r];
@@ -2656,6 +2675,7 @@ __global__ void __launch_bounds__(kThreads)
           __syncthreads();
           block_forward_solve<T>(F, N, d, D);
           block_back_solve<T>(F, N, d, D);
+          if (it + 1 < kFbRefine && refine_done<T>(m, d, b.z, red)) break;
         }
         for (int r = tid; r < m; r += blockDim.x)
           y[(size_t)i * m + r] = (double)b.z[r] + (double)d[r];
