@@ -107,7 +107,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "25"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except FileNotFoundError:
@@ -116,6 +116,15 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.rows.append([c.strip() for c in line.split(",")])
+
+    def ready(self, timeout=3.0):
+        """Waits for nvidia-smi's first sample (its start-up takes longer than a
+        short timed region), then forgets the samples taken so far, so that the
+        ones kept are those of the region that follows."""
+        t_end = time.time() + timeout
+        while self.proc and not self.rows and time.time() < t_end:
+            time.sleep(0.01)
+        self.rows = []
 
     def stop(self):
         if self.proc:
@@ -194,6 +203,7 @@ def run_gpu(args, rank, world):
     barrier(world)
     clocks = ClockSampler(local)
     clocks.start()
+    clocks.ready()
     launches0 = s.launchCount()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
