@@ -409,6 +409,47 @@ def test_ragged_draw_counts(built_lib, golden, n):
     np.testing.assert_allclose(vb["sum_det_weights"], sw, rtol=1e-9)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_draw_buffers_kept_across_smaller_counts(built_lib, precision):
+    """The per-draw buffers only grow: a call with fewer draws after one with more
+    reuses the larger allocations (their old contents included) and must give
+    bit for bit what a freshly allocated engine gives (m = 96: block LU, iterative
+    forecast solve, the draw-major Gamma copy)."""
+    import bench
+
+    wl = bench.make_workload(m=96, kmax=10, T=4, seed=778)
+    m, P = wl["m"], wl["P"]
+    rng = np.random.default_rng(6)
+    mt = np.asfortranarray(rng.normal(0.0, 0.05, (P, m)))
+    Ct = np.asfortranarray(np.repeat((1e-3 * np.eye(P))[:, :, None], m, axis=2))
+    nt, st = np.full(m, 50.0), np.full(m, 0.0025)
+    x = wl["F_of"](2, False)
+
+    def run(first):
+        s = SGDLM(1, strict=True, precision=precision)
+        s.setSimultaneousParents(wl["p"], na_sp(wl["sp"], m))
+        s.setDiscountFactors(np.full(m, 0.97), np.full((P, P, m), 0.98))
+        if first:
+            s.setRngState(99, 0)
+            s.setPosteriorParameters(mt, Ct, nt, st)
+            s.computeVBPosterior(first, first)   # allocates for `first` draws
+            s.computePrior()
+            s.computeForecast(first, first, x)
+        s.setRngState(31, 3)
+        s.setPosteriorParameters(mt, Ct, nt, st)
+        vb = s.computeVBPosterior(700, 700)
+        s.computePrior()
+        y = s.computeForecast(300, 300, x)
+        s.close()
+        return vb, y
+
+    vb0, y0 = run(0)
+    vb1, y1 = run(5000)
+    for k in ("m", "C", "n", "s", "IS_weights"):
+        np.testing.assert_array_equal(vb1[k], vb0[k])
+    np.testing.assert_array_equal(y1, y0)
+
+
 def test_single_series_and_empty_predictors(built_lib):
     """m = 1 with no parents, and a series with p_j = 0."""
     s = SGDLM(1, strict=True, precision="fp64")
